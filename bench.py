@@ -1,0 +1,410 @@
+#!/usr/bin/env python
+"""Benchmark of the time-domain FDTD hot path on GB300.
+
+Workload (default): the 2D TMz configuration -- 4096 x 4096 cells (dr 2 nm), periodic x / CPML y,
+a perforated 40 nm Drude silver film, 1e4 two-level emitters (FP64 density matrices) 10 nm above
+it, a Gaussian 3.0 eV line source and 16 point detectors sampled every step.  One "step" is one
+full time step of the reference's loop (H update, sources, E update with ADE and emitter current,
+emitter gather/propagate/scatter, detector sampling).
+
+  value        Gcell-updates/s of the chosen FP32 fused path, device-timed (CUDA events on the
+               library's stream) over K steps run by the device-side loop (CUDA graph).
+  e2e          the same metric through the reference-facing C-ABI call sequence (per-step calls,
+               per-step host->device step scalars and device->host detector samples).
+  plain_fp64   the plain FP64 path on the same workload (the speed-up reference) and the FP32
+               path's stated error against it (detector fields, emitter dipoles).
+  roofline     dominant kernel: algorithmic bytes per launch / mean launch duration (CUDA events).
+  cpu_baseline the FP64 CPU oracle (restatement of the reference) on the same workload, a
+               bounded sample of steps with all host threads.
+
+--impl reference runs the CPU restatement of the reference on the host cores (the reference
+itself is Fortran with an external DFTB+ dependency and no Fortran compiler exists in this image).
+--gpus N (torchrun, one process per GPU): independent replicas, weak scaling.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "one-mxll-to-rule-them-all_gb300")
+sys.path.insert(0, PKG)
+
+METRIC = "Gcell-updates/s & emitter-steps/s, chosen vs plain form, at stated field error"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=300)
+    p.add_argument("--warmup", type=int, default=10)
+    p.add_argument("--impl", default="omx", choices=["omx", "reference"])
+    p.add_argument("--config", default="cfg2", choices=["cfg1", "cfg2", "cfg3"])
+    p.add_argument("--cpu-seconds", type=float, default=12.0)
+    p.add_argument("--skip-plain", action="store_true")
+    return p.parse_args()
+
+
+# ---------------------------------------------------------------------------------- distributed
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo", rank=self.rank, world_size=self.world)
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, x):
+        if not self.pg:
+            return x
+        import torch
+
+        t = torch.tensor([float(x)], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi samples (200 ms) during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------------- workload
+def make_deck(cfg):
+    from omx import decks
+
+    if cfg == "cfg1":
+        return decks.deck_cfg1(), "cfg1: 3D 128^3 dr 2 nm, 10-cell CPML, Drude-Lorentz Au sphere r 20 nm, " \
+                                  "x-polarised 2.2 eV plane-wave soft source, 16 point detectors"
+    if cfg == "cfg3":
+        return decks.deck_cfg3(), "cfg3: 3D 512^3 dr 1 nm, 10-cell CPML, 4x4 Au nanorod dimers, 1e5 three-level " \
+                                  "emitters in the gaps, chirped 1.8-2.6 eV drive, 16 point detectors"
+    return decks.deck_cfg2(), "cfg2: 2D TMz 4096x4096 dr 2 nm, periodic x / CPML y, 40 nm Drude Ag film with " \
+                              "150 nm holes at 400 nm pitch, 1e4 two-level emitters, 3.0 eV source, 16 point detectors"
+
+
+def build_gpu(deck, precision):
+    import omx
+    from omx import decks
+
+    g = omx.TMxll(deck["dimensions"], deck["grid_Ndims"], deck["npml"], deck["boundaries"], deck["dt"], deck["dr"],
+                  mode=deck["mode"], precision=precision)
+    mm = decks.media_map(deck, omx.media_map_from_voxels)
+    groups = decks.apply_deck(g, deck, omx, mm)
+    for det in deck["detectors"]:
+        g.add_detector(det["type"], det["field"], det["idx"])
+    return g, groups
+
+
+def cells_of(deck):
+    n = 1
+    for v in deck["grid_Ndims"]:
+        n *= v
+    return n
+
+
+def n_emitters(deck):
+    return sum(len(g["cells"]) for g in deck["groups"])
+
+
+class Loop:
+    """The reference's loop state (mxim_mxll.f90:92-104) for the per-call drive."""
+
+    def __init__(self, deck):
+        self.deck = deck
+        self.tq_old = 0
+        self.t_skip = 0.0
+
+    def step(self, target, groups, tt):
+        d = self.deck
+        time_ = d["dt"] * (tt - 0.5)
+        tt_0 = 1 if d["n_skip"] == 1 else 0
+        tq = 1 + (tt - tt_0) // d["n_skip"]
+        move = False
+        if tq > self.tq_old:
+            self.t_skip, self.tq_old, move = time_, tq, len(groups) > 0
+        target.td_propagate_H_field()
+        target.source_interactions(time_)
+        target.td_propagate_E_field(time_, self.t_skip)
+        if move:
+            for g in groups:
+                target.q_group_step(g, tq)
+        return time_
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def rel_err(a, b):
+    import numpy as np
+
+    scale = np.maximum(np.max(np.abs(b), axis=0), 1e-300)
+    return float(np.max(np.abs(a - b) / scale))
+
+
+# ---------------------------------------------------------------------------------- CPU leg
+def cpu_run(deck, seconds, max_steps=None):
+    """The FP64 oracle (CPU restatement of the reference) stepping the same workload."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import build_oracle
+
+    build_oracle.build()
+    import omx
+    import oracle as orc
+    from omx import decks
+    from gpu_harness import OracleFactory
+
+    g = orc.Grid(deck["dimensions"], deck["grid_Ndims"], deck["npml"], deck["boundaries"], deck["dt"], deck["dr"],
+                 mode=deck["mode"])
+    mm = decks.media_map(deck, omx.media_map_from_voxels)
+    groups = decks.apply_deck(g, deck, OracleFactory(orc), mm)
+    loop = Loop(deck)
+    loop.step(g, groups, 1)            # first step outside the clock
+    n, t0 = 0, time.perf_counter()
+    while True:
+        loop.step(g, groups, 2 + n)
+        for det in deck["detectors"]:
+            g.sample(det["type"], det["field"], det["idx"])
+        n += 1
+        el = time.perf_counter() - t0
+        if (el >= seconds and n >= 2) or (max_steps and n >= max_steps):
+            break
+    return n, el, orc.lib().orc_num_threads()
+
+
+def reference_arm(args, dist):
+    if dist.rank != 0:
+        return
+    deck, desc = make_deck(args.config)
+    cells = cells_of(deck)
+    # W warm-up steps and K timed steps of the CPU restatement, each bounded: the whole run is
+    # sized to finish within a few minutes (about 2 s per timed step at most).
+    per_step_budget = 2.0
+    n, el, cores = cpu_run(deck, seconds=min(per_step_budget * args.steps, 150.0), max_steps=args.steps)
+    v = cells * n / el / 1e9
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "Gcell-updates/s", "n_gpus": 0,
+            "steps": n, "warmup": 1, "ms_per_step": el / n * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": desc, "cells": cells, "emitters": n_emitters(deck)},
+            "cpu_baseline": {"value": v, "unit": "Gcell-updates/s", "cores": cores, "kind": "port",
+                             "sample": f"{n} steps of the full workload (FP64 oracle restating the reference)"},
+            "e2e": {"value": v, "unit": "Gcell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------------- GPU arm
+def gpu_arm(args, dist):
+    import numpy as np
+
+    import omx
+
+    if dist.world > 1:
+        omx.select_device(dist.local_rank % max(1, omx.device_count()))
+    deck, desc = make_deck(args.config)
+    cells = cells_of(deck)
+    ne = n_emitters(deck)
+    K, W = args.steps, max(3, args.warmup)
+    tdp = deck["t_det_print"]
+
+    # ---- chosen path: FP32 fused, device loop in a CUDA graph ------------------------------
+    gpu, groups = build_gpu(deck, "fp32")
+    gpu.run(1, W, deck["n_skip"], tdp, use_graph=True)
+    gpu.synchronize()
+    dist.barrier()
+    clocks = ClockSampler(dist.local_rank)
+    clocks.start()
+    l0 = gpu.launch_count()
+    gpu.timer_start()
+    gpu.run(1 + W, K, deck["n_skip"], tdp, use_graph=True)
+    ms = gpu.timer_stop()
+    launches = gpu.launch_count() - l0
+    clk = clocks.stop()
+    dist.barrier()
+    ms_max = dist.max(ms)
+    value = dist.world * cells * K / (ms_max / 1e3) / 1e9
+    emitter_rate = dist.world * ne * K / (ms_max / 1e3)
+    _, rec32 = gpu.drain_detectors()
+    dip32 = groups[0].read()["dipole"] if groups else None
+
+    # ---- per-kernel durations (events around every launch), same K steps ----------------
+    gpu.profile(True)
+    gpu.run(1 + W + K, K, deck["n_skip"], tdp, use_graph=False)
+    gpu.synchronize()
+    per = {}
+    for kc, name in ((omx.KC_H, "H"), (omx.KC_E, "E"), (omx.KC_EMIT, "emitters"), (omx.KC_SRC, "sources"),
+                     (omx.KC_DET, "detectors")):
+        t, n = gpu.profile_query(kc)
+        per[name] = {"ms_total": t, "launches": n, "us_per_launch": (t / n * 1e3) if n else None}
+    gpu.profile(False)
+    gpu.drain_detectors()
+    dom = max(("H", "E"), key=lambda k: per[k]["ms_total"])
+    kc_dom = omx.KC_H if dom == "H" else omx.KC_E
+    alg_bytes = gpu.algorithmic_bytes(kc_dom)
+    avg_s = per[dom]["ms_total"] / per[dom]["launches"] / 1e3
+    peak, peak_kind = peaks()
+    achieved = alg_bytes / avg_s / 1e9
+    gpu.kill()
+
+    # ---- end to end through the reference-facing C-ABI calls ------------------------------
+    e2e_gpu, e2e_groups = build_gpu(deck, "fp32")
+    loop = Loop(deck)
+    npts = sum(len(d["idx"]) for d in deck["detectors"])
+    for tt in range(1, W + 1):
+        t_ = loop.step(e2e_gpu, e2e_groups, tt)
+        e2e_gpu.write_detectors_outputs(t_)
+        e2e_gpu.drain_detectors(max_records=1)
+    e2e_gpu.synchronize()
+    dist.barrier()
+    t0 = time.perf_counter()
+    for tt in range(W + 1, W + K + 1):
+        t_ = loop.step(e2e_gpu, e2e_groups, tt)
+        e2e_gpu.write_detectors_outputs(t_)
+        e2e_gpu.drain_detectors(max_records=1)         # device->host read of the step's samples
+    e2e_gpu.synchronize()
+    e2e_s = dist.max(time.perf_counter() - t0)
+    e2e_value = dist.world * cells * K / e2e_s / 1e9
+    e2e_gpu.kill()
+
+    # ---- plain FP64 path on the same workload; stated FP32 error against it --------------
+    plain = None
+    if not args.skip_plain:
+        g64, groups64 = build_gpu(deck, "fp64")
+        g64.run(1, W, deck["n_skip"], tdp, use_graph=True)
+        g64.synchronize()
+        g64.timer_start()
+        g64.run(1 + W, K, deck["n_skip"], tdp, use_graph=True)
+        ms64 = dist.max(g64.timer_stop())
+        _, rec64 = g64.drain_detectors()
+        dip64 = groups64[0].read()["dipole"] if groups64 else None
+        v64 = dist.world * cells * K / (ms64 / 1e3) / 1e9
+        field_err = rel_err(rec32, rec64) if len(rec64) == len(rec32) else None
+        dip_err = None
+        if dip64 is not None:
+            dip_err = float(np.max(np.abs(dip32 - dip64)) / max(np.max(np.abs(dip64)), 1e-300))
+        plain = {"value": v64, "unit": "Gcell-updates/s", "ms_per_step": ms64 / K,
+                 "emitter_steps_per_s": dist.world * ne * K / (ms64 / 1e3),
+                 "speedup_fp32_over_fp64": value / v64,
+                 "fp32_max_rel_detector_error": field_err, "fp32_max_rel_dipole_error": dip_err,
+                 "error_window_steps": W + K}
+        g64.kill()
+
+    # ---- CPU baseline: bounded sample of the oracle on rank 0 --------------------------------
+    cpu = None
+    if dist.rank == 0:
+        n, el, cores = cpu_run(deck, seconds=args.cpu_seconds)
+        cpu = {"value": cells * n / el / 1e9, "unit": "Gcell-updates/s", "cores": cores, "kind": "port",
+               "sample": f"{n} full steps of the same workload, FP64 oracle (C restatement of the reference, "
+                         f"OpenMP on the bulk loops as in the reference)"}
+
+    if dist.rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "Gcell-updates/s", "n_gpus": dist.world, "steps": K,
+            "warmup": W, "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded deck of the configuration's shape)",
+            "config": {"workload": desc, "cells": cells, "emitters": ne, "precision": "fp32 fields, fp64 emitters",
+                       "parallelism": f"replicas x{dist.world}" if dist.world > 1 else "single GPU",
+                       "l2": "working set %.0f MB > 126 MB L2, no flush" % (cells * 3 * 4 / 1e6),
+                       "loop": "device-side loop captured in a CUDA graph, one graph launch per step"},
+            "emitter_steps_per_s": emitter_rate,
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
+                         "algorithmic_bytes_per_launch": alg_bytes},
+            "kernels": per,
+            "plain_fp64": plain,
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": "Gcell-updates/s", "h2d_bytes_per_step": 8 * (4 + len(deck["sources"]) + len(deck["plane_sources"])),
+                    "d2h_bytes_per_step": 8 * (npts + 1),
+                    "how": "per-step C-ABI calls (H, sources, E, q-group, detector sample) + per-step drain"},
+            "gpu_launches": launches,
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            reference_arm(args, dist)
+        else:
+            gpu_arm(args, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

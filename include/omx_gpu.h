@@ -1,0 +1,247 @@
+/*
+ * omx_gpu.h -- C-ABI of the GB300 (sm_103a) library for OMxRTA's time-domain hot path.
+ *
+ * The entry points replace the bodies behind the reference's plugin interfaces
+ * (paths relative to the reference project root):
+ *   TMxll        src/FDTD/mxll_base_mod.f90:7-69   (init / kill / td_propagate_H_field /
+ *                                                   td_propagate_E_field)
+ *   TQ_sys_base  src/FDTD/q_sys_base_mod.f90:7-71  (td_propagate, batched per q-group)
+ *   free routines called by the driver src/FDTD/mxim_mxll.f90:107-126:
+ *                source_interactions, send_E_to_J_ranks, td_propagate_q_group,
+ *                send_J_to_E_ranks, write_detectors_outputs (sampling only).
+ *
+ * Conventions
+ *   - Every call returns an int status (OMX_OK == 0).  The reference stops the program
+ *     on errors; a Fortran caller maps a non-zero status to `error stop`.
+ *   - All device memory is owned by the library; callers pass host pointers.
+ *   - Array arguments use the reference's Fortran layout (column-major, first index
+ *     fastest) and the reference's array bounds, so a Fortran caller passes its own
+ *     arrays unchanged.
+ *   - Units are atomic units, as inside the reference after its input conversion.
+ *   - One host thread per context; calls on one context are not re-entrant.
+ *   - There is no CPU fallback: omx_create fails when no CUDA device is usable.
+ */
+#ifndef OMX_GPU_H
+#define OMX_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------------------------- */
+#define OMX_OK 0
+#define OMX_ERR_ARG 1      /* invalid argument or unsupported combination */
+#define OMX_ERR_CUDA 2     /* CUDA runtime error (message in omx_last_error) */
+#define OMX_ERR_STATE 3    /* call out of order (e.g. media after the first step) */
+#define OMX_ERR_NOMEM 4    /* device allocation failed */
+#define OMX_ERR_NODEV 5    /* no usable CUDA device */
+
+/* ---- enum codes: identical to constants_mod.f90:52-105 ----------------------------------- */
+#define OMX_CLOSE_BOUNDARIES 1
+#define OMX_PERIODIC_BOUNDARIES 2
+#define OMX_CPML_BOUNDARIES 3
+
+#define OMX_TMZ_2D_MODE 1
+#define OMX_TEZ_2D_MODE 2
+
+#define OMX_NONE_MEDIUM 0
+#define OMX_DIELECTRIC_MEDIUM 1
+#define OMX_DRUDE_MEDIUM 2
+#define OMX_DL_MEDIUM 3
+
+#define OMX_EX_FIELD 1
+#define OMX_EY_FIELD 2
+#define OMX_EZ_FIELD 3
+#define OMX_HX_FIELD 4
+#define OMX_HY_FIELD 5
+#define OMX_HZ_FIELD 6
+
+#define OMX_POINT_DETECTOR 1
+#define OMX_LINE_X_DETECTOR 2
+#define OMX_LINE_Y_DETECTOR 3
+#define OMX_LINE_Z_DETECTOR 4
+#define OMX_PLANE_XY_DETECTOR 5
+#define OMX_PLANE_YZ_DETECTOR 6
+#define OMX_PLANE_ZX_DETECTOR 7
+#define OMX_VOLUME_DETECTOR 8
+
+#define OMX_Q_MATERIAL 1
+#define OMX_Q_SINGLE 2
+
+/* ---- library-specific codes ---------------------------------------------------------------- */
+#define OMX_PREC_FP64 0    /* plain FP64 path: reference arithmetic, no FMA contraction */
+#define OMX_PREC_FP32 1    /* fused FP32 path: FP32 state, FP64-precomputed coefficients */
+
+#define OMX_EMITTER_TWO_LEVEL 1    /* params: w0, mu, T1, T2, ux, uy, uz           (7) */
+#define OMX_EMITTER_THREE_LEVEL 2  /* params: e1, e2, mu1, mu2, T1, T2, ux, uy, uz (9) */
+
+#define OMX_MAX_POLES 8
+
+typedef struct omx_ctx omx_ctx;
+
+/* TMxll%init arguments (mxll_base_mod.f90:41-57) plus the precision of the GPU path. */
+typedef struct {
+    int    dimensions;     /* 1, 2 or 3 */
+    int    grid_Ndims[3];  /* cells per axis (1D: grid_Ndims[0] is the only axis) */
+    int    npml;           /* CPML thickness in cells (>= 2 when any axis is CPML) */
+    int    boundaries[3];  /* OMX_*_BOUNDARIES per axis */
+    int    mode;           /* 2D only: OMX_TMZ_2D_MODE or OMX_TEZ_2D_MODE */
+    int    precision;      /* OMX_PREC_FP64 or OMX_PREC_FP32 */
+    double dt;             /* a.u. */
+    double dr;             /* a.u. */
+} omx_grid_desc;
+
+/* TClassicalMedium coefficients (classical_medium_mod.f90:6-37). */
+typedef struct {
+    int    medium_type;    /* OMX_*_MEDIUM */
+    int    n_poles;        /* Drude-Lorentz poles (<= OMX_MAX_POLES) */
+    double eps_r;
+    double A1, A2, C1, C2, C3, C4;
+    double alpha_k[OMX_MAX_POLES], beta_k[OMX_MAX_POLES], gamma_k[OMX_MAX_POLES];
+    double B1_k[OMX_MAX_POLES], B2_k[OMX_MAX_POLES];
+} omx_medium;
+
+/* TSource (source_mod.f90:7-27), values in a.u. */
+typedef struct {
+    char   dir;            /* 'x', 'y' or 'z' */
+    double j_amp, w0, t0, tau, t_init, t_final, phase;
+    double r0[3];
+    double radius;
+    double chirp;          /* extension, d(omega)/dt in a.u.; 0 reproduces the reference */
+} omx_source_desc;
+
+/* Plane-wave soft source (extension; no reference counterpart). */
+typedef struct {
+    int    comp;           /* 1..3: E component driven */
+    int    plane_axis;     /* 1..3 */
+    int    plane_index;    /* 1-based cell index along plane_axis */
+    double j_amp, w0, t0, tau, t_init, t_final, phase, chirp;
+} omx_plane_source_desc;
+
+/* TQ_group (q_group_mod.f90:12-28) with a few-level emitter model behind TQ_sys_base. */
+typedef struct {
+    int    group_type;     /* OMX_Q_MATERIAL or OMX_Q_SINGLE */
+    int    model;          /* OMX_EMITTER_* */
+    int    n_systems;
+    double density;        /* q_group%density, a.u. */
+    double dt;             /* q_group%dt (= n_skip_steps * dt) */
+} omx_qgroup_desc;
+
+/* ---- device selection ------------------------------------------------------------------------ */
+/* Make `device` current for this host thread; contexts created afterwards live on it.  One
+ * process per GPU (the reference's one-rank-per-process model) calls this once at start. */
+int omx_select_device(int device);
+int omx_device_count(int *count);
+
+/* ---- context (TMxll%init / TMxll%kill) ---------------------------------------------------- */
+/* init_{1,2,3}Dgrid: mxll_1D_mod.f90:53, mxll_2D_mod.f90:59, mxll_3D_mod.f90:63.  Computes the
+ * CPML tables and den_* arrays exactly as the reference does and zeroes every field. */
+int omx_create(const omx_grid_desc *desc, omx_ctx **out);
+/* kill_{1,2,3}Dgrid: mxll_3D_mod.f90:435 */
+int omx_destroy(omx_ctx *ctx);
+const char *omx_last_error(const omx_ctx *ctx);   /* never NULL; ctx may be NULL */
+int omx_synchronize(omx_ctx *ctx);
+
+/* CPML tables as computed at create (be,ce[npml]; bh,ch[npml-1]); den arrays per axis. */
+int omx_get_cpml_tables(const omx_ctx *ctx, double *be, double *ce, double *bh, double *ch);
+int omx_get_den(const omx_ctx *ctx, int axis, double *den_e, double *den_h); /* axis 1..3 */
+/* Host-only restatement of the CPML grading (mxll_3D_mod.f90:282-318) for a given npml, dr, dt:
+ * be,ce,kappae[npml]; bh,ch,kappah[npml-1].  Needs no device. */
+int omx_compute_cpml_tables(int npml, double dr, double dt, double *be, double *ce, double *bh,
+                            double *ch, double *kappae, double *kappah);
+/* Override the tables, e.g. with the Fortran caller's own arrays (same layout as get). */
+int omx_set_cpml_tables(omx_ctx *ctx, const double *be, const double *ce, const double *bh,
+                        const double *ch, const double *den_e_x, const double *den_e_y,
+                        const double *den_e_z, const double *den_h_x, const double *den_h_y,
+                        const double *den_h_z);
+
+/* ---- media (read_init_media_* results; classical_medium_mod.f90:203-769) ------------------- */
+/* media[0..n_media-1] describe media 1..n_media.  media_map is the reference's integer array:
+ * 3D (nx,ny,nz,3), 2D (nx,ny,3), 1D (nz).  eps_{x,y,z} are the inverse-permittivity arrays
+ * (nx,ny,nz) of the reference; pass NULL to derive them from media_map with the reference's
+ * rule.  Must precede the first step. */
+int omx_set_media(omx_ctx *ctx, int n_media, const omx_medium *media, const int32_t *media_map,
+                  const double *eps_x, const double *eps_y, const double *eps_z);
+
+/* Host helpers restating init_classical_medium (classical_medium_mod.f90:46-104). */
+int omx_medium_dielectric(double eps_r, omx_medium *m);
+int omx_medium_drude(double omegaD, double GammaD, double eps_r, double dt, omx_medium *m);
+int omx_medium_dl_library(const char *material, double eps_r, double dt, omx_medium *m);
+int omx_medium_dl_custom(double eps_inf, double wp_ev, double gamma_ev, int n_poles,
+                         const double *pole_ev, const double *strength, const double *width_ev,
+                         double dt, omx_medium *m);   /* extension: A_k = f_k * wp^2 */
+/* read_init_media_{1D,2D,3D} voxel rule (file I/O left to the caller): n_vox[m] voxels of
+ * medium m+1, coordinates in nm (dims per voxel), media_map out as documented above. */
+int omx_media_map_from_voxels(int dimensions, const int grid_Ndims[3], double dr, int n_media,
+                              const int *n_vox, const double *vox_nm, int32_t *media_map);
+
+/* ---- time stepping (TMxll%td_propagate_*) --------------------------------------------------- */
+int omx_step_H(omx_ctx *ctx);                                  /* td_propagate_H_field */
+int omx_step_E(omx_ctx *ctx, double time, double t_skip);      /* td_propagate_E_field */
+
+/* ---- sources (source_mod.f90 / interactions_mod.f90:21-163) -------------------------------- */
+int omx_source_add(omx_ctx *ctx, const omx_source_desc *d, int *source_id);  /* init_source */
+int omx_plane_source_add(omx_ctx *ctx, const omx_plane_source_desc *d, int *source_id);
+/* update_sources + source_interactions for every registered source at `time`. */
+int omx_source_interactions(omx_ctx *ctx, double time);
+
+/* ---- emitters (q_group_mod.f90, interactions_mod.f90:167-1220) ------------------------------ */
+/* cell: n_systems x dimensions, 1-based local cell indices (q_group%map(:,3:5));
+ * params: n_systems x (7 | 9) per the model. */
+int omx_qgroup_create(omx_ctx *ctx, const omx_qgroup_desc *d, const int32_t *cell,
+                      const double *params, int *group_id);
+/* send_E_to_J_ranks + td_propagate_q_group + send_J_to_E_ranks for one group */
+int omx_qgroup_step(omx_ctx *ctx, int group_id, int tq_step);
+/* dipole, dPt_dt, E (n x 3 each, any may be NULL); rho (n x state) may be NULL */
+int omx_qgroup_read(omx_ctx *ctx, int group_id, double *dipole, double *dPt_dt, double *efield,
+                    double *rho);
+int omx_qgroup_state_size(int model);
+
+/* ---- detectors (write_fields_subs_mod.f90 sampling stencils) ------------------------------- */
+/* indx_list: nd x dimensions (TDetector%indx_list, detector_mod.f90:21) */
+int omx_detector_add(omx_ctx *ctx, int detector_type, int field, int nd, const int32_t *indx_list,
+                     int *detector_id);
+int omx_detectors_total_points(const omx_ctx *ctx);
+/* sample every detector now into the device record buffer (capacity set here, default 1) */
+int omx_detectors_set_capacity(omx_ctx *ctx, int records);
+int omx_detectors_record(omx_ctx *ctx, double time);
+/* copy out and clear the recorded samples: times[n_rec], values[n_rec x total_points] */
+int omx_detectors_drain(omx_ctx *ctx, double *times, double *values, int max_records,
+                        int *n_records);
+
+/* ---- whole driver loop on the device (mxim_mxll.f90:92-132) --------------------------------- */
+/* Runs steps tt = tt0 .. tt0+nsteps-1 with the reference's ordering: H, sources, E, q-groups
+ * on q-steps, detector records every t_det_print steps (0 disables).  n_skip_steps as in
+ * mxim_mxll.f90:73-83.  use_graph != 0 captures the step sequence in a CUDA graph. */
+int omx_run(omx_ctx *ctx, int tt0, int nsteps, int n_skip_steps, int t_det_print, int use_graph);
+
+/* ---- field access (debug / parity) ---------------------------------------------------------- */
+/* Copies a field over the reference's bounds (e.g. 3D Ex(0:nx,1:ny+1,1:nz+1)) to/from host
+ * FP64.  Ghost planes of periodic axes are implicit on the device and read back as zero. */
+int omx_field_bounds(const omx_ctx *ctx, int field, int lo[3], int hi[3]);
+int omx_read_field(omx_ctx *ctx, int field, double *host);
+int omx_write_field(omx_ctx *ctx, int field, const double *host);
+
+/* ---- measurement ------------------------------------------------------------------------------ */
+/* Per-kernel timing with CUDA events on the context's stream: enable, run, then query the
+ * accumulated milliseconds and launch count of a kernel class (0 = H update, 1 = E update,
+ * 2 = emitters, 3 = sources, 4 = detectors). */
+int omx_profile_enable(omx_ctx *ctx, int on);
+int omx_profile_query(omx_ctx *ctx, int kernel_class, double *total_ms, long long *launches);
+/* algorithmic bytes moved by one launch of a kernel class in the current configuration */
+int omx_algorithmic_bytes(const omx_ctx *ctx, int kernel_class, double *bytes);
+/* number of library kernel launches issued since creation */
+long long omx_launch_count(const omx_ctx *ctx);
+/* events around a region on the context stream */
+int omx_timer_start(omx_ctx *ctx);
+int omx_timer_stop(omx_ctx *ctx, float *ms);
+/* flush L2 by writing a scratch buffer larger than L2 on the context stream */
+int omx_flush_l2(omx_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

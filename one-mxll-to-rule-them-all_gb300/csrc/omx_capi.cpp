@@ -1,0 +1,1671 @@
+// omx_capi.cpp -- the C-ABI entry points of include/omx_gpu.h: context creation (init_*Dgrid),
+// media / source / q-group / detector set-up, per-call stepping and the whole-loop runner with
+// optional CUDA-graph capture.  All device memory is owned here; kernels live in
+// omx_kernels_{exact,fast}.cu.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <tuple>
+#include <type_traits>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/omx_gpu.h"
+#include "omx_host.h"
+#include "omx_internal.h"
+
+using namespace omx;
+
+namespace {
+
+thread_local std::string g_last_error = "";
+
+struct Fail {
+    int code;
+    std::string msg;
+};
+
+inline void ck(cudaError_t e, const char *what)
+{
+    if (e != cudaSuccess) throw Fail{OMX_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e)};
+}
+inline void req(bool ok, const std::string &msg, int code = OMX_ERR_ARG)
+{
+    if (!ok) throw Fail{code, msg};
+}
+
+template <class T> struct DevBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    ~DevBuf() { release(); }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    void alloc(size_t count, bool zero = true)
+    {
+        release();
+        if (count == 0) return;
+        cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+        if (e != cudaSuccess) {
+            p = nullptr;
+            throw Fail{OMX_ERR_NOMEM, std::string("cudaMalloc failed: ") + cudaGetErrorString(e)};
+        }
+        n = count;
+        if (zero) ck(cudaMemset(p, 0, count * sizeof(T)), "cudaMemset");
+    }
+    void upload(const std::vector<T> &v)
+    {
+        alloc(v.size(), false);
+        if (!v.empty()) ck(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice), "upload");
+    }
+};
+
+int field_code_to_index(int field) { return field - 1; }
+
+}  // namespace
+
+// ----------------------------------------------------------------------------------------------
+struct SourceRec {
+    int kind;            // 0 kernel source, 1 plane source
+    omx_source_desc d;
+    omx_plane_source_desc pd;
+    int comp;            // 0..2
+    int avg;
+    double c_src;
+    DevBuf<long long> eidx;
+    DevBuf<double> ka, kb;
+    int n;
+};
+
+struct GroupRec {
+    omx_qgroup_desc d;
+    int npar, nst;
+    DevBuf<int> ci, cj, ck;
+    DevBuf<double> par, rho, E, dipole, dPdt;
+    DevBuf<int> win;
+    DevBuf<double> wk;
+    std::vector<std::pair<long long, double>> pts;   // (cell key, wk) in write order
+    std::vector<int> pts_owner;                       // emitter index per point
+};
+
+struct omx_ctx {
+    omx_grid_desc desc{};
+    int dims = 3;
+    int n[3] = {1, 1, 1};
+    bool fp32 = false;
+    cudaStream_t stream = nullptr;
+    Lay L{};
+    size_t felems = 0;
+    DevBuf<float> ff[6];
+    DevBuf<double> fd[6];
+    bool field_used[6] = {false, false, false, false, false, false};
+    // host tables
+    CpmlTables T;
+    std::vector<double> den_e[3], den_h[3];
+    bool cpml_axis[3] = {false, false, false};
+    int per[3] = {0, 0, 0};
+    // device tables (one of the two precisions used)
+    DevBuf<float> tf[3][6];   // den_e, den_h, bE, cE, bH, cH per axis
+    DevBuf<double> td[3][6];
+    DevBuf<short> tl[3][2];   // lE, lH per axis
+    DevBuf<float> psif[3][2][2];
+    DevBuf<double> psid[3][2][2];
+    int L2 = 0;
+    // media
+    int n_media = 0;
+    std::vector<omx_medium> media;
+    int bb0[3] = {1, 1, 1}, bb1[3] = {0, 0, 0};
+    long long bbV = 0;
+    DevBuf<uint8_t> mat[3];
+    DevBuf<unsigned char> clsbuf, medbuf;
+    DevBuf<float> adef;
+    DevBuf<double> aded;
+    int P = 1;
+    bool has_ade = false;
+    std::vector<uint8_t> host_mat[3];   // class per component over the box (for injection checks)
+    std::vector<int> cls_type;          // per class id
+    // sources
+    std::vector<std::unique_ptr<SourceRec>> sources;
+    // emitters and J points
+    std::vector<std::unique_ptr<GroupRec>> groups;
+    std::vector<long long> jkeys;                  // cell keys of J points (sorted)
+    std::unordered_map<long long, int> jslot;
+    DevBuf<double> jbuf;                           // 9 * np: J[3], Jo[3], dJ[3]
+    DevBuf<long long> inj_e;
+    DevBuf<int> inj_c, inj_a, inj_b;
+    int inj_n = 0;
+    bool j_dirty = false;
+    // detectors
+    struct Det { int type, field, nd; };
+    std::vector<Det> dets;
+    std::vector<int> tap_field, tap_nt;
+    std::vector<double> tap_w;
+    std::vector<long long> tap[4];
+    DevBuf<int> d_tap_field, d_tap_nt;
+    DevBuf<double> d_tap_w;
+    DevBuf<long long> d_tap[4];
+    DevBuf<double> rec, rec_times;
+    int rec_capacity = 0, rec_count = 0;
+    bool det_dirty = false;
+    // stepping state (mxim_mxll.f90:96-104)
+    bool started = false;
+    int tq_step_old = 0;
+    double t_skip = 0.0;
+    // run tables
+    DevBuf<double> tab;
+    DevBuf<int> d_step;
+    // graph
+    cudaGraphExec_t gexec = nullptr;
+    // profiling
+    bool prof = false;
+    struct Ev { int cls; cudaEvent_t a, b; };
+    std::vector<Ev> evs;
+    double prof_ms[KC_N] = {0, 0, 0, 0, 0};
+    long long prof_n[KC_N] = {0, 0, 0, 0, 0};
+    long long launches = 0;
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    DevBuf<float> flushbuf;
+    std::string err;
+};
+
+namespace {
+
+int set_err(omx_ctx *ctx, const Fail &f)
+{
+    g_last_error = f.msg;
+    if (ctx) ctx->err = f.msg;
+    return f.code;
+}
+
+#define OMX_API_BEGIN try {
+#define OMX_API_END(ctx)                                                                          \
+    }                                                                                             \
+    catch (const Fail &f) { return set_err(ctx, f); }                                             \
+    catch (const std::exception &e) { return set_err(ctx, Fail{OMX_ERR_ARG, e.what()}); }         \
+    return OMX_OK;
+
+long long cell_key(const omx_ctx *c, int i, int j, int k)
+{
+    return (long long)i + (long long)(c->n[0] + 2) * ((long long)j + (long long)(c->n[1] + 2) * (long long)k);
+}
+
+long long eindex(const omx_ctx *c, int i, int j, int k)
+{
+    return c->L.off + i + (long long)c->L.px * j + c->L.pz * k;
+}
+
+// ---- profiling helpers ------------------------------------------------------------------------
+struct ProfScope {
+    omx_ctx *c;
+    int cls;
+    cudaEvent_t a = nullptr, b = nullptr;
+    ProfScope(omx_ctx *ctx, int k) : c(ctx), cls(k)
+    {
+        if (c->prof) {
+            cudaEventCreate(&a);
+            cudaEventCreate(&b);
+            cudaEventRecord(a, c->stream);
+        }
+    }
+    ~ProfScope()
+    {
+        if (c->prof) {
+            cudaEventRecord(b, c->stream);
+            c->evs.push_back({cls, a, b});
+        }
+    }
+};
+
+void prof_collect(omx_ctx *c)
+{
+    if (c->evs.empty()) return;
+    ck(cudaStreamSynchronize(c->stream), "sync");
+    for (auto &e : c->evs) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e.a, e.b);
+        c->prof_ms[e.cls] += ms;
+        c->prof_n[e.cls] += 1;
+        cudaEventDestroy(e.a);
+        cudaEventDestroy(e.b);
+    }
+    c->evs.clear();
+}
+
+// ---- field bounds (reference arrays) -----------------------------------------------------------
+bool bounds_of(const omx_ctx *c, int field, int lo[3], int hi[3])
+{
+    const int nx = c->n[0], ny = c->n[1], nz = c->n[2];
+    for (int a = 0; a < 3; ++a) lo[a] = hi[a] = 0;
+    if (c->dims == 3) {
+        switch (field) {
+        case OMX_EX_FIELD: lo[0] = 0; hi[0] = nx; lo[1] = 1; hi[1] = ny + 1; lo[2] = 1; hi[2] = nz + 1; return true;
+        case OMX_EY_FIELD: lo[0] = 1; hi[0] = nx + 1; lo[1] = 0; hi[1] = ny; lo[2] = 1; hi[2] = nz + 1; return true;
+        case OMX_EZ_FIELD: lo[0] = 1; hi[0] = nx + 1; lo[1] = 1; hi[1] = ny + 1; lo[2] = 0; hi[2] = nz; return true;
+        case OMX_HX_FIELD: lo[0] = 1; hi[0] = nx; lo[1] = 0; hi[1] = ny; lo[2] = 0; hi[2] = nz; return true;
+        case OMX_HY_FIELD: lo[0] = 0; hi[0] = nx; lo[1] = 1; hi[1] = ny; lo[2] = 0; hi[2] = nz; return true;
+        case OMX_HZ_FIELD: lo[0] = 0; hi[0] = nx; lo[1] = 0; hi[1] = ny; lo[2] = 1; hi[2] = nz; return true;
+        }
+        return false;
+    }
+    if (c->dims == 2) {
+        if (c->desc.mode == OMX_TMZ_2D_MODE) {
+            switch (field) {
+            case OMX_EZ_FIELD: lo[0] = 1; hi[0] = nx + 1; lo[1] = 1; hi[1] = ny + 1; return true;
+            case OMX_HX_FIELD: lo[0] = 1; hi[0] = nx; lo[1] = 0; hi[1] = ny; return true;
+            case OMX_HY_FIELD: lo[0] = 0; hi[0] = nx; lo[1] = 1; hi[1] = ny; return true;
+            }
+        } else {
+            switch (field) {
+            case OMX_EX_FIELD: lo[0] = 0; hi[0] = nx; lo[1] = 1; hi[1] = ny + 1; return true;
+            case OMX_EY_FIELD: lo[0] = 1; hi[0] = nx + 1; lo[1] = 0; hi[1] = ny; return true;
+            case OMX_HZ_FIELD: lo[0] = 0; hi[0] = nx; lo[1] = 0; hi[1] = ny; return true;
+            }
+        }
+        return false;
+    }
+    switch (field) {
+    case OMX_EX_FIELD: lo[0] = 1; hi[0] = nx; return true;
+    case OMX_HY_FIELD: lo[0] = 1; hi[0] = nx - 1; return true;
+    }
+    return false;
+}
+
+// ---- device tables ------------------------------------------------------------------------------
+template <class R> DevBuf<R> (&tables(omx_ctx *c))[3][6];
+template <> DevBuf<float> (&tables<float>(omx_ctx *c))[3][6] { return c->tf; }
+template <> DevBuf<double> (&tables<double>(omx_ctx *c))[3][6] { return c->td; }
+template <class R> DevBuf<R> (&psis(omx_ctx *c))[3][2][2];
+template <> DevBuf<float> (&psis<float>(omx_ctx *c))[3][2][2] { return c->psif; }
+template <> DevBuf<double> (&psis<double>(omx_ctx *c))[3][2][2] { return c->psid; }
+template <class R> DevBuf<R> (&fields(omx_ctx *c))[6];
+template <> DevBuf<float> (&fields<float>(omx_ctx *c))[6] { return c->ff; }
+template <> DevBuf<double> (&fields<double>(omx_ctx *c))[6] { return c->fd; }
+template <class R> DevBuf<R> &adebuf(omx_ctx *c);
+template <> DevBuf<float> &adebuf<float>(omx_ctx *c) { return c->adef; }
+template <> DevBuf<double> &adebuf<double>(omx_ctx *c) { return c->aded; }
+
+template <class R> void upload_axis_tables(omx_ctx *c)
+{
+    const bool exact = std::is_same<R, double>::value;
+    const int npml = c->desc.npml;
+    for (int a = 0; a < 3; ++a) {
+        const int na = c->n[a];
+        std::vector<R> de(na + 2), dh(na + 2), bE(na + 2, R(0)), cE(na + 2, R(0)), bH(na + 2, R(0)), cH(na + 2, R(0));
+        std::vector<short> lE(na + 2, -1), lH(na + 2, -1);
+        for (int p = 0; p < na + 2; ++p) {
+            de[p] = (R)c->den_e[a][p];
+            dh[p] = (R)c->den_h[a][p];
+        }
+        if (c->cpml_axis[a]) {
+            const double dr = c->desc.dr;
+            auto cf = [&](double v) { return exact ? (R)v : (R)(v / dr); };
+            // E: low face i = 2..npml (be(i)), high face i = n+1-npml..n-1 (be(n+1-i))
+            for (int p = 2; p <= npml; ++p) {
+                lE[p] = (short)(p - 2);
+                bE[p] = (R)c->T.be[p - 1];
+                cE[p] = cf(c->T.ce[p - 1]);
+            }
+            for (int p = na + 1 - npml; p <= na - 1; ++p) {
+                lE[p] = (short)((npml - 1) + (p - (na + 1 - npml)));
+                bE[p] = (R)c->T.be[na + 1 - p - 1];
+                cE[p] = cf(c->T.ce[na + 1 - p - 1]);
+            }
+            // H: low face i = 1..npml-1 (bh(i)), high face i = n+1-npml..n-1 (bh(n-i))
+            for (int p = 1; p <= npml - 1; ++p) {
+                lH[p] = (short)(p - 1);
+                bH[p] = (R)c->T.bh[p - 1];
+                cH[p] = cf(c->T.ch[p - 1]);
+            }
+            for (int p = na + 1 - npml; p <= na - 1; ++p) {
+                lH[p] = (short)((npml - 1) + (p - (na + 1 - npml)));
+                bH[p] = (R)c->T.bh[na - p - 1];
+                cH[p] = cf(c->T.ch[na - p - 1]);
+            }
+        }
+        auto &tb = tables<R>(c)[a];
+        tb[0].upload(de);
+        tb[1].upload(dh);
+        tb[2].upload(bE);
+        tb[3].upload(cE);
+        tb[4].upload(bH);
+        tb[5].upload(cH);
+        c->tl[a][0].upload(lE);
+        c->tl[a][1].upload(lH);
+    }
+}
+
+template <class R> void alloc_psi(omx_ctx *c)
+{
+    const int npml = c->desc.npml;
+    c->L2 = 2 * (npml - 1);
+    auto &ps = psis<R>(c);
+    for (int a = 0; a < 3; ++a)
+        for (int f = 0; f < 2; ++f)
+            for (int q = 0; q < 2; ++q) ps[a][f][q].release();
+    for (int a = 0; a < c->dims; ++a) {
+        if (!c->cpml_axis[a]) continue;
+        long long tr = 1;
+        for (int b = 0; b < c->dims; ++b)
+            if (b != a) tr *= c->n[b];
+        const long long cnt = (long long)c->L2 * tr;
+        const int ncomp = (c->dims == 3) ? 2 : 1;
+        for (int f = 0; f < 2; ++f)
+            for (int q = 0; q < ncomp; ++q) ps[a][f][q].alloc((size_t)cnt);
+    }
+}
+
+template <class R> FieldPtrs<R> field_ptrs(omx_ctx *c)
+{
+    FieldPtrs<R> F;
+    for (int q = 0; q < 6; ++q) F.f[q] = fields<R>(c)[q].p;
+    return F;
+}
+
+template <class R> GridArgs<R> grid_args(omx_ctx *c)
+{
+    GridArgs<R> G;
+    std::memset(&G, 0, sizeof(G));
+    G.L = c->L;
+    const omx::Consts &K = omx::consts();
+    (void)K;
+    const double dt_eps0 = c->desc.dt / omx::consts().eps0, dt_mu0 = c->desc.dt / omx::consts().mu0;
+    G.dt_mu0 = (R)dt_mu0;
+    G.dt_eps0 = (R)dt_eps0;
+    G.dr = (R)c->desc.dr;
+    for (int a = 0; a < 3; ++a) G.per[a] = c->per[a];
+    G.npml = c->desc.npml;
+    G.L2 = c->L2;
+    auto &tb = tables<R>(c);
+    auto &ps = psis<R>(c);
+    for (int a = 0; a < 3; ++a) {
+        G.den_e[a] = tb[a][0].p;
+        G.den_h[a] = tb[a][1].p;
+        G.bE[a] = tb[a][2].p;
+        G.cE[a] = tb[a][3].p;
+        G.bH[a] = tb[a][4].p;
+        G.cH[a] = tb[a][5].p;
+        G.lE[a] = c->tl[a][0].p;
+        G.lH[a] = c->tl[a][1].p;
+        for (int q = 0; q < 2; ++q) {
+            G.psiE[a][q] = ps[a][0][q].p;
+            G.psiH[a][q] = ps[a][1][q].p;
+        }
+        G.bb0[a] = c->bb0[a];
+        G.bb1[a] = c->bb1[a];
+        G.bbd[a] = std::max(0, c->bb1[a] - c->bb0[a] + 1);
+        G.mat[a] = c->mat[a].p;
+    }
+    G.bbV = c->bbV;
+    G.cls = reinterpret_cast<const ClsR<R> *>(c->clsbuf.p);
+    G.med = reinterpret_cast<const MedR<R> *>(c->medbuf.p);
+    G.ade = adebuf<R>(c).p;
+    G.P = c->P;
+    G.mode2d = c->desc.mode;
+    return G;
+}
+
+// ---- media ----------------------------------------------------------------------------------------
+template <class R>
+void build_media(omx_ctx *c, const int32_t *map, const double *eps[3])
+{
+    const int dims = c->dims;
+    const int nx = c->n[0], ny = c->n[1], nz = c->n[2];
+    const long long N = (long long)nx * ny * nz;
+    const int comps = dims == 1 ? 1 : 3;
+    const double dt_eps0 = c->desc.dt / omx::consts().eps0;
+    auto mm = [&](long long cell, int comp) -> int32_t { return map ? map[cell + N * (comps == 1 ? 0 : comp)] : 0; };
+    auto is_ade = [&](int32_t m) {
+        return m > 0 && m <= c->n_media &&
+               (c->media[m - 1].medium_type == OMX_DRUDE_MEDIUM || c->media[m - 1].medium_type == OMX_DL_MEDIUM);
+    };
+    // effective inverse permittivity of component `comp` at a cell (reference rule or arrays)
+    auto eps_inv = [&](long long cell, int comp) -> double {
+        if (eps[0] || eps[1] || eps[2]) {
+            const double *e = eps[comp];
+            return e ? e[cell] : 1.0;
+        }
+        int32_t m;
+        if (dims == 3) m = mm(cell, comp);
+        else if (dims == 2) m = mm(cell, 0);   // classical_medium_mod.f90:526-538 keys on component 1
+        else m = mm(cell, 0);
+        if (m > 0 && m <= c->n_media && c->media[m - 1].medium_type == OMX_DIELECTRIC_MEDIUM)
+            return 1.0 / c->media[m - 1].eps_r;
+        return 1.0;
+    };
+    const int act[3] = {dims == 3 || dims == 1 || (dims == 2 && c->desc.mode == OMX_TEZ_2D_MODE),
+                        dims == 3 || (dims == 2 && c->desc.mode == OMX_TEZ_2D_MODE),
+                        dims == 3 || (dims == 2 && c->desc.mode == OMX_TMZ_2D_MODE)};
+    // bounding box of non-vacuum component cells
+    int b0[3] = {1 << 30, 1 << 30, 1 << 30}, b1[3] = {-1, -1, -1};
+    const bool all_vacuum = !map && !eps[0] && !eps[1] && !eps[2];
+    for (long long cell = 0; cell < (all_vacuum ? 0 : N); ++cell) {
+        bool nv = false;
+        for (int q = 0; q < 3 && !nv; ++q) {
+            if (!act[q]) continue;
+            if (dims == 1 && q > 0) break;
+            const int32_t m = (dims == 1) ? mm(cell, 0) : mm(cell, q);
+            if (is_ade(m) || eps_inv(cell, q) != 1.0) nv = true;
+        }
+        if (!nv) continue;
+        const int i = 1 + (int)(cell % nx), j = 1 + (int)((cell / nx) % ny), k = 1 + (int)(cell / ((long long)nx * ny));
+        const int ijk[3] = {i, j, k};
+        for (int a = 0; a < 3; ++a) {
+            b0[a] = std::min(b0[a], ijk[a]);
+            b1[a] = std::max(b1[a], ijk[a]);
+        }
+    }
+    if (b1[0] < 0) {
+        for (int a = 0; a < 3; ++a) { b0[a] = 1; b1[a] = 0; }
+    }
+    for (int a = 0; a < 3; ++a) { c->bb0[a] = b0[a]; c->bb1[a] = b1[a]; }
+    const int bd[3] = {std::max(0, b1[0] - b0[0] + 1), std::max(0, b1[1] - b0[1] + 1), std::max(0, b1[2] - b0[2] + 1)};
+    c->bbV = (long long)bd[0] * bd[1] * bd[2];
+    // classes
+    std::map<std::tuple<int, int, double>, int> ids;
+    std::vector<ClsR<R>> cls;
+    cls.push_back(ClsR<R>{CLS_PLAIN, 0, (R)dt_eps0, (R)0});
+    c->cls_type.assign(1, CLS_PLAIN);
+    ids[std::make_tuple((int)CLS_PLAIN, 0, 1.0)] = 0;
+    int maxP = 1;
+    for (int m = 0; m < c->n_media; ++m)
+        if (c->media[m].medium_type == OMX_DL_MEDIUM) maxP = std::max(maxP, c->media[m].n_poles);
+    c->P = maxP;
+    bool any_ade = false;
+    for (int q = 0; q < 3; ++q) c->host_mat[q].assign((size_t)c->bbV, 0);
+    for (int k = b0[2]; k <= b1[2]; ++k)
+        for (int j = b0[1]; j <= b1[1]; ++j)
+            for (int i = b0[0]; i <= b1[0]; ++i) {
+                const long long cell = (i - 1) + (long long)nx * ((j - 1) + (long long)ny * (k - 1));
+                const long long b = (i - b0[0]) + (long long)bd[0] * ((j - b0[1]) + (long long)bd[1] * (k - b0[2]));
+                for (int q = 0; q < comps; ++q) {
+                    if (!act[q]) continue;
+                    const int32_t m = mm(cell, q);
+                    std::tuple<int, int, double> key;
+                    if (is_ade(m)) {
+                        key = std::make_tuple(c->media[m - 1].medium_type == OMX_DRUDE_MEDIUM ? (int)CLS_DRUDE : (int)CLS_DL,
+                                              (int)m, 0.0);
+                        any_ade = true;
+                    } else {
+                        key = std::make_tuple((int)CLS_PLAIN, 0, eps_inv(cell, q));
+                    }
+                    auto it = ids.find(key);
+                    int id;
+                    if (it == ids.end()) {
+                        id = (int)cls.size();
+                        req(id < 255, "more than 254 distinct material classes");
+                        ids[key] = id;
+                        ClsR<R> cr{};
+                        cr.type = std::get<0>(key);
+                        cr.medium = std::get<1>(key) > 0 ? std::get<1>(key) - 1 : 0;
+                        cr.coef = (R)(dt_eps0 * std::get<2>(key));
+                        cls.push_back(cr);
+                        c->cls_type.push_back(cr.type);
+                    } else {
+                        id = it->second;
+                    }
+                    c->host_mat[q][(size_t)b] = (uint8_t)id;
+                }
+            }
+    for (int q = 0; q < 3; ++q) {
+        if (c->bbV > 0 && act[q]) {
+            c->mat[q].alloc((size_t)c->bbV, false);
+            ck(cudaMemcpy(c->mat[q].p, c->host_mat[q].data(), (size_t)c->bbV, cudaMemcpyHostToDevice), "mat");
+        } else {
+            c->mat[q].release();
+        }
+    }
+    std::vector<unsigned char> cb(cls.size() * sizeof(ClsR<R>));
+    std::memcpy(cb.data(), cls.data(), cb.size());
+    c->clsbuf.upload(cb);
+    std::vector<MedR<R>> med((size_t)std::max(1, c->n_media));
+    for (int m = 0; m < c->n_media; ++m) {
+        const omx_medium &s = c->media[m];
+        MedR<R> &d = med[(size_t)m];
+        std::memset(&d, 0, sizeof(d));
+        d.A1 = (R)s.A1; d.A2 = (R)s.A2; d.C1 = (R)s.C1; d.C2 = (R)s.C2; d.C3 = (R)s.C3; d.C4 = (R)s.C4;
+        d.np = s.medium_type == OMX_DL_MEDIUM ? s.n_poles : 0;
+        for (int p = 0; p < d.np; ++p) {
+            d.al[p] = (R)s.alpha_k[p]; d.be[p] = (R)s.beta_k[p]; d.ga[p] = (R)s.gamma_k[p];
+            d.B1[p] = (R)s.B1_k[p]; d.B2[p] = (R)s.B2_k[p];
+        }
+    }
+    std::vector<unsigned char> mb(med.size() * sizeof(MedR<R>));
+    std::memcpy(mb.data(), med.data(), mb.size());
+    c->medbuf.upload(mb);
+    c->has_ade = any_ade;
+    if (any_ade) adebuf<R>(c).alloc((size_t)(3LL * (2 + 2 * c->P) * c->bbV));
+    else adebuf<R>(c).release();
+}
+
+int comp_axis_active(const omx_ctx *c, int q)
+{
+    if (c->dims == 3) return 1;
+    if (c->dims == 1) return q == 0;
+    return c->desc.mode == OMX_TMZ_2D_MODE ? q == 2 : q < 2;
+}
+
+// Injection list for the emitter current term of the E update.
+void rebuild_injection(omx_ctx *c)
+{
+    const int np = (int)c->jkeys.size();
+    const int avg = (c->dims == 3 || (c->dims == 2 && c->desc.mode == OMX_TEZ_2D_MODE)) ? 1 : 0;
+    struct Ent { long long e; int comp, a, b; };
+    std::map<std::pair<int, long long>, Ent> ents;
+    const int nxx = c->n[0] + 2, nyy = c->n[1] + 2;
+    for (int p = 0; p < np; ++p) {
+        const long long key = c->jkeys[p];
+        const int i = (int)(key % nxx), j = (int)((key / nxx) % nyy), k = (int)(key / ((long long)nxx * nyy));
+        for (int q = 0; q < 3; ++q) {
+            if (!comp_axis_active(c, q)) continue;
+            int cand[2][3] = {{i, j, k}, {i, j, k}};
+            int ncand = 1;
+            if (avg) {
+                cand[1][q] -= 1;   // E cell whose i+1 neighbour is this J point
+                ncand = 2;
+            }
+            for (int t = 0; t < ncand; ++t) {
+                const int ci = cand[t][0], cj = cand[t][1], cz = cand[t][2];
+                // E update ranges: 3D/2D i,j,k in 1..n; 1D i in 2..n-1
+                if (c->dims == 1) {
+                    if (ci < 2 || ci > c->n[0] - 1) continue;
+                } else {
+                    if (ci < 1 || ci > c->n[0] || cj < 1 || cj > c->n[1]) continue;
+                    if (c->dims == 3 && (cz < 1 || cz > c->n[2])) continue;
+                }
+                // skip dispersive components (the reference ignores J there); the media box
+                // carries j == k == 1 on the axes a 1D/2D grid does not have
+                const int bj = c->dims >= 2 ? cj : 1, bk = c->dims == 3 ? cz : 1;
+                if (ci >= c->bb0[0] && ci <= c->bb1[0] && bj >= c->bb0[1] && bj <= c->bb1[1] &&
+                    bk >= c->bb0[2] && bk <= c->bb1[2] && c->bbV > 0) {
+                    const int bd0 = c->bb1[0] - c->bb0[0] + 1, bd1 = c->bb1[1] - c->bb0[1] + 1;
+                    const long long b = (ci - c->bb0[0]) + (long long)bd0 * ((bj - c->bb0[1]) + (long long)bd1 * (bk - c->bb0[2]));
+                    if (!c->host_mat[q].empty() && c->cls_type[c->host_mat[q][(size_t)b]] != CLS_PLAIN) continue;
+                }
+                const long long ck_ = cell_key(c, ci, cj, cz);
+                auto kk = std::make_pair(q, ck_);
+                if (ents.count(kk)) continue;
+                Ent en;
+                en.e = eindex(c, ci, cj, cz);
+                en.comp = q;
+                auto fa = c->jslot.find(ck_);
+                en.a = fa == c->jslot.end() ? -1 : fa->second;
+                en.b = -1;
+                if (avg) {
+                    int nb[3] = {ci, cj, cz};
+                    nb[q] += 1;
+                    auto fb = c->jslot.find(cell_key(c, nb[0], nb[1], nb[2]));
+                    en.b = fb == c->jslot.end() ? -1 : fb->second;
+                }
+                ents[kk] = en;
+            }
+        }
+    }
+    std::vector<long long> e;
+    std::vector<int> comp, a, b;
+    for (auto &kv : ents) {
+        e.push_back(kv.second.e);
+        comp.push_back(kv.second.comp);
+        a.push_back(kv.second.a);
+        b.push_back(kv.second.b);
+    }
+    c->inj_n = (int)e.size();
+    c->inj_e.upload(e);
+    c->inj_c.upload(comp);
+    c->inj_a.upload(a);
+    c->inj_b.upload(b);
+}
+
+void rebuild_jpoints(omx_ctx *c)
+{
+    std::vector<long long> keys;
+    for (auto &g : c->groups)
+        for (auto &pt : g->pts) keys.push_back(pt.first);
+    std::sort(keys.begin(), keys.end());
+    keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
+    c->jkeys = keys;
+    c->jslot.clear();
+    for (size_t p = 0; p < keys.size(); ++p) c->jslot[keys[p]] = (int)p;
+    const int np = (int)keys.size();
+    c->jbuf.alloc((size_t)9 * std::max(np, 1));
+    for (auto &g : c->groups) {
+        std::vector<int> win((size_t)std::max(np, 1), -1);
+        std::vector<double> wk((size_t)std::max(np, 1), 0.0);
+        for (size_t t = 0; t < g->pts.size(); ++t) {   // assignment: the last writer wins
+            const int s = c->jslot[g->pts[t].first];
+            win[(size_t)s] = g->pts_owner[t];
+            wk[(size_t)s] = g->pts[t].second;
+        }
+        g->win.upload(win);
+        g->wk.upload(wk);
+    }
+    rebuild_injection(c);
+    c->j_dirty = false;
+}
+
+JState jstate(omx_ctx *c)
+{
+    JState J;
+    J.np = (int)c->jkeys.size();
+    const size_t np = (size_t)std::max(J.np, 1);
+    for (int q = 0; q < 3; ++q) {
+        J.J[q] = c->jbuf.p + np * q;
+        J.Jo[q] = c->jbuf.p + np * (3 + q);
+        J.dJ[q] = c->jbuf.p + np * (6 + q);
+    }
+    return J;
+}
+
+void rebuild_detectors(omx_ctx *c)
+{
+    c->d_tap_field.upload(c->tap_field);
+    c->d_tap_nt.upload(c->tap_nt);
+    c->d_tap_w.upload(c->tap_w);
+    for (int t = 0; t < 4; ++t) c->d_tap[t].upload(c->tap[t]);
+    c->det_dirty = false;
+}
+
+void ensure_rec_capacity(omx_ctx *c, int need)
+{
+    const int npts = (int)c->tap_field.size();
+    if (need <= c->rec_capacity) return;
+    int cap = std::max(need, c->rec_capacity * 2);
+    DevBuf<double> nrec, ntim;
+    nrec.alloc((size_t)cap * std::max(npts, 1));
+    ntim.alloc((size_t)cap);
+    if (c->rec_count > 0 && c->rec.p) {
+        ck(cudaMemcpyAsync(nrec.p, c->rec.p, sizeof(double) * (size_t)c->rec_count * std::max(npts, 1),
+                           cudaMemcpyDeviceToDevice, c->stream), "rec copy");
+        ck(cudaMemcpyAsync(ntim.p, c->rec_times.p, sizeof(double) * (size_t)c->rec_count, cudaMemcpyDeviceToDevice,
+                           c->stream), "rec copy");
+        ck(cudaStreamSynchronize(c->stream), "sync");
+    }
+    std::swap(c->rec.p, nrec.p);
+    std::swap(c->rec.n, nrec.n);
+    std::swap(c->rec_times.p, ntim.p);
+    std::swap(c->rec_times.n, ntim.n);
+    c->rec_capacity = cap;
+}
+
+DetArgs det_args(omx_ctx *c)
+{
+    DetArgs D;
+    D.n = (int)c->tap_field.size();
+    D.field = c->d_tap_field.p;
+    D.nt = c->d_tap_nt.p;
+    D.w = c->d_tap_w.p;
+    D.t0 = c->d_tap[0].p;
+    D.t1 = c->d_tap[1].p;
+    D.t2 = c->d_tap[2].p;
+    D.t3 = c->d_tap[3].p;
+    D.rec = c->rec.p;
+    D.times = c->rec_times.p;
+    return D;
+}
+
+void prepare(omx_ctx *c)
+{
+    if (c->j_dirty) rebuild_jpoints(c);
+    if (c->det_dirty) rebuild_detectors(c);
+    c->started = true;
+}
+
+StepParam imm(double v) { return StepParam{v, nullptr, nullptr}; }
+
+// ---- launch sequences (templated on the field precision) --------------------------------------
+template <class R> void do_H(omx_ctx *c)
+{
+    ProfScope ps(c, KC_H);
+    launch_h<R>(field_ptrs<R>(c), grid_args<R>(c), c->stream);
+    c->launches++;
+}
+
+template <class R> void do_sources(omx_ctx *c, const std::vector<StepParam> &amps)
+{
+    ProfScope ps(c, KC_SRC);
+    const FieldPtrs<R> F = field_ptrs<R>(c);
+    for (size_t s = 0; s < c->sources.size(); ++s) {
+        SourceRec &S = *c->sources[s];
+        if (S.kind == 0) {
+            SrcArgs a;
+            a.n = S.n;
+            a.eidx = S.eidx.p;
+            a.ka = S.ka.p;
+            a.kb = S.kb.p;
+            a.comp = S.comp;
+            a.avg = S.avg;
+            a.c_src = S.c_src;
+            launch_src<R>(F, a, amps[s], c->stream);
+        } else {
+            PlaneArgs p;
+            p.comp = S.pd.comp - 1;
+            p.axis = S.pd.plane_axis - 1;
+            p.index = S.pd.plane_index;
+            p.c_src = S.c_src;
+            launch_plane<R>(F, c->L, p, amps[s], c->stream);
+        }
+        c->launches++;
+    }
+}
+
+template <class R> void do_E(omx_ctx *c, StepParam time, StepParam t_skip)
+{
+    {
+        ProfScope ps(c, KC_E);
+        launch_e<R>(field_ptrs<R>(c), grid_args<R>(c), c->stream);
+        c->launches++;
+    }
+    if (c->inj_n > 0) {
+        InjArgs I;
+        I.n = c->inj_n;
+        I.eidx = c->inj_e.p;
+        I.comp = c->inj_c.p;
+        I.sa = c->inj_a.p;
+        I.sb = c->inj_b.p;
+        I.avg = (c->dims == 3 || (c->dims == 2 && c->desc.mode == OMX_TEZ_2D_MODE)) ? 1 : 0;
+        ProfScope ps(c, KC_EMIT);
+        launch_inject<R>(field_ptrs<R>(c), jstate(c), I, time, t_skip, c->desc.dt / omx::consts().eps0, c->stream);
+        c->launches++;
+    }
+}
+
+template <class R> void do_group(omx_ctx *c, GroupRec &g, StepParam move)
+{
+    ProfScope ps(c, KC_EMIT);
+    EmitArgs A;
+    A.n = g.d.n_systems;
+    A.model = g.d.model;
+    A.npar = g.npar;
+    A.nst = g.nst;
+    A.dims = c->dims;
+    A.mode2d = c->desc.mode;
+    A.ci = g.ci.p;
+    A.cj = g.cj.p;
+    A.ck = g.ck.p;
+    A.par = g.par.p;
+    A.rho = g.rho.p;
+    A.E = g.E.p;
+    A.dipole = g.dipole.p;
+    A.dPdt = g.dPdt.p;
+    A.dt = g.d.dt;
+    launch_emit<R>(field_ptrs<R>(c), c->L, A, move, c->stream);
+    ScatArgs S;
+    S.np = (int)c->jkeys.size();
+    if (c->dims == 3) { S.c0 = 0; S.c1 = 2; }
+    else if (c->dims == 1) { S.c0 = 0; S.c1 = 0; }
+    else if (c->desc.mode == OMX_TMZ_2D_MODE) { S.c0 = 2; S.c1 = 2; }
+    else { S.c0 = 0; S.c1 = 1; }
+    S.win = g.win.p;
+    S.wk = g.wk.p;
+    S.dPdt = g.dPdt.p;
+    S.dt = g.d.dt;
+    launch_scatter(jstate(c), S, move, c->stream);
+    c->launches += 2;
+}
+
+template <class R> void do_sample(omx_ctx *c, StepParam slot, StepParam time)
+{
+    ProfScope ps(c, KC_DET);
+    launch_sample<R>(field_ptrs<R>(c), det_args(c), slot, time, c->stream);
+    c->launches++;
+}
+
+double source_amp(const SourceRec &S, double time)
+{
+    // update_source (source_mod.f90:114-130): j_amp * exp(-((t-t0)/tau)^2) * cos(w0 (t-t0) + phase)
+    const double j_amp = S.kind == 0 ? S.d.j_amp : S.pd.j_amp;
+    const double t0 = S.kind == 0 ? S.d.t0 : S.pd.t0;
+    const double tau = S.kind == 0 ? S.d.tau : S.pd.tau;
+    const double w0 = S.kind == 0 ? S.d.w0 : S.pd.w0;
+    const double ph0 = S.kind == 0 ? S.d.phase : S.pd.phase;
+    const double chirp = S.kind == 0 ? S.d.chirp : S.pd.chirp;
+    const double ti = S.kind == 0 ? S.d.t_init : S.pd.t_init;
+    const double tf = S.kind == 0 ? S.d.t_final : S.pd.t_final;
+    if (!(time >= ti && time <= tf)) return 0.0;
+    const double a = (time - t0) / tau;
+    const double envelope = std::exp(-(a * a));
+    double ph = w0 * (time - t0) + ph0;
+    if (chirp != 0.0) ph = ph + 0.5 * chirp * ((time - t0) * (time - t0));
+    const double cos_t = std::cos(ph);
+    return j_amp * envelope * cos_t;
+}
+
+template <class R> void run_impl(omx_ctx *c, int tt0, int nsteps, int n_skip, int t_det_print, int use_graph)
+{
+    prepare(c);
+    const int nsrc = (int)c->sources.size();
+    const bool has_det = !c->tap_field.empty() && t_det_print > 0;
+    // per-step scalars: time, t_skip, move, slot, amps...
+    const int W = 4 + nsrc;
+    std::vector<double> tab((size_t)W * nsteps);
+    const int tt_0 = (n_skip == 1) ? 1 : 0;
+    int nrec = 0;
+    for (int s = 0; s < nsteps; ++s) {
+        const int tt = tt0 + s;
+        const double time = c->desc.dt * ((double)tt - 0.5);
+        const int tq_step = 1 + (tt - tt_0) / n_skip;
+        bool move = false;
+        if (tq_step > c->tq_step_old) {
+            c->t_skip = time;
+            c->tq_step_old = tq_step;
+            move = !c->groups.empty();
+        }
+        int slot = -1;
+        if (has_det && tt % t_det_print == 0) slot = c->rec_count + nrec++;
+        tab[(size_t)0 * nsteps + s] = time;
+        tab[(size_t)1 * nsteps + s] = c->t_skip;
+        tab[(size_t)2 * nsteps + s] = move ? 1.0 : 0.0;
+        tab[(size_t)3 * nsteps + s] = (double)slot;
+        for (int q = 0; q < nsrc; ++q) tab[(size_t)(4 + q) * nsteps + s] = source_amp(*c->sources[q], time);
+    }
+    if (has_det) ensure_rec_capacity(c, c->rec_count + nrec);
+    c->tab.alloc(tab.size(), false);
+    ck(cudaMemcpyAsync(c->tab.p, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream), "tab");
+    if (!c->d_step.p) c->d_step.alloc(1);
+    ck(cudaMemsetAsync(c->d_step.p, 0, sizeof(int), c->stream), "step");
+    auto P = [&](int row) { return StepParam{0.0, c->tab.p + (size_t)row * nsteps, c->d_step.p}; };
+    std::vector<StepParam> amps;
+    for (int q = 0; q < nsrc; ++q) amps.push_back(P(4 + q));
+    auto one_step = [&]() {
+        do_H<R>(c);
+        do_sources<R>(c, amps);
+        do_E<R>(c, P(0), P(1));
+        for (auto &g : c->groups) do_group<R>(c, *g, P(2));
+        if (has_det) do_sample<R>(c, P(3), P(0));
+        launch_step_advance(c->d_step.p, c->stream);
+        c->launches++;
+    };
+    if (use_graph && !c->prof) {
+        if (c->gexec) {
+            cudaGraphExecDestroy(c->gexec);
+            c->gexec = nullptr;
+        }
+        cudaGraph_t graph;
+        const long long before = c->launches;
+        ck(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "capture");
+        one_step();
+        ck(cudaStreamEndCapture(c->stream, &graph), "end capture");
+        const long long per_step = c->launches - before;
+        c->launches = before;
+        ck(cudaGraphInstantiate(&c->gexec, graph, 0), "instantiate");
+        cudaGraphDestroy(graph);
+        for (int s = 0; s < nsteps; ++s) ck(cudaGraphLaunch(c->gexec, c->stream), "graph launch");
+        c->launches += per_step * nsteps;
+    } else {
+        for (int s = 0; s < nsteps; ++s) one_step();
+    }
+    ck(cudaPeekAtLastError(), "launch");
+    c->rec_count += nrec;
+}
+
+template <class R> void read_field_impl(omx_ctx *c, int field, double *host)
+{
+    int lo[3], hi[3];
+    req(bounds_of(c, field, lo, hi), "field not present in this grid/mode");
+    const int q = field_code_to_index(field);
+    std::vector<R> tmp(c->felems);
+    ck(cudaStreamSynchronize(c->stream), "sync");
+    ck(cudaMemcpy(tmp.data(), fields<R>(c)[q].p, c->felems * sizeof(R), cudaMemcpyDeviceToHost), "read field");
+    long long o = 0;
+    for (int k = lo[2]; k <= hi[2]; ++k)
+        for (int j = lo[1]; j <= hi[1]; ++j)
+            for (int i = lo[0]; i <= hi[0]; ++i) {
+                bool ghost_periodic = false;
+                const int ijk[3] = {i, j, k};
+                for (int a = 0; a < c->dims; ++a)
+                    if (c->per[a] && (ijk[a] == 0 || ijk[a] == c->n[a] + 1)) ghost_periodic = true;
+                host[o++] = ghost_periodic ? 0.0 : (double)tmp[(size_t)eindex(c, i, j, k)];
+            }
+}
+
+template <class R> void write_field_impl(omx_ctx *c, int field, const double *host)
+{
+    int lo[3], hi[3];
+    req(bounds_of(c, field, lo, hi), "field not present in this grid/mode");
+    const int q = field_code_to_index(field);
+    std::vector<R> tmp(c->felems);
+    ck(cudaStreamSynchronize(c->stream), "sync");
+    ck(cudaMemcpy(tmp.data(), fields<R>(c)[q].p, c->felems * sizeof(R), cudaMemcpyDeviceToHost), "read field");
+    long long o = 0;
+    for (int k = lo[2]; k <= hi[2]; ++k)
+        for (int j = lo[1]; j <= hi[1]; ++j)
+            for (int i = lo[0]; i <= hi[0]; ++i) tmp[(size_t)eindex(c, i, j, k)] = (R)host[o++];
+    ck(cudaMemcpy(fields<R>(c)[q].p, tmp.data(), c->felems * sizeof(R), cudaMemcpyHostToDevice), "write field");
+}
+
+}  // namespace
+
+// =================================================================================================
+extern "C" {
+
+const char *omx_last_error(const omx_ctx *ctx)
+{
+    if (ctx && !ctx->err.empty()) return ctx->err.c_str();
+    return g_last_error.c_str();
+}
+
+int omx_select_device(int device)
+{
+    OMX_API_BEGIN
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        throw Fail{OMX_ERR_NODEV, "no CUDA device available (the library has no CPU path)"};
+    }
+    req(device >= 0 && device < ndev, "device index out of range");
+    ck(cudaSetDevice(device), "cudaSetDevice");
+    OMX_API_END(nullptr)
+}
+
+int omx_device_count(int *count)
+{
+    OMX_API_BEGIN
+    req(count, "null argument");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess) {
+        cudaGetLastError();
+        ndev = 0;
+    }
+    *count = ndev;
+    OMX_API_END(nullptr)
+}
+
+int omx_create(const omx_grid_desc *d, omx_ctx **out)
+{
+    omx_ctx *c = nullptr;
+    try {
+        req(d && out, "null argument");
+        *out = nullptr;
+        req(d->dimensions >= 1 && d->dimensions <= 3, "dimensions must be 1, 2 or 3");
+        req(d->precision == OMX_PREC_FP64 || d->precision == OMX_PREC_FP32, "precision");
+        req(d->dt > 0 && d->dr > 0, "dt and dr must be positive");
+        int ndev = 0;
+        if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+            cudaGetLastError();
+            throw Fail{OMX_ERR_NODEV, "no CUDA device available (the library has no CPU path)"};
+        }
+        std::unique_ptr<omx_ctx> C(new omx_ctx);
+        c = C.get();
+        c->desc = *d;
+        c->dims = d->dimensions;
+        c->fp32 = d->precision == OMX_PREC_FP32;
+        for (int a = 0; a < 3; ++a) c->n[a] = 1;
+        for (int a = 0; a < c->dims; ++a) {
+            req(d->grid_Ndims[a] >= 3, "grid_Ndims must be >= 3 on every active axis");
+            c->n[a] = d->grid_Ndims[a];
+        }
+        if (c->dims == 2) req(d->mode == OMX_TMZ_2D_MODE || d->mode == OMX_TEZ_2D_MODE,
+                              "2D mode must be TMz or TEz (the reference's 'full' mode allocates TEz only)");
+        bool any_cpml = false;
+        const int naxes = c->dims;
+        for (int a = 0; a < naxes; ++a) {
+            const int b = d->boundaries[a];
+            req(b == OMX_CLOSE_BOUNDARIES || b == OMX_PERIODIC_BOUNDARIES || b == OMX_CPML_BOUNDARIES,
+                "boundaries must be close, periodic or cpml");
+            c->cpml_axis[a] = b == OMX_CPML_BOUNDARIES;
+            c->per[a] = b == OMX_PERIODIC_BOUNDARIES;
+            any_cpml |= c->cpml_axis[a];
+        }
+        req(!(c->dims == 1 && c->per[0]), "1D periodic boundaries write out of bounds in the reference (unsupported)");
+        if (any_cpml) {
+            req(d->npml >= 2, "npml must be >= 2 with CPML boundaries");
+            for (int a = 0; a < naxes; ++a)
+                if (c->cpml_axis[a]) req(c->n[a] >= 2 * d->npml, "grid too small for two CPML slabs");
+        }
+        ck(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream");
+        // layout
+        const int align = c->fp32 ? 32 : 16;
+        Lay &L = c->L;
+        L.dims = c->dims;
+        L.nx = c->n[0];
+        L.ny = c->n[1];
+        L.nz = c->n[2];
+        L.off = align - 1;
+        if (c->dims == 1) {
+            L.px = 0;
+            L.pz = 0;
+            c->felems = (size_t)(L.off + L.nx + 2 + align);
+        } else {
+            L.px = ((L.nx + 2 + align - 1) / align) * align;
+            L.pz = (c->dims == 3) ? (long long)L.px * (L.ny + 2) : 0;
+            const long long rows = (long long)(L.ny + 2) * (c->dims == 3 ? (L.nz + 2) : 1);
+            c->felems = (size_t)(L.off + (long long)L.px * rows + align);
+        }
+        bool used[6] = {false, false, false, false, false, false};
+        if (c->dims == 3) for (int q = 0; q < 6; ++q) used[q] = true;
+        else if (c->dims == 1) used[0] = used[4] = true;
+        else if (d->mode == OMX_TMZ_2D_MODE) used[2] = used[3] = used[4] = true;
+        else used[0] = used[1] = used[5] = true;
+        for (int q = 0; q < 6; ++q) {
+            c->field_used[q] = used[q];
+            if (!used[q]) continue;
+            if (c->fp32) c->ff[q].alloc(c->felems);
+            else c->fd[q].alloc(c->felems);
+        }
+        // CPML tables and den arrays (init_*Dgrid)
+        if (any_cpml) c->T = cpml_tables(d->npml, d->dr, d->dt);
+        int b3[3] = {d->boundaries[0], c->dims >= 2 ? d->boundaries[1] : 0, c->dims == 3 ? d->boundaries[2] : 0};
+        den_arrays(c->dims, c->n, d->npml, b3, d->dr, c->T, c->den_e, c->den_h);
+        if (c->fp32) {
+            upload_axis_tables<float>(c);
+            alloc_psi<float>(c);
+        } else {
+            upload_axis_tables<double>(c);
+            alloc_psi<double>(c);
+        }
+        // vacuum media
+        const double *noeps[3] = {nullptr, nullptr, nullptr};
+        if (c->fp32) build_media<float>(c, nullptr, noeps);
+        else build_media<double>(c, nullptr, noeps);
+        c->jbuf.alloc(9);
+        ck(cudaEventCreate(&c->t0), "event");
+        ck(cudaEventCreate(&c->t1), "event");
+        *out = C.release();
+        return OMX_OK;
+    } catch (const Fail &f) {
+        g_last_error = f.msg;
+        return f.code;
+    } catch (const std::exception &e) {
+        g_last_error = e.what();
+        return OMX_ERR_ARG;
+    }
+}
+
+int omx_destroy(omx_ctx *c)
+{
+    if (!c) return OMX_OK;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (auto &e : c->evs) {
+        cudaEventDestroy(e.a);
+        cudaEventDestroy(e.b);
+    }
+    if (c->gexec) cudaGraphExecDestroy(c->gexec);
+    if (c->t0) cudaEventDestroy(c->t0);
+    if (c->t1) cudaEventDestroy(c->t1);
+    cudaStream_t s = c->stream;
+    delete c;
+    if (s) cudaStreamDestroy(s);
+    return OMX_OK;
+}
+
+int omx_synchronize(omx_ctx *c)
+{
+    OMX_API_BEGIN
+    req(c, "null context");
+    ck(cudaStreamSynchronize(c->stream), "synchronize");
+    OMX_API_END(c)
+}
+
+int omx_get_cpml_tables(const omx_ctx *c, double *be, double *ce, double *bh, double *ch)
+{
+    OMX_API_BEGIN
+    req(c, "null context");
+    req(!c->T.be.empty(), "no CPML axis in this grid");
+    if (be) std::copy(c->T.be.begin(), c->T.be.end(), be);
+    if (ce) std::copy(c->T.ce.begin(), c->T.ce.end(), ce);
+    if (bh) std::copy(c->T.bh.begin(), c->T.bh.end(), bh);
+    if (ch) std::copy(c->T.ch.begin(), c->T.ch.end(), ch);
+    OMX_API_END(const_cast<omx_ctx *>(c))
+}
+
+int omx_get_den(const omx_ctx *c, int axis, double *den_e, double *den_h)
+{
+    OMX_API_BEGIN
+    req(c && axis >= 1 && axis <= 3, "bad axis");
+    const int a = axis - 1;
+    for (int k = 1; k <= c->n[a]; ++k) {
+        if (den_e) den_e[k - 1] = c->den_e[a][k];
+        if (den_h) den_h[k - 1] = c->den_h[a][k];
+    }
+    OMX_API_END(const_cast<omx_ctx *>(c))
+}
+
+int omx_compute_cpml_tables(int npml, double dr, double dt, double *be, double *ce, double *bh, double *ch,
+                            double *kappae, double *kappah)
+{
+    OMX_API_BEGIN
+    req(npml >= 2 && dr > 0 && dt > 0, "bad argument");
+    CpmlTables T = cpml_tables(npml, dr, dt);
+    if (be) std::copy(T.be.begin(), T.be.end(), be);
+    if (ce) std::copy(T.ce.begin(), T.ce.end(), ce);
+    if (bh) std::copy(T.bh.begin(), T.bh.end(), bh);
+    if (ch) std::copy(T.ch.begin(), T.ch.end(), ch);
+    if (kappae) std::copy(T.kappae.begin(), T.kappae.end(), kappae);
+    if (kappah) std::copy(T.kappah.begin(), T.kappah.end(), kappah);
+    OMX_API_END(nullptr)
+}
+
+int omx_set_cpml_tables(omx_ctx *c, const double *be, const double *ce, const double *bh, const double *ch,
+                        const double *dex, const double *dey, const double *dez, const double *dhx,
+                        const double *dhy, const double *dhz)
+{
+    OMX_API_BEGIN
+    req(c, "null context");
+    req(!c->started, "tables must be set before the first step", OMX_ERR_STATE);
+    const int npml = c->desc.npml;
+    if (be && ce && bh && ch && npml >= 2) {
+        c->T.be.assign(be, be + npml);
+        c->T.ce.assign(ce, ce + npml);
+        c->T.bh.assign(bh, bh + npml - 1);
+        c->T.ch.assign(ch, ch + npml - 1);
+    }
+    const double *de[3] = {dex, dey, dez}, *dh[3] = {dhx, dhy, dhz};
+    for (int a = 0; a < 3; ++a)
+        for (int k = 1; k <= c->n[a]; ++k) {
+            if (de[a]) c->den_e[a][k] = de[a][k - 1];
+            if (dh[a]) c->den_h[a][k] = dh[a][k - 1];
+        }
+    if (c->fp32) upload_axis_tables<float>(c);
+    else upload_axis_tables<double>(c);
+    OMX_API_END(c)
+}
+
+int omx_set_media(omx_ctx *c, int n_media, const omx_medium *media, const int32_t *media_map, const double *ex,
+                  const double *ey, const double *ez)
+{
+    OMX_API_BEGIN
+    req(c, "null context");
+    req(!c->started, "media must be set before the first step", OMX_ERR_STATE);
+    req(n_media >= 0 && n_media < 255, "n_media out of range");
+    req(n_media == 0 || media, "media descriptors missing");
+    c->n_media = n_media;
+    c->media.assign(media, media + n_media);
+    for (auto &m : c->media) {
+        req(m.medium_type >= OMX_NONE_MEDIUM && m.medium_type <= OMX_DL_MEDIUM, "medium_type");
+        if (m.medium_type == OMX_DL_MEDIUM) req(m.n_poles >= 1 && m.n_poles <= OMX_MAX_POLES, "n_poles");
+        if (m.medium_type == OMX_DIELECTRIC_MEDIUM) req(m.eps_r > 0, "dielectric eps_r must be positive");
+    }
+    const double *eps[3] = {ex, ey, ez};
+    if (c->fp32) build_media<float>(c, media_map, eps);
+    else build_media<double>(c, media_map, eps);
+    c->j_dirty = true;
+    OMX_API_END(c)
+}
+
+int omx_medium_dielectric(double eps_r, omx_medium *m)
+{
+    OMX_API_BEGIN
+    req(m, "null medium");
+    medium_dielectric(eps_r, m);
+    OMX_API_END(nullptr)
+}
+
+int omx_medium_drude(double omegaD, double GammaD, double eps_r, double dt, omx_medium *m)
+{
+    OMX_API_BEGIN
+    req(m && dt > 0, "bad argument");
+    medium_drude(omegaD, GammaD, eps_r, dt, m);
+    OMX_API_END(nullptr)
+}
+
+int omx_medium_dl_library(const char *material, double eps_r, double dt, omx_medium *m)
+{
+    OMX_API_BEGIN
+    req(material && m && dt > 0, "bad argument");
+    req(medium_dl_library(material, eps_r, dt, m), std::string("unknown Drude-Lorentz material ") + material);
+    OMX_API_END(nullptr)
+}
+
+int omx_medium_dl_custom(double eps_inf, double wp_ev, double gamma_ev, int n_poles, const double *pole_ev,
+                         const double *strength, const double *width_ev, double dt, omx_medium *m)
+{
+    OMX_API_BEGIN
+    req(m && dt > 0 && n_poles >= 1 && n_poles <= OMX_MAX_POLES && pole_ev && strength && width_ev, "bad argument");
+    medium_dl_custom(eps_inf, wp_ev, gamma_ev, n_poles, pole_ev, strength, width_ev, dt, m);
+    OMX_API_END(nullptr)
+}
+
+int omx_media_map_from_voxels(int dims, const int grid_Ndims[3], double dr, int n_media, const int *n_vox,
+                              const double *vox_nm, int32_t *media_map)
+{
+    OMX_API_BEGIN
+    req(dims >= 1 && dims <= 3 && grid_Ndims && media_map && dr > 0, "bad argument");
+    int n[3] = {grid_Ndims[0], dims >= 2 ? grid_Ndims[1] : 1, dims == 3 ? grid_Ndims[2] : 1};
+    media_map_from_voxels(dims, n, dr, n_media, n_vox, vox_nm, media_map);
+    OMX_API_END(nullptr)
+}
+
+int omx_step_H(omx_ctx *c)
+{
+    OMX_API_BEGIN
+    req(c, "null context");
+    prepare(c);
+    if (c->fp32) do_H<float>(c);
+    else do_H<double>(c);
+    ck(cudaPeekAtLastError(), "H launch");
+    OMX_API_END(c)
+}
+
+int omx_step_E(omx_ctx *c, double time, double t_skip)
+{
+    OMX_API_BEGIN
+    req(c, "null context");
+    prepare(c);
+    if (c->fp32) do_E<float>(c, imm(time), imm(t_skip));
+    else do_E<double>(c, imm(time), imm(t_skip));
+    ck(cudaPeekAtLastError(), "E launch");
+    OMX_API_END(c)
+}
+
+int omx_source_add(omx_ctx *c, const omx_source_desc *d, int *id)
+{
+    OMX_API_BEGIN
+    req(c && d, "null argument");
+    req(d->dir == 'x' || d->dir == 'y' || d->dir == 'z', "source direction must be x, y or z");
+    if (c->dims == 1) req(d->dir == 'x', "1D sources must be along x (interactions_mod.f90:43-53)");
+    if (c->dims == 2) {
+        if (c->desc.mode == OMX_TMZ_2D_MODE) req(d->dir == 'z', "TMz sources drive Ez");
+        else req(d->dir != 'z', "TEz sources drive Ex or Ey");
+    }
+    std::unique_ptr<SourceRec> S(new SourceRec);
+    S->kind = 0;
+    S->d = *d;
+    const double dr = c->desc.dr;
+    const int n_ker = (int)(d->radius / dr);   // source_mod.f90:71
+    const int side = 2 * n_ker + 1;
+    const int dims = c->dims;
+    std::vector<double> ker = source_kernel(dims, n_ker, dr);
+    const int npts = (int)ker.size();
+    S->comp = d->dir == 'x' ? 0 : (d->dir == 'y' ? 1 : 2);
+    S->avg = (dims == 1 || (dims == 2 && d->dir == 'z')) ? 0 : 1;
+    S->c_src = c->desc.dt / omx::consts().eps0 / dr / omx::consts().c0 / 2.0;   // interactions_mod.f90:32
+    // the next point along the source direction in the reference's column-major J_mat; the
+    // reference reads one element past the kernel array at its last point (taken as zero)
+    const int stride = d->dir == 'x' ? 1 : (d->dir == 'y' ? side : side * side);
+    int N[3] = {c->n[0], c->n[1], c->n[2]};
+    std::vector<long long> e;
+    std::vector<double> ka, kb;
+    const int kl = dims == 3 ? n_ker : 0, jl = dims >= 2 ? n_ker : 0;
+    int q = 0;
+    for (int k = -kl; k <= kl; ++k)
+        for (int j = -jl; j <= jl; ++j)
+            for (int i = -n_ker; i <= n_ker; ++i, ++q) {
+                // determine_indx_and_ranks (source_mod.f90:345-367)
+                const int ii = i + (int)(d->r0[0] / dr) + N[0] / 2;
+                const int jj = dims >= 2 ? j + (int)(d->r0[1] / dr) + N[1] / 2 : 0;
+                const int kk = dims == 3 ? k + (int)(d->r0[2] / dr) + N[2] / 2 : 0;
+                req(ii >= 0 && ii <= N[0] + 1 && jj >= 0 && jj <= N[1] + 1 && kk >= 0 && kk <= N[2] + 1,
+                    "source kernel extends outside the grid");
+                e.push_back(eindex(c, ii, jj, kk));
+                ka.push_back(ker[(size_t)q]);
+                kb.push_back(S->avg ? (q + stride < npts ? ker[(size_t)(q + stride)] : 0.0) : 0.0);
+            }
+    S->n = (int)e.size();
+    S->eidx.upload(e);
+    S->ka.upload(ka);
+    S->kb.upload(kb);
+    c->sources.push_back(std::move(S));
+    if (id) *id = (int)c->sources.size() - 1;
+    OMX_API_END(c)
+}
+
+int omx_plane_source_add(omx_ctx *c, const omx_plane_source_desc *d, int *id)
+{
+    OMX_API_BEGIN
+    req(c && d, "null argument");
+    req(d->comp >= 1 && d->comp <= 3 && d->plane_axis >= 1 && d->plane_axis <= c->dims, "plane source axis/comp");
+    req(c->field_used[d->comp - 1], "plane source component not present in this grid/mode");
+    req(d->plane_index >= 1 && d->plane_index <= c->n[d->plane_axis - 1], "plane index");
+    std::unique_ptr<SourceRec> S(new SourceRec);
+    S->kind = 1;
+    S->pd = *d;
+    S->comp = d->comp - 1;
+    S->avg = 0;
+    S->n = 0;
+    S->c_src = c->desc.dt / omx::consts().eps0 / c->desc.dr / omx::consts().c0 / 2.0;
+    c->sources.push_back(std::move(S));
+    if (id) *id = (int)c->sources.size() - 1;
+    OMX_API_END(c)
+}
+
+int omx_source_interactions(omx_ctx *c, double time)
+{
+    OMX_API_BEGIN
+    req(c, "null context");
+    prepare(c);
+    std::vector<StepParam> amps;
+    for (auto &s : c->sources) amps.push_back(imm(source_amp(*s, time)));
+    if (c->fp32) do_sources<float>(c, amps);
+    else do_sources<double>(c, amps);
+    ck(cudaPeekAtLastError(), "source launch");
+    OMX_API_END(c)
+}
+
+int omx_qgroup_state_size(int model) { return model == OMX_EMITTER_TWO_LEVEL ? 3 : (model == OMX_EMITTER_THREE_LEVEL ? 8 : -1); }
+
+int omx_qgroup_create(omx_ctx *c, const omx_qgroup_desc *d, const int32_t *cell, const double *params, int *gid)
+{
+    OMX_API_BEGIN
+    req(c && d && cell && params, "null argument");
+    req(!c->started, "q-groups must be created before the first step", OMX_ERR_STATE);
+    req(d->model == OMX_EMITTER_TWO_LEVEL || d->model == OMX_EMITTER_THREE_LEVEL, "emitter model");
+    req(d->group_type == OMX_Q_MATERIAL || d->group_type == OMX_Q_SINGLE, "group type");
+    req(d->n_systems >= 1 && d->dt > 0, "n_systems and dt must be positive");
+    std::unique_ptr<GroupRec> G(new GroupRec);
+    G->d = *d;
+    G->npar = d->model == OMX_EMITTER_TWO_LEVEL ? 7 : 9;
+    G->nst = omx_qgroup_state_size(d->model);
+    const int n = d->n_systems, dims = c->dims;
+    std::vector<int> ci(n), cj(n), ckk(n);
+    for (int e = 0; e < n; ++e) {
+        int ijk[3] = {cell[dims * e], dims >= 2 ? cell[dims * e + 1] : 0, dims == 3 ? cell[dims * e + 2] : 0};
+        for (int a = 0; a < dims; ++a) req(ijk[a] >= 1 && ijk[a] <= c->n[a], "emitter cell outside the grid");
+        ci[e] = ijk[0];
+        cj[e] = ijk[1];
+        ckk[e] = ijk[2];
+    }
+    G->ci.upload(ci);
+    G->cj.upload(cj);
+    G->ck.upload(ckk);
+    std::vector<double> par(params, params + (size_t)n * G->npar);
+    G->par.upload(par);
+    G->rho.alloc((size_t)n * G->nst);
+    G->E.alloc((size_t)n * 3);
+    G->dipole.alloc((size_t)n * 3);
+    G->dPdt.alloc((size_t)n * 3);
+    // J points written by this group, in the reference's write order
+    if (d->group_type == OMX_Q_MATERIAL) {
+        for (int e = 0; e < n; ++e) {
+            G->pts.push_back({cell_key(c, ci[e], cj[e], ckk[e]), d->density});
+            G->pts_owner.push_back(e);
+        }
+    } else {
+        const int nk = 3;   // q_group_mod.f90:19
+        std::vector<double> mk = qgroup_kernel(dims, nk);
+        const int side = 2 * nk + 1;
+        const int kl = dims == 3 ? nk : 0, jl = dims >= 2 ? nk : 0;
+        for (int e = 0; e < n; ++e)
+            for (int kk = -kl; kk <= kl; ++kk)
+                for (int jj = -jl; jj <= jl; ++jj)
+                    for (int ii = -nk; ii <= nk; ++ii) {
+                        const int p = (ii + nk) + side * ((jj + jl) + side * (kk + kl));
+                        const int pi = ci[e] + ii, pj = dims >= 2 ? cj[e] + jj : 0, pk = dims == 3 ? ckk[e] + kk : 0;
+                        if (pi < 1 || pi > c->n[0] + 1 || (dims >= 2 && (pj < 1 || pj > c->n[1] + 1)) ||
+                            (dims == 3 && (pk < 1 || pk > c->n[2] + 1)))
+                            continue;   // outside the reference's J arrays
+                        G->pts.push_back({cell_key(c, pi, pj, pk), d->density * mk[(size_t)p]});
+                        G->pts_owner.push_back(e);
+                    }
+    }
+    c->groups.push_back(std::move(G));
+    c->j_dirty = true;
+    if (gid) *gid = (int)c->groups.size() - 1;
+    OMX_API_END(c)
+}
+
+int omx_qgroup_step(omx_ctx *c, int gid, int tq_step)
+{
+    OMX_API_BEGIN
+    (void)tq_step;
+    req(c && gid >= 0 && gid < (int)c->groups.size(), "bad group id");
+    prepare(c);
+    if (c->fp32) do_group<float>(c, *c->groups[gid], imm(1.0));
+    else do_group<double>(c, *c->groups[gid], imm(1.0));
+    ck(cudaPeekAtLastError(), "emitter launch");
+    OMX_API_END(c)
+}
+
+int omx_qgroup_read(omx_ctx *c, int gid, double *dipole, double *dPdt, double *efield, double *rho)
+{
+    OMX_API_BEGIN
+    req(c && gid >= 0 && gid < (int)c->groups.size(), "bad group id");
+    GroupRec &g = *c->groups[gid];
+    ck(cudaStreamSynchronize(c->stream), "sync");
+    const size_t n = (size_t)g.d.n_systems;
+    if (dipole) ck(cudaMemcpy(dipole, g.dipole.p, n * 3 * sizeof(double), cudaMemcpyDeviceToHost), "read");
+    if (dPdt) ck(cudaMemcpy(dPdt, g.dPdt.p, n * 3 * sizeof(double), cudaMemcpyDeviceToHost), "read");
+    if (efield) ck(cudaMemcpy(efield, g.E.p, n * 3 * sizeof(double), cudaMemcpyDeviceToHost), "read");
+    if (rho) ck(cudaMemcpy(rho, g.rho.p, n * g.nst * sizeof(double), cudaMemcpyDeviceToHost), "read");
+    OMX_API_END(c)
+}
+
+int omx_detector_add(omx_ctx *c, int type, int field, int nd, const int32_t *idx, int *did)
+{
+    OMX_API_BEGIN
+    req(c && idx && nd >= 1, "bad argument");
+    req(type >= OMX_POINT_DETECTOR && type <= OMX_VOLUME_DETECTOR, "detector type");
+    req(field >= OMX_EX_FIELD && field <= OMX_HZ_FIELD, "field");
+    req(c->field_used[field - 1], "detector field not present in this grid/mode");
+    const int dims = c->dims;
+    for (int s = 0; s < nd; ++s) {
+        const int i = idx[s], j = dims >= 2 ? idx[nd + s] : 0, k = dims == 3 ? idx[2 * nd + s] : 0;
+        req(i >= 1 && i <= c->n[0] && (dims < 2 || (j >= 1 && j <= c->n[1])) && (dims < 3 || (k >= 1 && k <= c->n[2])),
+            "detector index outside the grid");
+        long long t[4] = {0, 0, 0, 0};
+        int nt = 1;
+        double w = 1.0;
+        auto E = [&](int a, int b, int cc) { return eindex(c, a, b, cc); };
+        // write_fields_subs_mod.f90 stencils
+        if (dims == 1) {
+            if (field == OMX_EX_FIELD) { t[0] = E(i, 0, 0); }
+            else { nt = 2; w = 0.5; t[0] = E(i - 1, 0, 0); t[1] = E(i, 0, 0); }   // :145
+        } else if (dims == 2) {
+            switch (field) {   // :346-369
+            case OMX_EX_FIELD: nt = 2; w = 0.5; t[0] = E(i - 1, j, 0); t[1] = E(i, j, 0); break;
+            case OMX_EY_FIELD: nt = 2; w = 0.5; t[0] = E(i, j - 1, 0); t[1] = E(i, j, 0); break;
+            case OMX_EZ_FIELD: t[0] = E(i, j, 0); break;
+            case OMX_HX_FIELD: nt = 2; w = 0.5; t[0] = E(i, j, 0); t[1] = E(i, j - 1, 0); break;
+            case OMX_HY_FIELD: nt = 2; w = 0.5; t[0] = E(i, j, 0); t[1] = E(i - 1, j, 0); break;
+            default: nt = 4; w = 0.25; t[0] = E(i, j, 0); t[1] = E(i - 1, j - 1, 0); t[2] = E(i - 1, j, 0); t[3] = E(i, j - 1, 0);
+            }
+        } else {
+            switch (field) {   // :821-846 (points), :865-929 (lines, planes, volumes)
+            case OMX_EX_FIELD: nt = 2; w = 0.5; t[0] = E(i - 1, j, k); t[1] = E(i, j, k); break;
+            case OMX_EY_FIELD: nt = 2; w = 0.5; t[0] = E(i, j - 1, k); t[1] = E(i, j, k); break;
+            case OMX_EZ_FIELD:
+                if (type == OMX_POINT_DETECTOR) { t[0] = E(i, j, k); }
+                else { nt = 2; w = 0.5; t[0] = E(i, j, k - 1); t[1] = E(i, j, k); }
+                break;
+            case OMX_HX_FIELD: nt = 4; w = 0.25; t[0] = E(i, j - 1, k); t[1] = E(i, j, k); t[2] = E(i, j, k - 1); t[3] = E(i, j - 1, k - 1); break;
+            case OMX_HY_FIELD: nt = 4; w = 0.25; t[0] = E(i - 1, j, k); t[1] = E(i, j, k); t[2] = E(i, j, k - 1); t[3] = E(i - 1, j, k - 1); break;
+            default: nt = 4; w = 0.25; t[0] = E(i, j, k); t[1] = E(i - 1, j, k); t[2] = E(i, j - 1, k); t[3] = E(i - 1, j - 1, k);
+            }
+        }
+        c->tap_field.push_back(field - 1);
+        c->tap_nt.push_back(nt);
+        c->tap_w.push_back(w);
+        for (int q = 0; q < 4; ++q) c->tap[q].push_back(t[q]);
+    }
+    c->dets.push_back({type, field, nd});
+    c->det_dirty = true;
+    if (did) *did = (int)c->dets.size() - 1;
+    OMX_API_END(c)
+}
+
+int omx_detectors_total_points(const omx_ctx *c) { return c ? (int)c->tap_field.size() : 0; }
+
+int omx_detectors_set_capacity(omx_ctx *c, int records)
+{
+    OMX_API_BEGIN
+    req(c && records >= 1, "bad argument");
+    prepare(c);
+    ensure_rec_capacity(c, records);
+    OMX_API_END(c)
+}
+
+int omx_detectors_record(omx_ctx *c, double time)
+{
+    OMX_API_BEGIN
+    req(c, "null context");
+    req(!c->tap_field.empty(), "no detectors");
+    prepare(c);
+    ensure_rec_capacity(c, c->rec_count + 1);
+    if (c->fp32) do_sample<float>(c, imm((double)c->rec_count), imm(time));
+    else do_sample<double>(c, imm((double)c->rec_count), imm(time));
+    ck(cudaPeekAtLastError(), "sample launch");
+    c->rec_count++;
+    OMX_API_END(c)
+}
+
+int omx_detectors_drain(omx_ctx *c, double *times, double *values, int max_records, int *n_records)
+{
+    OMX_API_BEGIN
+    req(c && n_records, "null argument");
+    ck(cudaStreamSynchronize(c->stream), "sync");
+    const int npts = (int)c->tap_field.size();
+    const int n = std::min(c->rec_count, max_records);
+    if (n > 0) {
+        if (times) ck(cudaMemcpy(times, c->rec_times.p, sizeof(double) * n, cudaMemcpyDeviceToHost), "drain");
+        if (values) ck(cudaMemcpy(values, c->rec.p, sizeof(double) * (size_t)n * npts, cudaMemcpyDeviceToHost), "drain");
+    }
+    // keep records beyond max_records (moved to the front through host memory)
+    if (n < c->rec_count) {
+        const size_t rest = (size_t)(c->rec_count - n);
+        std::vector<double> tv(rest), vv(rest * (size_t)npts);
+        ck(cudaMemcpy(tv.data(), c->rec_times.p + n, sizeof(double) * rest, cudaMemcpyDeviceToHost), "drain");
+        ck(cudaMemcpy(vv.data(), c->rec.p + (size_t)n * npts, sizeof(double) * vv.size(), cudaMemcpyDeviceToHost), "drain");
+        ck(cudaMemcpy(c->rec_times.p, tv.data(), sizeof(double) * rest, cudaMemcpyHostToDevice), "drain");
+        ck(cudaMemcpy(c->rec.p, vv.data(), sizeof(double) * vv.size(), cudaMemcpyHostToDevice), "drain");
+    }
+    c->rec_count -= n;
+    *n_records = n;
+    OMX_API_END(c)
+}
+
+int omx_run(omx_ctx *c, int tt0, int nsteps, int n_skip_steps, int t_det_print, int use_graph)
+{
+    OMX_API_BEGIN
+    req(c && nsteps >= 0 && n_skip_steps >= 1 && tt0 >= 1, "bad argument");
+    if (nsteps == 0) return OMX_OK;
+    if (c->fp32) run_impl<float>(c, tt0, nsteps, n_skip_steps, t_det_print, use_graph);
+    else run_impl<double>(c, tt0, nsteps, n_skip_steps, t_det_print, use_graph);
+    OMX_API_END(c)
+}
+
+int omx_field_bounds(const omx_ctx *c, int field, int lo[3], int hi[3])
+{
+    OMX_API_BEGIN
+    req(c && lo && hi, "null argument");
+    req(bounds_of(c, field, lo, hi), "field not present in this grid/mode");
+    OMX_API_END(const_cast<omx_ctx *>(c))
+}
+
+int omx_read_field(omx_ctx *c, int field, double *host)
+{
+    OMX_API_BEGIN
+    req(c && host, "null argument");
+    if (c->fp32) read_field_impl<float>(c, field, host);
+    else read_field_impl<double>(c, field, host);
+    OMX_API_END(c)
+}
+
+int omx_write_field(omx_ctx *c, int field, const double *host)
+{
+    OMX_API_BEGIN
+    req(c && host, "null argument");
+    if (c->fp32) write_field_impl<float>(c, field, host);
+    else write_field_impl<double>(c, field, host);
+    OMX_API_END(c)
+}
+
+int omx_profile_enable(omx_ctx *c, int on)
+{
+    OMX_API_BEGIN
+    req(c, "null context");
+    prof_collect(c);
+    c->prof = on != 0;
+    for (int k = 0; k < KC_N; ++k) {
+        c->prof_ms[k] = 0;
+        c->prof_n[k] = 0;
+    }
+    OMX_API_END(c)
+}
+
+int omx_profile_query(omx_ctx *c, int kc, double *total_ms, long long *launches)
+{
+    OMX_API_BEGIN
+    req(c && kc >= 0 && kc < KC_N, "bad argument");
+    prof_collect(c);
+    if (total_ms) *total_ms = c->prof_ms[kc];
+    if (launches) *launches = c->prof_n[kc];
+    OMX_API_END(c)
+}
+
+int omx_algorithmic_bytes(const omx_ctx *c, int kc, double *bytes)
+{
+    OMX_API_BEGIN
+    req(c && bytes, "null argument");
+    const double w = c->fp32 ? 4.0 : 8.0;
+    const double cells = (double)c->n[0] * c->n[1] * c->n[2];
+    // per-cell words: 3D H reads 6 / writes 3, E reads 6 / writes 3; 2D TMz/TEz H 5, E 4;
+    // 1D H 3, E 3.  CPML cells add psi read+write per component; media-box cells add the
+    // 1-byte material id per component and ADE cells their state.
+    double b = 0.0;
+    int ncomp_e = c->dims == 3 ? 3 : (c->dims == 1 ? 1 : (c->desc.mode == OMX_TMZ_2D_MODE ? 1 : 2));
+    int ncomp_h = c->dims == 3 ? 3 : (c->dims == 1 ? 1 : (c->desc.mode == OMX_TMZ_2D_MODE ? 2 : 1));
+    double psi_cells_h = 0.0, psi_cells_e = 0.0;   // component-cells carrying a psi term
+    for (int a = 0; a < c->dims; ++a) {
+        if (!c->cpml_axis[a]) continue;
+        double tr = 1.0;
+        for (int q = 0; q < c->dims; ++q)
+            if (q != a) tr *= c->n[q];
+        const double layers = 2.0 * (c->desc.npml - 1);
+        const int pc = c->dims == 3 ? 2 : 1;
+        psi_cells_h += layers * tr * pc;
+        psi_cells_e += layers * tr * pc;
+    }
+    if (kc == KC_H) {
+        b = cells * w * (ncomp_e + 2.0 * ncomp_h) + psi_cells_h * 2.0 * w;
+    } else if (kc == KC_E) {
+        b = cells * w * (ncomp_h + 2.0 * ncomp_e) + psi_cells_e * 2.0 * w + (double)c->bbV * ncomp_e;
+        if (c->has_ade) {
+            // count dispersive component cells and their state words
+            long long drude = 0, dl = 0;
+            for (int q = 0; q < 3; ++q)
+                for (size_t t = 0; t < c->host_mat[q].size(); ++t) {
+                    const int ty = c->cls_type[c->host_mat[q][t]];
+                    if (ty == CLS_DRUDE) drude++;
+                    else if (ty == CLS_DL) dl++;
+                }
+            b += (double)drude * 2.0 * w + (double)dl * (2.0 + 2.0 + 4.0 * c->P) * w;
+        }
+    } else {
+        b = 0.0;
+    }
+    *bytes = b;
+    OMX_API_END(const_cast<omx_ctx *>(c))
+}
+
+long long omx_launch_count(const omx_ctx *c) { return c ? c->launches : 0; }
+
+int omx_timer_start(omx_ctx *c)
+{
+    OMX_API_BEGIN
+    req(c, "null context");
+    ck(cudaEventRecord(c->t0, c->stream), "event");
+    OMX_API_END(c)
+}
+
+int omx_timer_stop(omx_ctx *c, float *ms)
+{
+    OMX_API_BEGIN
+    req(c && ms, "null argument");
+    ck(cudaEventRecord(c->t1, c->stream), "event");
+    ck(cudaEventSynchronize(c->t1), "event sync");
+    ck(cudaEventElapsedTime(ms, c->t0, c->t1), "elapsed");
+    OMX_API_END(c)
+}
+
+int omx_flush_l2(omx_ctx *c)
+{
+    OMX_API_BEGIN
+    req(c, "null context");
+    const long long n = 64LL << 20;   // 256 MB of floats, twice the L2
+    if (!c->flushbuf.p) c->flushbuf.alloc((size_t)n);
+    launch_flush(c->flushbuf.p, n, c->stream);
+    ck(cudaPeekAtLastError(), "flush");
+    OMX_API_END(c)
+}
+
+}  // extern "C"

@@ -1,0 +1,146 @@
+// omx_internal.h -- device-side data layout and kernel argument blocks.
+//
+// HBM layout (every field component, both precisions):
+//   element (i, j, k) lives at  off + i + px*j + pz*k  with i in [0, nx+1], j in [0, ny+1],
+//   k in [0, nz+1] (2D: k == 0; 1D: j == k == 0 and the only axis is i).  px is a multiple
+//   of 32 elements and off is chosen so that element i == 1 of every row starts on a 128-byte
+//   boundary: a warp reading 32 consecutive interior cells touches exactly one 128-byte line
+//   per row (FP32) or two (FP64).  The ghost layers i,j,k == 0 and n+1 hold the reference's
+//   boundary values (zero for PEC); periodic axes are closed by index remapping in the
+//   kernels instead of ghost copies.
+//
+// CPML auxiliary fields (psi) exist only inside the absorbing slabs: for each axis a and each
+// field kind (E or H) two components, stored over 2*(npml-1) layers (low face layers first,
+// then high face) x the two transverse axes, ordered so that consecutive i are consecutive in
+// memory.  Material ids (uint8, one per component) and the auxiliary-differential-equation
+// state exist only inside the bounding box of non-vacuum cells.
+#pragma once
+#include <stdint.h>
+
+namespace omx {
+
+enum KernelClass { KC_H = 0, KC_E = 1, KC_EMIT = 2, KC_SRC = 3, KC_DET = 4, KC_N = 5 };
+
+struct Lay {
+    int dims;
+    int nx, ny, nz;   // interior cells per axis (1D: nx = N, ny = nz = 1)
+    int px;           // row pitch in elements
+    long long pz;     // plane pitch in elements
+    long long off;    // element offset of (0,0,0)
+};
+
+// Scalar that is either an immediate value or table[*step] on the device (for graphs).
+struct StepParam {
+    double val;
+    const double *tab;
+    const int *step;
+};
+
+enum ClsType { CLS_PLAIN = 0, CLS_DRUDE = 1, CLS_DL = 2 };
+
+template <class R> struct ClsR {
+    int type;      // ClsType
+    int medium;    // index into the medium table (ADE classes)
+    R coef;        // dt_eps0 * eps_inv (plain classes)
+    R pad;
+};
+
+template <class R> struct MedR {
+    R A1, A2, C1, C2, C3, C4;
+    R al[8], be[8], ga[8], B1[8], B2[8];
+    int np;
+    int pad;
+};
+
+template <class R> struct GridArgs {
+    Lay L;
+    R dt_mu0, dt_eps0;
+    R dr;              // used by the exact path's CPML division
+    int per[3];        // periodic axes
+    int npml, L2;      // L2 = 2*(npml-1) psi layers per axis
+    const R *den_e[3], *den_h[3];
+    const R *bE[3], *cE[3], *bH[3], *cH[3];
+    const short *lE[3], *lH[3];
+    R *psiE[3][2], *psiH[3][2];
+    // media bounding box (1-based inclusive); empty when bb1 < bb0
+    int bb0[3], bb1[3], bbd[3];
+    long long bbV;
+    const uint8_t *mat[3];
+    const ClsR<R> *cls;
+    const MedR<R> *med;
+    R *ade;            // [comp][slot][bbV], slot 0 = PD, 1 = E_old, 2+p = PL, 2+P+p = PL_old
+    int P;             // poles per cell in the ADE state
+    int mode2d;        // 1 TMz, 2 TEz
+};
+
+template <class R> struct FieldPtrs {
+    R *f[6];           // Ex, Ey, Ez, Hx, Hy, Hz
+};
+
+struct JState {
+    int np;            // number of J points
+    double *J[3], *Jo[3], *dJ[3];
+};
+
+struct InjArgs {
+    int n;
+    const long long *eidx;
+    const int *comp;
+    const int *sa, *sb;
+    int avg;           // 1: 0.5*(J(i) + J(i+1)) average; 0: J(i) only
+};
+
+struct SrcArgs {
+    int n;
+    const long long *eidx;
+    const double *ka, *kb;
+    int comp;          // 0..2
+    int avg;
+    double c_src;
+};
+
+struct PlaneArgs {
+    int comp, axis, index;
+    double c_src;
+};
+
+struct EmitArgs {
+    int n, model, npar, nst, dims, mode2d;
+    const int *ci, *cj, *ck;
+    const double *par;
+    double *rho, *E, *dipole, *dPdt;
+    double dt;
+};
+
+struct ScatArgs {
+    int np, c0, c1;
+    const int *win;
+    const double *wk;
+    const double *dPdt;
+    double dt;
+};
+
+struct DetArgs {
+    int n;
+    const int *field;      // 0..5
+    const int *nt;
+    const double *w;
+    const long long *t0, *t1, *t2, *t3;
+    double *rec;           // [capacity][n]
+    double *times;
+};
+
+// ---- launchers (instantiated in omx_kernels_fast.cu / omx_kernels_exact.cu) ------------------
+template <class R> void launch_h(const FieldPtrs<R> &F, const GridArgs<R> &G, void *stream);
+template <class R> void launch_e(const FieldPtrs<R> &F, const GridArgs<R> &G, void *stream);
+template <class R> void launch_src(const FieldPtrs<R> &F, const SrcArgs &S, StepParam amp, void *stream);
+template <class R> void launch_plane(const FieldPtrs<R> &F, const Lay &L, const PlaneArgs &P, StepParam amp, void *stream);
+template <class R> void launch_inject(const FieldPtrs<R> &F, const JState &J, const InjArgs &I, StepParam time,
+                                      StepParam t_skip, double dt_eps0, void *stream);
+template <class R> void launch_emit(const FieldPtrs<R> &F, const Lay &L, const EmitArgs &A, StepParam move, void *stream);
+void launch_scatter(const JState &J, const ScatArgs &S, StepParam move, void *stream);
+template <class R> void launch_sample(const FieldPtrs<R> &F, const DetArgs &D, StepParam slot, StepParam time, void *stream);
+void launch_step_advance(int *step, void *stream);
+void launch_flush(float *buf, long long n, void *stream);
+
+}  // namespace omx

@@ -1,0 +1,73 @@
+// omx_kernels_exact.cu -- FP64 plain path (reference arithmetic) and the FP64 sparse kernels
+// used by both paths.  Compiled with -fmad=false: no multiply-add contraction, so every
+// expression rounds exactly as the FP64 CPU restatement does.
+#include <cuda_runtime.h>
+#include "omx_stencil.cuh"
+#include "omx_sparse.cuh"
+
+namespace omx {
+
+template <> void launch_h<double>(const FieldPtrs<double> &F, const GridArgs<double> &G, void *s)
+{
+    launch_h_impl<double, true>(F, G, s);
+}
+template <> void launch_e<double>(const FieldPtrs<double> &F, const GridArgs<double> &G, void *s)
+{
+    launch_e_impl<double, true>(F, G, s);
+}
+
+template <class R> void launch_src(const FieldPtrs<R> &F, const SrcArgs &S, StepParam amp, void *s)
+{
+    if (S.n <= 0) return;
+    k_src<R><<<(S.n + 127) / 128, 128, 0, (cudaStream_t)s>>>(F, S, amp);
+}
+template <class R> void launch_plane(const FieldPtrs<R> &F, const Lay &L, const PlaneArgs &P, StepParam amp, void *s)
+{
+    int n[3] = {L.nx, L.ny, L.nz};
+    int ax0 = (P.axis == 0) ? 1 : 0;
+    int ax1 = (P.axis == 2) ? 1 : 2;
+    int nb = (L.dims == 2) ? 1 : n[ax1];
+    dim3 g((n[ax0] + 127) / 128, nb, 1);
+    k_plane<R><<<g, 128, 0, (cudaStream_t)s>>>(F, L, P, amp);
+}
+template <class R> void launch_inject(const FieldPtrs<R> &F, const JState &J, const InjArgs &I, StepParam t,
+                                      StepParam ts, double dt_eps0, void *s)
+{
+    if (I.n <= 0) return;
+    k_inject<R><<<(I.n + 127) / 128, 128, 0, (cudaStream_t)s>>>(F, J, I, t, ts, dt_eps0);
+}
+template <class R> void launch_emit(const FieldPtrs<R> &F, const Lay &L, const EmitArgs &A, StepParam move, void *s)
+{
+    if (A.n <= 0) return;
+    k_emit<R><<<(A.n + 127) / 128, 128, 0, (cudaStream_t)s>>>(F, L, A, move);
+}
+void launch_scatter(const JState &J, const ScatArgs &S, StepParam move, void *s)
+{
+    if (S.np <= 0) return;
+    k_scatter<<<(S.np + 127) / 128, 128, 0, (cudaStream_t)s>>>(J, S, move);
+}
+template <class R> void launch_sample(const FieldPtrs<R> &F, const DetArgs &D, StepParam slot, StepParam time, void *s)
+{
+    const int n = D.n > 0 ? D.n : 1;
+    k_sample<R><<<(n + 127) / 128, 128, 0, (cudaStream_t)s>>>(F, D, slot, time);
+}
+void launch_step_advance(int *step, void *s)
+{
+    k_step_advance<<<1, 32, 0, (cudaStream_t)s>>>(step);
+}
+void launch_flush(float *buf, long long n, void *s)
+{
+    k_flush<<<152 * 8, 256, 0, (cudaStream_t)s>>>(buf, n);
+}
+
+#define OMX_INST(R)                                                                                      \
+    template void launch_src<R>(const FieldPtrs<R> &, const SrcArgs &, StepParam, void *);                \
+    template void launch_plane<R>(const FieldPtrs<R> &, const Lay &, const PlaneArgs &, StepParam, void *); \
+    template void launch_inject<R>(const FieldPtrs<R> &, const JState &, const InjArgs &, StepParam,      \
+                                   StepParam, double, void *);                                           \
+    template void launch_emit<R>(const FieldPtrs<R> &, const Lay &, const EmitArgs &, StepParam, void *); \
+    template void launch_sample<R>(const FieldPtrs<R> &, const DetArgs &, StepParam, StepParam, void *);
+OMX_INST(float)
+OMX_INST(double)
+
+}  // namespace omx

@@ -1,0 +1,248 @@
+// omx_sparse.cuh -- the small kernels around the stencil: source injection, emitter
+// gather / density-matrix step / current scatter, the emitter-current term of the E update,
+// and detector sampling.  All arithmetic here is FP64 (also on the FP32 field path) and is
+// compiled without FMA contraction so that it reproduces the FP64 CPU oracle bit for bit.
+#pragma once
+#include "omx_internal.h"
+
+namespace omx {
+
+__device__ __forceinline__ double sp_get(const StepParam &p)
+{
+    return p.tab ? p.tab[*p.step] : p.val;
+}
+
+// ---- source_interactions (interactions_mod.f90:21-163) ----------------------------------------
+// J_mat = amp*ker (amp = j_amp*envelope*cos, computed on the host with the reference's libm
+// calls); J_av = 0.5*(J_mat(p) + J_mat(p+1 along dir)); E += c_src*J_av.
+template <class R>
+__global__ void k_src(FieldPtrs<R> F, SrcArgs S, StepParam amp_p)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= S.n) return;
+    const double amp = sp_get(amp_p);
+    const double ja = amp * S.ka[q];
+    double jav;
+    if (S.avg) {
+        const double jb = amp * S.kb[q];
+        jav = 0.5 * (ja + jb);
+    } else {
+        jav = ja;
+    }
+    R *E = F.f[S.comp];
+    const long long e = S.eidx[q];
+    E[e] = (R)((double)E[e] + S.c_src * jav);
+}
+
+// Plane-wave soft source (extension): E_comp += c_src*amp on one plane of cells.
+template <class R>
+__global__ void k_plane(FieldPtrs<R> F, Lay L, PlaneArgs P, StepParam amp_p)
+{
+    const double amp = sp_get(amp_p);
+    if (amp == 0.0) return;
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    const int b = blockIdx.y;
+    int n[3] = {L.nx, L.ny, L.nz};
+    int ax0 = (P.axis == 0) ? 1 : 0;
+    int ax1 = (P.axis == 2) ? 1 : 2;
+    if (L.dims == 2) ax1 = -1;
+    if (a >= n[ax0]) return;
+    int c[3] = {0, 0, 0};
+    c[P.axis] = P.index;
+    c[ax0] = a + 1;
+    if (ax1 >= 0) {
+        if (b >= n[ax1]) return;
+        c[ax1] = b + 1;
+    }
+    R *E = F.f[P.comp];
+    const long long e = L.off + c[0] + (long long)L.px * c[1] + L.pz * c[2];
+    E[e] = (R)((double)E[e] + P.c_src * amp);
+}
+
+// ---- emitter current in the E update (mxll_3D_mod.f90:756-761 and 2D/1D analogues) --------
+// E -= dt_eps0 * Jav with Jav = 0.5*(J_old(i) + tt*dJ(i) + J_old(i+1) + tt*dJ(i+1)), tt =
+// time - t_skip, evaluated only at E components next to an emitter current point and
+// outside dispersive media (where the reference ignores J).
+template <class R>
+__global__ void k_inject(FieldPtrs<R> F, JState J, InjArgs I, StepParam time_p, StepParam tskip_p, double dt_eps0)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= I.n) return;
+    const double tt = sp_get(time_p) - sp_get(tskip_p);
+    const int c = I.comp[q];
+    const int a = I.sa[q], b = I.sb[q];
+    const double ao = (a >= 0) ? J.Jo[c][a] : 0.0, ad = (a >= 0) ? J.dJ[c][a] : 0.0;
+    double jav;
+    if (I.avg) {
+        const double bo = (b >= 0) ? J.Jo[c][b] : 0.0, bd = (b >= 0) ? J.dJ[c][b] : 0.0;
+        jav = 0.5 * (ao + tt * ad + bo + tt * bd);
+    } else {
+        jav = ao + tt * ad;
+    }
+    R *E = F.f[c];
+    const long long e = I.eidx[q];
+    E[e] = (R)((double)E[e] - dt_eps0 * jav);
+}
+
+// ---- few-level density-matrix emitters (new model behind TQ_sys_base%td_propagate) --------
+// State (FP64): 2-level [p_e, Re rho_eg, Im rho_eg]; 3-level (V system)
+// [p1, p2, Re r10, Im r10, Re r20, Im r20, Re r21, Im r21].  d rho/dt = -i[H0 - E_u V, rho]
+// + T1 population decay to the ground state + T2 coherence decay, RK4 with E_u held over dt.
+__device__ __forceinline__ void rhs2(const double *pr, double E_u, const double *rho, double *d)
+{
+    const double w0 = pr[0], mu = pr[1], T1 = pr[2], T2 = pr[3];
+    const double pe = rho[0], a = rho[1], b = rho[2];
+    const double pg = 1.0 - pe;
+    const double muE = mu * E_u;
+    d[0] = 2.0 * muE * b - pe / T1;
+    d[1] = w0 * b - a / T2;
+    d[2] = -(w0 * a) + muE * (pg - pe) - b / T2;
+}
+
+__device__ __forceinline__ void rhs3(const double *pr, double E_u, const double *rho, double *d)
+{
+    const double e1 = pr[0], e2 = pr[1], mu1 = pr[2], mu2 = pr[3], T1 = pr[4], T2 = pr[5];
+    const double p1 = rho[0], p2 = rho[1];
+    const double a10 = rho[2], b10 = rho[3], a20 = rho[4], b20 = rho[5], a21 = rho[6], b21 = rho[7];
+    const double p0 = 1.0 - p1 - p2;
+    const double g1 = mu1 * E_u, g2 = mu2 * E_u;
+    d[0] = 2.0 * g1 * b10 - p1 / T1;
+    d[1] = 2.0 * g2 * b20 - p2 / T1;
+    d[2] = e1 * b10 - g2 * b21 - a10 / T2;
+    d[3] = -(e1 * a10) + g1 * (p0 - p1) - g2 * a21 - b10 / T2;
+    d[4] = e2 * b20 + g1 * b21 - a20 / T2;
+    d[5] = -(e2 * a20) + g2 * (p0 - p2) - g1 * a21 - b20 / T2;
+    const double de = e2 - e1;
+    d[6] = de * b21 + g2 * b10 + g1 * b20 - a21 / T2;
+    d[7] = -(de * a21) + g2 * a10 - g1 * a20 - b21 / T2;
+}
+
+template <int NST>
+__device__ __forceinline__ void rk4(int model, const double *pr, double *rho, double E_u, double dt)
+{
+    double k1[NST], k2[NST], k3[NST], k4[NST], t[NST];
+    const double h2 = 0.5 * dt, h6 = dt / 6.0;
+    if (model == 1) rhs2(pr, E_u, rho, k1); else rhs3(pr, E_u, rho, k1);
+#pragma unroll
+    for (int q = 0; q < NST; ++q) t[q] = rho[q] + h2 * k1[q];
+    if (model == 1) rhs2(pr, E_u, t, k2); else rhs3(pr, E_u, t, k2);
+#pragma unroll
+    for (int q = 0; q < NST; ++q) t[q] = rho[q] + h2 * k2[q];
+    if (model == 1) rhs2(pr, E_u, t, k3); else rhs3(pr, E_u, t, k3);
+#pragma unroll
+    for (int q = 0; q < NST; ++q) t[q] = rho[q] + dt * k3[q];
+    if (model == 1) rhs2(pr, E_u, t, k4); else rhs3(pr, E_u, t, k4);
+#pragma unroll
+    for (int q = 0; q < NST; ++q) rho[q] = rho[q] + h6 * (k1[q] + 2.0 * k2[q] + 2.0 * k3[q] + k4[q]);
+}
+
+// send_E_to_J_ranks (interactions_mod.f90:656-691, 2D :486-526, 1D :329-346) fused with
+// td_propagate_q_group (q_group_mod.f90:813-816): gather E at the emitter cell, advance the
+// density matrix, dipole = Tr(rho V) along u, dPt_dt = (dipole - dip_old)/dt.
+template <class R>
+__global__ void k_emit(FieldPtrs<R> F, Lay L, EmitArgs A, StepParam move_p)
+{
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= A.n) return;
+    if (sp_get(move_p) == 0.0) return;
+    const int i = A.ci[n], j = A.cj[n], k = A.ck[n];
+    const long long c = L.off + i + (long long)L.px * j + L.pz * k;
+    double E[3] = {0.0, 0.0, 0.0};
+    if (A.dims == 3) {
+        E[0] = 0.5 * ((double)F.f[0][c - 1] + (double)F.f[0][c]);
+        E[1] = 0.5 * ((double)F.f[1][c - L.px] + (double)F.f[1][c]);
+        E[2] = 0.5 * ((double)F.f[2][c - L.pz] + (double)F.f[2][c]);
+    } else if (A.dims == 2) {
+        if (A.mode2d == 2) {
+            E[0] = 0.5 * ((double)F.f[0][c - 1] + (double)F.f[0][c]);
+            E[1] = 0.5 * ((double)F.f[1][c - L.px] + (double)F.f[1][c]);
+        } else {
+            E[2] = (double)F.f[2][c];
+        }
+    } else {
+        E[0] = (double)F.f[0][c];
+    }
+    const double *pr = A.par + (long long)n * A.npar;
+    const double *u = pr + (A.npar - 3);
+    const double E_u = u[0] * E[0] + u[1] * E[1] + u[2] * E[2];
+    double rho[8];
+    double *st = A.rho + (long long)n * A.nst;
+    double d;
+    if (A.model == 1) {
+#pragma unroll
+        for (int q = 0; q < 3; ++q) rho[q] = st[q];
+        rk4<3>(1, pr, rho, E_u, A.dt);
+#pragma unroll
+        for (int q = 0; q < 3; ++q) st[q] = rho[q];
+        d = 2.0 * pr[1] * rho[1];
+    } else {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) rho[q] = st[q];
+        rk4<8>(2, pr, rho, E_u, A.dt);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) st[q] = rho[q];
+        d = 2.0 * pr[2] * rho[2] + 2.0 * pr[3] * rho[4];
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const double old = A.dipole[3 * n + a];
+        const double nw = d * u[a];
+        A.dipole[3 * n + a] = nw;
+        A.dPdt[3 * n + a] = (nw - old) / A.dt;
+        A.E[3 * n + a] = E[a];
+    }
+}
+
+// send_J_to_E_ranks (interactions_mod.f90:1046-1220): J_old = J; J(point) = wk*dPt_dt of the
+// last emitter writing the point (assignment); dJ = (J - J_old)/dt.  Points this group does
+// not write keep J, so their dJ becomes zero, as with the reference's full-grid passes.
+__global__ void k_scatter(JState J, ScatArgs S, StepParam move_p)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= S.np) return;
+    if (sp_get(move_p) == 0.0) return;
+    const int w = S.win[p];
+    for (int c = S.c0; c <= S.c1; ++c) {
+        const double jo = J.J[c][p];
+        const double jn = (w >= 0) ? S.wk[p] * S.dPdt[3 * w + c] : jo;
+        J.Jo[c][p] = jo;
+        J.J[c][p] = jn;
+        J.dJ[c][p] = (jn - jo) / S.dt;
+    }
+}
+
+// ---- detector sampling (write_fields_subs_mod.f90 stencils) -------------------------------
+template <class R>
+__global__ void k_sample(FieldPtrs<R> F, DetArgs D, StepParam slot_p, StepParam time_p)
+{
+    const int slot = (int)sp_get(slot_p);
+    if (slot < 0) return;
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s == 0) D.times[slot] = sp_get(time_p);
+    if (s >= D.n) return;
+    const R *a = F.f[D.field[s]];
+    const int nt = D.nt[s];
+    double v = (double)a[D.t0[s]];
+    if (nt >= 2) {
+        v = v + (double)a[D.t1[s]];
+        if (nt == 4) {
+            v = v + (double)a[D.t2[s]];
+            v = v + (double)a[D.t3[s]];
+        }
+        v = D.w[s] * v;
+    }
+    D.rec[(long long)slot * D.n + s] = v;
+}
+
+__global__ void k_step_advance(int *step)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) *step = *step + 1;
+}
+
+__global__ void k_flush(float *buf, long long n)
+{
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x)
+        buf[q] = buf[q] * 0.5f + 1.0f;
+}
+
+}  // namespace omx

@@ -1,0 +1,179 @@
+"""GPU parity: the CUDA library (through its C-ABI) against the CPU FP64 oracle on the same
+seeded decks.
+
+FP64 plain path: bit-identical fields, detector samples and emitter dipoles (the kernels keep
+the reference's operand order and are compiled without FMA contraction); the bar stated for
+it is 1e-12 relative, checked first.  FP32 fused path: max relative detector-field error
+<= 1e-4 (normalised per detector by the max |field| of its trace), emitter dipoles <= 1e-3.
+"""
+import math
+
+import numpy as np
+import pytest
+
+import omx
+from omx import decks
+from gpu_harness import compare_fields, make_pair, run_both, step_loop, trace_error
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-12
+FP32_TOL = 1e-4
+
+
+def small_cfg1():
+    return decks.deck_cfg1(n=32, radius_nm=8.0, npml=6, steps=80)
+
+
+def small_cfg2():
+    return decks.deck_cfg2(nx=240, ny=160, n_emitters=300, npml=8, pitch_nm=120.0, hole_nm=40.0, film_nm=20.0)
+
+
+def small_cfg3():
+    return decks.deck_cfg3(n=64, n_emitters=400, npml=6)
+
+
+def small_cfg5():
+    return decks.deck_cfg5_instance(36, seed=5, npml=6)
+
+
+def tez_single_group_deck():
+    """2D TEz, CPML x / periodic y, Drude disc, radial x-source, a `single` q-group (7x7 kernels)
+    and a second `material` group sharing cells (last writer wins across groups)."""
+    d = decks._base(2, (96, 80), 8, (3, 2, 1), 2.0, mode=2)
+    n = (96, 80)
+    g = np.arange(1, 97)
+    I, J = np.meshgrid(np.arange(1, 97), np.arange(1, 81), indexing="ij")
+    disc = (I - 60.5) ** 2 + (J - 40.5) ** 2 <= 64
+    d["media"].append(dict(kind="drude", omegaD=8.0, GammaD=0.3, eps_r=2.0))
+    d["voxels"].append(np.stack([decks._cell_nm(I[disc], 96, 2.0), decks._cell_nm(J[disc], 80, 2.0)], axis=1))
+    ev, fs = omx.UNITS["ev_to_au"], omx.UNITS["fs_to_au"]
+    d["sources"].append(dict(dir="x", j_amp=1.0, w0=2.5 * ev, t0=6 * fs, tau=2 * fs, r0=[-30 * 2 * decks.NM, 0.0],
+                             radius=2.2 * d["dr"], t_init=0.0, t_final=1e30, phase=0.3, chirp=0.0))
+    rng = np.random.default_rng(9)
+    ne = 40
+    cells = np.stack([rng.integers(30, 50, ne), rng.integers(20, 60, ne)], axis=1).astype(np.int32)
+    par = np.stack([rng.normal(2.5, 0.05, ne) * ev, np.full(ne, 8 * decks.DEBYE), np.full(ne, 500 * fs),
+                    np.full(ne, 50 * fs), np.full(ne, 0.6), np.full(ne, 0.8), np.zeros(ne)], axis=1)
+    d["groups"].append(dict(group_type=2, model=1, cells=cells, params=par, density=2e-3 / decks.NM ** 3, dt=d["dt"]))
+    cells2 = cells[:10] + np.array([1, 0], np.int32)
+    par2 = np.stack([np.full(10, 2.4 * ev), np.full(10, 6 * decks.DEBYE), np.full(10, 300 * fs), np.full(10, 40 * fs),
+                     np.ones(10), np.zeros(10), np.zeros(10)], axis=1)
+    d["groups"].append(dict(group_type=1, model=1, cells=cells2, params=par2, density=1e-3 / decks.NM ** 3,
+                            dt=d["dt"]))
+    for p in ([20, 20], [70, 60], [50, 11]):
+        for f in (1, 2, 6):
+            d["detectors"].append(dict(type=1, field=f, idx=np.array([p], np.int32)))
+    return d
+
+
+def one_d_deck():
+    """1D CPML, library Ag Drude-Lorentz slab, point source, three-level material group."""
+    d = decks._base(1, (400,), 12, (3,), 1.0)
+    ev, fs = omx.UNITS["ev_to_au"], omx.UNITS["fs_to_au"]
+    d["media"].append(dict(kind="dl_library", material="Ag", eps_r=1.0))
+    d["voxels"].append(decks._cell_nm(np.arange(260, 300), 400, 1.0).reshape(-1, 1))
+    d["sources"].append(dict(dir="x", j_amp=1.0, w0=3.0 * ev, t0=3 * fs, tau=1 * fs, r0=[-50 * decks.NM], radius=0.0,
+                             t_init=0.0, t_final=1e30, phase=0.0, chirp=0.0))
+    ne = 5
+    cells = np.array([[230], [231], [231], [240], [305]], np.int32)
+    par = np.tile([2.9 * ev, 3.1 * ev, 5 * decks.DEBYE, 7 * decks.DEBYE, 800 * fs, 60 * fs, 1.0, 0.0, 0.0], (ne, 1))
+    d["groups"].append(dict(group_type=1, model=2, cells=cells, params=par, density=5e-3 / decks.NM ** 3, dt=d["dt"]))
+    for k in (100, 250, 280, 330):
+        for f in (1, 5):
+            d["detectors"].append(dict(type=1, field=f, idx=np.array([[k]], np.int32)))
+    return d
+
+
+def periodic_box_deck():
+    """3D periodic on all axes with a dielectric block and a radial y-source; line/plane detectors."""
+    d = decks._base(3, (24, 20, 16), 4, (2, 2, 2), 2.0)
+    I, J, K = np.meshgrid(np.arange(8, 14), np.arange(5, 12), np.arange(6, 10), indexing="ij")
+    d["media"].append(dict(kind="dielectric", eps_r=4.0))
+    d["voxels"].append(np.stack([decks._cell_nm(I.ravel(), 24, 2.0), decks._cell_nm(J.ravel(), 20, 2.0),
+                                 decks._cell_nm(K.ravel(), 16, 2.0)], axis=1))
+    ev, fs = omx.UNITS["ev_to_au"], omx.UNITS["fs_to_au"]
+    d["sources"].append(dict(dir="y", j_amp=2.0, w0=2.0 * ev, t0=4 * fs, tau=1.5 * fs, r0=[10 * decks.NM, 0.0, 0.0],
+                             radius=1.5 * d["dr"], t_init=0.0, t_final=1e30, phase=0.0, chirp=0.0))
+    line = np.array([[i, 3, 4] for i in range(1, 25)], np.int32)
+    plane = np.array([[i, j, 8] for j in range(1, 21) for i in range(1, 25)], np.int32)
+    for f in range(1, 7):
+        d["detectors"].append(dict(type=2, field=f, idx=line))
+    d["detectors"].append(dict(type=5, field=3, idx=plane))
+    return d
+
+
+CASES = {
+    "cfg1_small": (small_cfg1, 70),
+    "cfg2_small": (small_cfg2, 300),
+    "cfg3_small": (small_cfg3, 60),
+    "cfg5_small": (small_cfg5, 60),
+    "tez_single": (tez_single_group_deck, 120),
+    "one_d": (one_d_deck, 500),
+    "periodic": (periodic_box_deck, 80),
+}
+
+
+@pytest.fixture(scope="module")
+def orc_mod(orc):
+    return orc
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_fp64_matches_oracle(orc_mod, case):
+    make, steps = CASES[case]
+    deck = make()
+    gpu, cpu, gg, cg, tc, tg = run_both(orc_mod, deck, steps, "fp64", "calls")
+    err = compare_fields(gpu, cpu, deck)
+    assert err <= FP64_TOL, err
+    assert tg.shape == tc.shape
+    assert trace_error(tg, tc) <= FP64_TOL
+    # bit-identical is what the exact path delivers
+    assert err == 0.0 and np.array_equal(tg, tc), (err, np.max(np.abs(tg - tc)))
+    for a, b in zip(gg, cg):
+        ga, cb = a.read(), cpu.q_group_read(b)
+        for key in ("dipole", "dPt_dt", "E", "rho"):
+            assert np.array_equal(ga[key], cb[key]), key
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_device_loop_matches_calls(orc_mod, case):
+    """omx_run (device-side loop, with and without a CUDA graph) equals the per-call API."""
+    make, steps = CASES[case]
+    deck = make()
+    steps = min(steps, 60)
+    for graph in (False, True):
+        gpu, cpu, gg, cg, tc, tg = run_both(orc_mod, deck, steps, "fp64", "run", use_graph=graph)
+        assert compare_fields(gpu, cpu, deck) == 0.0
+        assert np.array_equal(tg, tc)
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_fp32_within_tolerance(orc_mod, case):
+    make, steps = CASES[case]
+    deck = make()
+    gpu, cpu, gg, cg, tc, tg = run_both(orc_mod, deck, steps, "fp32", "run", use_graph=True)
+    err = trace_error(tg, tc)
+    assert err <= FP32_TOL, err
+    for a, b in zip(gg, cg):
+        ga, cb = a.read(), cpu.q_group_read(b)
+        ref = max(np.max(np.abs(cb["dipole"])), 1e-300)
+        assert np.max(np.abs(ga["dipole"] - cb["dipole"])) / ref <= 1e-3
+
+
+def test_long_run_fp64_cfg1_shape(orc_mod):
+    """A longer plain 3D run (Au sphere, plane wave, CPML) keeps bit parity over 400 steps."""
+    deck = decks.deck_cfg1(n=40, radius_nm=10.0, npml=8)
+    gpu, cpu, gg, cg, tc, tg = run_both(orc_mod, deck, 400, "fp64", "run", use_graph=True)
+    assert compare_fields(gpu, cpu, deck) == 0.0
+    assert np.array_equal(tg, tc)
+
+
+def test_media_after_start_is_rejected(orc_mod):
+    deck = small_cfg1()
+    gpu = omx.TMxll(3, deck["grid_Ndims"], deck["npml"], deck["boundaries"], deck["dt"], deck["dr"])
+    gpu.td_propagate_H_field()
+    with pytest.raises(omx.OMXError):
+        gpu.set_media([omx.medium_dielectric(2.0)], np.zeros((32, 32, 32, 3), np.int32))
+    with pytest.raises(omx.OMXError):
+        omx.TMxll(3, (40, 40, 40), 25, (3, 3, 3), deck["dt"], deck["dr"])   # two CPML slabs do not fit
