@@ -220,7 +220,9 @@ int omx_run(omx_ctx *ctx, int tt0, int nsteps, int n_skip_steps, int t_det_print
 
 /* ---- field access (debug / parity) ---------------------------------------------------------- */
 /* Copies a field over the reference's bounds (e.g. 3D Ex(0:nx,1:ny+1,1:nz+1)) to/from host
- * FP64.  Ghost planes of periodic axes are implicit on the device and read back as zero. */
+ * FP64.  The E ghost planes n+1 of periodic axes are closed by index remapping on the device and
+ * read back as zero; the H ghost planes 0 of periodic axes hold the wrapped values, as in the
+ * reference after its E-step wraps. */
 int omx_field_bounds(const omx_ctx *ctx, int field, int lo[3], int hi[3]);
 int omx_read_field(omx_ctx *ctx, int field, double *host);
 int omx_write_field(omx_ctx *ctx, int field, const double *host);

@@ -134,6 +134,9 @@ struct omx_ctx {
     DevBuf<double> aded;
     int P = 1;
     bool has_ade = false;
+    DevBuf<int4> ade_ent;   // dispersive component-cells (i, j, k, component)
+    DevBuf<int> ade_b;      // their media-box index
+    int ade_n = 0;
     std::vector<uint8_t> host_mat[3];   // class per component over the box (for injection checks)
     std::vector<int> cls_type;          // per class id
     // sources
@@ -413,6 +416,9 @@ template <class R> GridArgs<R> grid_args(omx_ctx *c)
     G.ade = adebuf<R>(c).p;
     G.P = c->P;
     G.mode2d = c->desc.mode;
+    G.ade_n = c->ade_n;
+    G.ade_ent = c->ade_ent.p;
+    G.ade_b = c->ade_b.p;
     return G;
 }
 
@@ -547,6 +553,26 @@ void build_media(omx_ctx *c, const int32_t *map, const double *eps[3])
     c->has_ade = any_ade;
     if (any_ade) adebuf<R>(c).alloc((size_t)(3LL * (2 + 2 * c->P) * c->bbV));
     else adebuf<R>(c).release();
+    // compact list of dispersive component-cells inside the E-update range
+    std::vector<int4> ent;
+    std::vector<int> eb;
+    if (any_ade) {
+        for (int k = b0[2]; k <= b1[2]; ++k)
+            for (int j = b0[1]; j <= b1[1]; ++j)
+                for (int i = b0[0]; i <= b1[0]; ++i) {
+                    if (dims == 1 && (i < 2 || i > nx - 1)) continue;   // mxll_1D_mod.f90:320
+                    const long long b = (i - b0[0]) + (long long)bd[0] * ((j - b0[1]) + (long long)bd[1] * (k - b0[2]));
+                    for (int q = 0; q < comps; ++q) {
+                        if (!act[q]) continue;
+                        if (c->cls_type[c->host_mat[q][(size_t)b]] == CLS_PLAIN) continue;
+                        ent.push_back(make_int4(i, dims >= 2 ? j : 0, dims == 3 ? k : 0, q));
+                        eb.push_back((int)b);
+                    }
+                }
+    }
+    c->ade_n = (int)ent.size();
+    c->ade_ent.upload(ent);
+    c->ade_b.upload(eb);
 }
 
 int comp_axis_active(const omx_ctx *c, int q)
@@ -921,10 +947,12 @@ template <class R> void read_field_impl(omx_ctx *c, int field, double *host)
     for (int k = lo[2]; k <= hi[2]; ++k)
         for (int j = lo[1]; j <= hi[1]; ++j)
             for (int i = lo[0]; i <= hi[0]; ++i) {
+                // E ghost planes n+1 of periodic axes are closed by index remapping on the device
+                // (not stored); H ghost planes 0 hold the wrapped values as in the reference
                 bool ghost_periodic = false;
                 const int ijk[3] = {i, j, k};
                 for (int a = 0; a < c->dims; ++a)
-                    if (c->per[a] && (ijk[a] == 0 || ijk[a] == c->n[a] + 1)) ghost_periodic = true;
+                    if (field <= OMX_EZ_FIELD && c->per[a] && ijk[a] == c->n[a] + 1) ghost_periodic = true;
                 host[o++] = ghost_periodic ? 0.0 : (double)tmp[(size_t)eindex(c, i, j, k)];
             }
 }

@@ -71,6 +71,11 @@ template <class R> struct GridArgs {
     R *ade;            // [comp][slot][bbV], slot 0 = PD, 1 = E_old, 2+p = PL, 2+P+p = PL_old
     int P;             // poles per cell in the ADE state
     int mode2d;        // 1 TMz, 2 TEz
+    // dispersive component-cells, updated by their own kernel before the bulk E pass:
+    // (i, j, k, component) and the media-box index of each
+    int ade_n;
+    const int4 *ade_ent;
+    const int *ade_b;
 };
 
 template <class R> struct FieldPtrs {

@@ -33,11 +33,10 @@ __device__ __forceinline__ R psi2(R b, R psi, R c, R d, R dr)
 }
 
 // Auxiliary-differential-equation update of one dispersive E component
-// (get_medium_polarization, classical_medium_mod.f90:773-833).  Kept out of line: only cells
-// inside dispersive media take this path, and inlining it would raise the register count of
-// the whole stencil.  ADE state lives at ade[(c*(2+2P) + slot)*bbV + b].
+// (get_medium_polarization, classical_medium_mod.f90:773-833).  ADE state lives at
+// ade[(c*(2+2P) + slot)*bbV + b].
 template <class R>
-__device__ __noinline__ R ade_update(R e, R rot, ClsR<R> cl, int c, long long b, const GridArgs<R> &G)
+__device__ __forceinline__ R ade_update(R e, R rot, const ClsR<R> &cl, int c, long long b, const GridArgs<R> &G)
 {
     const MedR<R> &m = G.med[cl.medium];
     R *st = G.ade + (long long)c * (2 + 2 * G.P) * G.bbV + b;
@@ -72,14 +71,54 @@ __device__ __noinline__ R ade_update(R e, R rot, ClsR<R> cl, int c, long long b,
     return t;
 }
 
-// Material update of one E component inside the media box: plain (vacuum / dielectric:
-// E + dt_eps0*eps_inv*rotH) or the ADE path.
+// Bulk update of one E component inside the media box.  Vacuum and dielectric classes update
+// here (E + dt_eps0*eps_inv*rotH); dispersive classes were already advanced by k_ade in this
+// half-step and only receive their CPML terms from the bulk pass.
 template <class R>
-__device__ __forceinline__ R medium_update(R e, R rot, int cls_id, int c, long long b, const GridArgs<R> &G)
+__device__ __forceinline__ R plain_update(R e, R rot, int cls_id, const GridArgs<R> &G)
 {
     const ClsR<R> cl = G.cls[cls_id];
-    if (cl.type == CLS_PLAIN) return e + cl.coef * rot;
-    return ade_update<R>(e, rot, cl, c, b, G);
+    return cl.type == CLS_PLAIN ? e + cl.coef * rot : e;
+}
+
+// curl H of component c at (i,j,k) with the bulk kernels' expressions and periodic remaps
+template <class R>
+__device__ __forceinline__ R curl_h(const FieldPtrs<R> &F, const GridArgs<R> &G, int c, int i, int j, int k)
+{
+    const Lay &L = G.L;
+    const long long idx = L.off + i + (long long)L.px * j + L.pz * k;
+    const long long mx = (i == 1 && G.per[0]) ? (long long)(L.nx - 1) : -1LL;
+    if (L.dims == 1) return (F.f[4][idx - 1] - F.f[4][idx]) * G.den_e[0][i];
+    const long long my = (j == 1 && G.per[1]) ? (long long)(L.ny - 1) * L.px : -(long long)L.px;
+    if (L.dims == 2) {
+        if (G.mode2d == 1)
+            return (F.f[4][idx] - F.f[4][idx + mx]) * G.den_e[0][i] + (F.f[3][idx + my] - F.f[3][idx]) * G.den_e[1][j];
+        if (c == 0) return (F.f[5][idx] - F.f[5][idx + my]) * G.den_e[1][j];
+        return (F.f[5][idx + mx] - F.f[5][idx]) * G.den_e[0][i];
+    }
+    const long long mz = (k == 1 && G.per[2]) ? (long long)(L.nz - 1) * L.pz : -L.pz;
+    if (c == 0)
+        return (F.f[5][idx] - F.f[5][idx + my]) * G.den_e[1][j] + (F.f[4][idx + mz] - F.f[4][idx]) * G.den_e[2][k];
+    if (c == 1)
+        return (F.f[5][idx + mx] - F.f[5][idx]) * G.den_e[0][i] + (F.f[3][idx] - F.f[3][idx + mz]) * G.den_e[2][k];
+    return (F.f[4][idx] - F.f[4][idx + mx]) * G.den_e[0][i] + (F.f[3][idx + my] - F.f[3][idx]) * G.den_e[1][j];
+}
+
+// Dispersive cells (compact list): the ADE part of the E update, run before the bulk pass.
+template <class R>
+__global__ void k_ade(FieldPtrs<R> F, GridArgs<R> G)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= G.ade_n) return;
+    const int4 en = G.ade_ent[q];
+    const int b = G.ade_b[q];
+    const int c = en.w;
+    const R rot = curl_h<R>(F, G, c, en.x, en.y, en.z);
+    const Lay &L = G.L;
+    const long long idx = L.off + en.x + (long long)L.px * en.y + L.pz * en.z;
+    const ClsR<R> cl = G.cls[G.mat[c][b]];
+    R *E = F.f[c];
+    E[idx] = ade_update<R>(E[idx], rot, cl, c, b, G);
 }
 
 // ===================================================================================== 3D
@@ -148,6 +187,22 @@ __global__ void __launch_bounds__(128) k_h3(FieldPtrs<R> F, GridArgs<R> G, int k
         Hx[idx] = hx;
         Hy[idx] = hy;
         Hz[idx] = hz;
+        // periodic ghost planes H(0) = H(n) (mxll_3D_mod.f90:725-738); the wraps run one after the
+        // other over whole planes, so a corner ghost ends up equal to H(n, n, .) as well
+        const bool gx = G.per[0] && i == L.nx, gy = G.per[1] && j == L.ny, gz = G.per[2] && k == L.nz;
+        if (gx | gy | gz) {
+            const long long ox = gx ? -(long long)L.nx : 0, oy = gy ? -(long long)L.ny * L.px : 0;
+            const long long oz = gz ? -(long long)L.nz * L.pz : 0;
+            if (gy) Hx[idx + oy] = hx;
+            if (gz) Hx[idx + oz] = hx;
+            if (gy && gz) Hx[idx + oy + oz] = hx;
+            if (gx) Hy[idx + ox] = hy;
+            if (gz) Hy[idx + oz] = hy;
+            if (gx && gz) Hy[idx + ox + oz] = hy;
+            if (gx) Hz[idx + ox] = hz;
+            if (gy) Hz[idx + oy] = hz;
+            if (gx && gy) Hz[idx + ox + oy] = hz;
+        }
         ex_c = ex_kp;
         ey_c = ey_kp;
     }
@@ -188,9 +243,9 @@ __global__ void __launch_bounds__(128) k_e3(FieldPtrs<R> F, GridArgs<R> G, int k
         R ex = Ex[idx], ey = Ey[idx], ez = Ez[idx];
         if (bb_ij && k >= G.bb0[2] && k <= G.bb1[2]) {
             const long long b = (i - G.bb0[0]) + (long long)G.bbd[0] * ((j - G.bb0[1]) + (long long)G.bbd[1] * (k - G.bb0[2]));
-            ex = medium_update<R>(ex, rx, G.mat[0][b], 0, b, G);
-            ey = medium_update<R>(ey, ry, G.mat[1][b], 1, b, G);
-            ez = medium_update<R>(ez, rz, G.mat[2][b], 2, b, G);
+            ex = plain_update<R>(ex, rx, G.mat[0][b], G);
+            ey = plain_update<R>(ey, ry, G.mat[1][b], G);
+            ez = plain_update<R>(ez, rz, G.mat[2][b], G);
         } else {
             ex = ex + dt_eps0 * rx;
             ey = ey + dt_eps0 * ry;
@@ -276,6 +331,9 @@ __global__ void __launch_bounds__(128) k_h2(FieldPtrs<R> F, GridArgs<R> G, int j
             }
             Hx[idx] = hx;
             Hy[idx] = hy;
+            // periodic ghosts Hy(0,:) = Hy(nx,:), Hx(:,0) = Hx(:,ny) (mxll_2D_mod.f90:666-672)
+            if (G.per[0] && i == L.nx) Hy[idx - L.nx] = hy;
+            if (G.per[1] && j == L.ny) Hx[idx - (long long)L.ny * L.px] = hx;
             ez_c = ez_jp;
         }
     } else {
@@ -301,6 +359,13 @@ __global__ void __launch_bounds__(128) k_h2(FieldPtrs<R> F, GridArgs<R> G, int j
                 hz = hz + dt_mu0 * v;
             }
             Hz[idx] = hz;
+            // periodic ghosts Hz(0,:) = Hz(nx,:) then Hz(:,0) = Hz(:,ny) (mxll_2D_mod.f90:757-763)
+            {
+                const bool gx = G.per[0] && i == L.nx, gy = G.per[1] && j == L.ny;
+                if (gx) Hz[idx - L.nx] = hz;
+                if (gy) Hz[idx - (long long)L.ny * L.px] = hz;
+                if (gx && gy) Hz[idx - L.nx - (long long)L.ny * L.px] = hz;
+            }
             ex_c = ex_jp;
         }
     }
@@ -332,7 +397,7 @@ __global__ void __launch_bounds__(128) k_e2(FieldPtrs<R> F, GridArgs<R> G, int j
             R ez = Ez[idx];
             if (bb_i && j >= G.bb0[1] && j <= G.bb1[1]) {
                 const long long b = (i - G.bb0[0]) + (long long)G.bbd[0] * (j - G.bb0[1]);
-                ez = medium_update<R>(ez, r, G.mat[2][b], 2, b, G);
+                ez = plain_update<R>(ez, r, G.mat[2][b], G);
             } else {
                 ez = ez + dt_eps0 * r;
             }
@@ -364,8 +429,8 @@ __global__ void __launch_bounds__(128) k_e2(FieldPtrs<R> F, GridArgs<R> G, int j
             R ex = Ex[idx], ey = Ey[idx];
             if (bb_i && j >= G.bb0[1] && j <= G.bb1[1]) {
                 const long long b = (i - G.bb0[0]) + (long long)G.bbd[0] * (j - G.bb0[1]);
-                ex = medium_update<R>(ex, rx, G.mat[0][b], 0, b, G);
-                ey = medium_update<R>(ey, ry, G.mat[1][b], 1, b, G);
+                ex = plain_update<R>(ex, rx, G.mat[0][b], G);
+                ey = plain_update<R>(ey, ry, G.mat[1][b], G);
             } else {
                 ex = ex + dt_eps0 * rx;
                 ey = ey + dt_eps0 * ry;
@@ -426,7 +491,7 @@ __global__ void k_e1(FieldPtrs<R> F, GridArgs<R> G)
     R ex = Ex[idx];
     if (i >= G.bb0[0] && i <= G.bb1[0]) {
         const long long b = i - G.bb0[0];
-        ex = medium_update<R>(ex, r, G.mat[0][b], 0, b, G);
+        ex = plain_update<R>(ex, r, G.mat[0][b], G);
     } else {
         ex = ex + G.dt_eps0 * r;
     }
@@ -464,6 +529,7 @@ void launch_e_impl(const FieldPtrs<R> &F, const GridArgs<R> &G, void *stream)
 {
     cudaStream_t s = (cudaStream_t)stream;
     const Lay &L = G.L;
+    if (G.ade_n > 0) k_ade<R><<<(G.ade_n + 127) / 128, 128, 0, s>>>(F, G);
     if (L.dims == 3) {
         dim3 b(32, 4, 1), g((L.nx + 31) / 32, (L.ny + 3) / 4, (L.nz + KCH3 - 1) / KCH3);
         k_e3<R, EXACT><<<g, b, 0, s>>>(F, G, KCH3);

@@ -1717,25 +1717,26 @@ void orc_plane_source_apply(orc_grid *g, const orc_plane_source_desc *d, double 
  * Ground populations are 1 - sum of excited populations.
  * Equation: d rho/dt = -i[H0 - E_u V, rho] + relaxation, with V the dipole operator
  * (couplings ground<->excited), T1 population decay to the ground state and T2
- * coherence decay.  Integrated with classical RK4 over dt with E_u held constant.
+ * coherence decay.  Integrated with classical RK4 over dt with E_u held constant; the
+ * relaxation rates 1/T1, 1/T2 are formed once per step.
  */
 
-static void rhs2(const double *pr, double E_u, const double *rho, double *d)
+static void rhs2(const double *pr, double E_u, double g1, double g2, const double *rho, double *d)
 {
-    const double w0 = pr[0], mu = pr[1], T1 = pr[2], T2 = pr[3];
+    const double w0 = pr[0], mu = pr[1];
     const double pe = rho[0], a = rho[1], b = rho[2];
     const double pg = 1.0 - pe;
     const double muE = mu * E_u;
-    /* d pe/dt = 2 mu E Im(rho_eg) - pe/T1 */
-    d[0] = 2.0 * muE * b - pe / T1;
+    /* d pe/dt = 2 mu E Im(rho_eg) - pe/T1   (g1 = 1/T1, g2 = 1/T2) */
+    d[0] = 2.0 * muE * b - pe * g1;
     /* d rho_eg/dt = -i w0 rho_eg + i mu E (pg - pe) - rho_eg/T2 */
-    d[1] = w0 * b - a / T2;
-    d[2] = -(w0 * a) + muE * (pg - pe) - b / T2;
+    d[1] = w0 * b - a * g2;
+    d[2] = -(w0 * a) + muE * (pg - pe) - b * g2;
 }
 
-static void rhs3(const double *pr, double E_u, const double *rho, double *d)
+static void rhs3(const double *pr, double E_u, double g1r, double g2r, const double *rho, double *d)
 {
-    const double e1 = pr[0], e2 = pr[1], mu1 = pr[2], mu2 = pr[3], T1 = pr[4], T2 = pr[5];
+    const double e1 = pr[0], e2 = pr[1], mu1 = pr[2], mu2 = pr[3];
     const double p1 = rho[0], p2 = rho[1];
     const double a10 = rho[2], b10 = rho[3], a20 = rho[4], b20 = rho[5], a21 = rho[6], b21 = rho[7];
     const double p0 = 1.0 - p1 - p2;
@@ -1743,28 +1744,28 @@ static void rhs3(const double *pr, double E_u, const double *rho, double *d)
     /* H = diag(0,e1,e2) - E_u (mu1 (|0><1|+|1><0|) + mu2 (|0><2|+|2><0|)).
      * d rho_kk = -i (H rho - rho H)_kk; with W = -E_u V:
      * d p1 = 2 g1 Im(rho_10) ... derived with rho_kl = a_kl + i b_kl (k>l). */
-    d[0] = 2.0 * g1 * b10 - p1 / T1;
-    d[1] = 2.0 * g2 * b20 - p2 / T1;
+    d[0] = 2.0 * g1 * b10 - p1 * g1r;
+    d[1] = 2.0 * g2 * b20 - p2 * g1r;
     {
         /* (H rho)_10 = e1 rho_10 - g1 rho_00 ; (rho H)_10 = -g1 rho_11 - g2 rho_12
          * -i[(H rho)_10 - (rho H)_10] = -i e1 rho_10 + i g1 (rho_00 - rho_11) - i g2 rho_12 */
         /* rho_12 = conj(rho_21) = a21 - i b21 ; -i g2 (a21 - i b21) = -g2 b21 - i g2 a21 */
-        d[2] = e1 * b10 - g2 * b21 - a10 / T2;
-        d[3] = -(e1 * a10) + g1 * (p0 - p1) - g2 * a21 - b10 / T2;
+        d[2] = e1 * b10 - g2 * b21 - a10 * g2r;
+        d[3] = -(e1 * a10) + g1 * (p0 - p1) - g2 * a21 - b10 * g2r;
     }
     {
         /* (H rho)_20 = e2 rho_20 - g2 rho_00 ; (rho H)_20 = -g1 rho_21 - g2 rho_22
          * -i[...]_20 = -i e2 rho_20 + i g2 (rho_00 - rho_22) - i g1 rho_21 */
-        d[4] = e2 * b20 + g1 * b21 - a20 / T2;
-        d[5] = -(e2 * a20) + g2 * (p0 - p2) - g1 * a21 - b20 / T2;
+        d[4] = e2 * b20 + g1 * b21 - a20 * g2r;
+        d[5] = -(e2 * a20) + g2 * (p0 - p2) - g1 * a21 - b20 * g2r;
     }
     {
         /* (H rho)_21 = e2 rho_21 - g2 rho_01 ; (rho H)_21 = e1 rho_21 - g1 rho_20
          * -i[...]_21 = -i (e2 - e1) rho_21 + i g2 rho_01 - i g1 rho_20,
          * rho_01 = conj(rho_10) = a10 - i b10, -i g1 rho_20 = g1 b20 - i g1 a20 */
         double de = e2 - e1;
-        d[6] = de * b21 + g2 * b10 + g1 * b20 - a21 / T2;
-        d[7] = -(de * a21) + g2 * a10 - g1 * a20 - b21 / T2;
+        d[6] = de * b21 + g2 * b10 + g1 * b20 - a21 * g2r;
+        d[7] = -(de * a21) + g2 * a10 - g1 * a20 - b21 * g2r;
     }
 }
 
@@ -1773,18 +1774,22 @@ void orc_emitter_step(int model, const double *pr, double *rho, double E_u, doub
     const int n = (model == ORC_EMITTER_2LEVEL) ? 3 : 8;
     double k1[8], k2[8], k3[8], k4[8], t[8];
     const double h2 = 0.5 * dt, h6 = dt / 6.0;
+    /* relaxation rates once per step (the 2-level params hold T1, T2 at 2, 3; 3-level at 4, 5) */
+    const double g1 = 1.0 / pr[model == ORC_EMITTER_2LEVEL ? 2 : 4];
+    const double g2 = 1.0 / pr[model == ORC_EMITTER_2LEVEL ? 3 : 5];
     int q;
-    void (*f)(const double *, double, const double *, double *) = (model == ORC_EMITTER_2LEVEL) ? rhs2 : rhs3;
-    f(pr, E_u, rho, k1);
+    void (*f)(const double *, double, double, double, const double *, double *) =
+        (model == ORC_EMITTER_2LEVEL) ? rhs2 : rhs3;
+    f(pr, E_u, g1, g2, rho, k1);
     for (q = 0; q < n; q++)
         t[q] = rho[q] + h2 * k1[q];
-    f(pr, E_u, t, k2);
+    f(pr, E_u, g1, g2, t, k2);
     for (q = 0; q < n; q++)
         t[q] = rho[q] + h2 * k2[q];
-    f(pr, E_u, t, k3);
+    f(pr, E_u, g1, g2, t, k3);
     for (q = 0; q < n; q++)
         t[q] = rho[q] + dt * k3[q];
-    f(pr, E_u, t, k4);
+    f(pr, E_u, g1, g2, t, k4);
     for (q = 0; q < n; q++)
         rho[q] = rho[q] + h6 * (k1[q] + 2.0 * k2[q] + 2.0 * k3[q] + k4[q]);
 }
