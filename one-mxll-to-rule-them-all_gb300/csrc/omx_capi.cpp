@@ -87,6 +87,7 @@ struct SourceRec {
     DevBuf<long long> eidx;
     DevBuf<double> ka, kb;
     int n;
+    std::vector<int4> cells;   // (i, j, k, component) of every point
 };
 
 struct GroupRec {
@@ -137,6 +138,7 @@ struct omx_ctx {
     DevBuf<int4> ade_ent;   // dispersive component-cells (i, j, k, component)
     DevBuf<int> ade_b;      // their media-box index
     int ade_n = 0;
+    std::vector<int4> ade_host;
     std::vector<uint8_t> host_mat[3];   // class per component over the box (for injection checks)
     std::vector<int> cls_type;          // per class id
     // sources
@@ -180,6 +182,13 @@ struct omx_ctx {
     long long launches = 0;
     cudaEvent_t t0 = nullptr, t1 = nullptr;
     DevBuf<float> flushbuf;
+    // FP32 fused 2D TMz step (ping-pong): second field / H-psi buffer set and the parity
+    DevBuf<float> ff2[6];
+    DevBuf<float> psiH2[3][2];
+    int cur = 0;
+    bool fused_ok = false;
+    bool fused_dirty = true;    // media or sources changed since the last eligibility check
+    int *run_step = nullptr;    // device step counter while omx_run issues a step sequence
     std::string err;
 };
 
@@ -369,10 +378,14 @@ template <class R> void alloc_psi(omx_ctx *c)
     }
 }
 
-template <class R> FieldPtrs<R> field_ptrs(omx_ctx *c)
+template <class R> FieldPtrs<R> field_ptrs(omx_ctx *c, int parity = -1)
 {
+    // the current buffer set (the FP32 fused path alternates between two sets)
+    const int p = parity < 0 ? c->cur : parity;
     FieldPtrs<R> F;
     for (int q = 0; q < 6; ++q) F.f[q] = fields<R>(c)[q].p;
+    if (p == 1 && std::is_same<R, float>::value)
+        for (int q = 0; q < 6; ++q) F.f[q] = reinterpret_cast<R *>(c->ff2[q].p);
     return F;
 }
 
@@ -404,6 +417,7 @@ template <class R> GridArgs<R> grid_args(omx_ctx *c)
         for (int q = 0; q < 2; ++q) {
             G.psiE[a][q] = ps[a][0][q].p;
             G.psiH[a][q] = ps[a][1][q].p;
+            if (c->cur == 1 && std::is_same<R, float>::value) G.psiH[a][q] = reinterpret_cast<R *>(c->psiH2[a][q].p);
         }
         G.bb0[a] = c->bb0[a];
         G.bb1[a] = c->bb1[a];
@@ -419,6 +433,7 @@ template <class R> GridArgs<R> grid_args(omx_ctx *c)
     G.ade_n = c->ade_n;
     G.ade_ent = c->ade_ent.p;
     G.ade_b = c->ade_b.p;
+    G.step_inc = c->run_step;
     return G;
 }
 
@@ -571,6 +586,7 @@ void build_media(omx_ctx *c, const int32_t *map, const double *eps[3])
                 }
     }
     c->ade_n = (int)ent.size();
+    c->ade_host = ent;
     c->ade_ent.upload(ent);
     c->ade_b.upload(eb);
 }
@@ -740,11 +756,49 @@ DetArgs det_args(omx_ctx *c)
     return D;
 }
 
+// The FP32 fused TMz step applies dispersive cells and sources after the bulk pass; that
+// commutes with the reference's order only outside the CPML slabs and away from sources.
+bool fused_eligible(const omx_ctx *c)
+{
+    if (!c->fp32 || c->dims != 2 || c->desc.mode != OMX_TMZ_2D_MODE || c->n[0] % 4 != 0) return false;
+    const int npml = c->desc.npml;
+    for (const int4 &e : c->ade_host) {
+        for (int a = 0; a < 2; ++a) {
+            const int p = a == 0 ? e.x : e.y;
+            if (c->cpml_axis[a] && (p <= npml || p >= c->n[a] + 1 - npml)) return false;
+        }
+    }
+    if (!c->ade_host.empty()) {
+        std::unordered_map<long long, int> disp;
+        for (const int4 &e : c->ade_host) disp[cell_key(c, e.x, e.y, 0) * 4 + e.w] = 1;
+        for (const auto &S : c->sources) {
+            if (S->kind == 0) {
+                for (const int4 &p : S->cells)
+                    if (disp.count(cell_key(c, p.x, p.y, 0) * 4 + p.w)) return false;
+            } else {
+                for (const int4 &e : c->ade_host)
+                    if (e.w == S->pd.comp - 1 && (S->pd.plane_axis == 1 ? e.x : e.y) == S->pd.plane_index) return false;
+            }
+        }
+    }
+    return true;
+}
+
 void prepare(omx_ctx *c)
 {
     if (c->j_dirty) rebuild_jpoints(c);
     if (c->det_dirty) rebuild_detectors(c);
     c->started = true;
+    if (c->fused_dirty) {
+        c->fused_ok = fused_eligible(c);
+        c->fused_dirty = false;
+    }
+    if (c->fused_ok && !c->ff2[2].p) {
+        for (int q = 0; q < 6; ++q)
+            if (c->field_used[q]) c->ff2[q].alloc(c->felems);
+        for (int a = 0; a < 2; ++a)
+            if (c->psif[a][1][0].p) c->psiH2[a][0].alloc(c->psif[a][1][0].n);
+    }
 }
 
 StepParam imm(double v) { return StepParam{v, nullptr, nullptr}; }
@@ -785,13 +839,20 @@ template <class R> void do_sources(omx_ctx *c, const std::vector<StepParam> &amp
     }
 }
 
+template <class R> void do_inject(omx_ctx *c, StepParam time, StepParam t_skip);
+
 template <class R> void do_E(omx_ctx *c, StepParam time, StepParam t_skip)
 {
     {
         ProfScope ps(c, KC_E);
         launch_e<R>(field_ptrs<R>(c), grid_args<R>(c), c->stream);
-        c->launches++;
+        c->launches += 1 + (c->ade_n > 0 ? 1 : 0);
     }
+    do_inject<R>(c, time, t_skip);
+}
+
+template <class R> void do_inject(omx_ctx *c, StepParam time, StepParam t_skip)
+{
     if (c->inj_n > 0) {
         InjArgs I;
         I.n = c->inj_n;
@@ -847,6 +908,35 @@ template <class R> void do_sample(omx_ctx *c, StepParam slot, StepParam time)
     c->launches++;
 }
 
+// One FP32 fused TMz step: bulk H+E pass from the current buffer set into the other, then the
+// dispersive cells; the caller adds sources and the emitter current to the new set.
+template <class R> void fused_step(omx_ctx *c);
+template <> void fused_step<double>(omx_ctx *) {}
+template <> void fused_step<float>(omx_ctx *c)
+{
+    ProfScope ps(c, KC_E);
+    const int in = c->cur, out = 1 - c->cur;
+    const FieldPtrs<float> Fin = field_ptrs<float>(c, in), Fout = field_ptrs<float>(c, out);
+    const GridArgs<float> G = grid_args<float>(c);
+    Fused2Args A;
+    A.ez_in = Fin.f[2];
+    A.hx_in = Fin.f[3];
+    A.hy_in = Fin.f[4];
+    A.ez_out = Fout.f[2];
+    A.hx_out = Fout.f[3];
+    A.hy_out = Fout.f[4];
+    A.psi_hyx_in = G.psiH[0][0];
+    A.psi_hxy_in = G.psiH[1][0];
+    A.psi_hyx_out = in == 0 ? c->psiH2[0][0].p : c->psif[0][1][0].p;
+    A.psi_hxy_out = in == 0 ? c->psiH2[1][0].p : c->psif[1][1][0].p;
+    A.psi_ezx = G.psiE[0][0];
+    A.psi_ezy = G.psiE[1][0];
+    launch_fused_tmz(A, G, c->stream);
+    launch_ade_post(Fin, Fout, G, c->stream);
+    c->launches += 1 + (c->ade_n > 0 ? 1 : 0);
+    c->cur = out;
+}
+
 double source_amp(const SourceRec &S, double time)
 {
     // update_source (source_mod.f90:114-130): j_amp * exp(-((t-t0)/tau)^2) * cos(w0 (t-t0) + phase)
@@ -899,35 +989,55 @@ template <class R> void run_impl(omx_ctx *c, int tt0, int nsteps, int n_skip, in
     c->tab.alloc(tab.size(), false);
     ck(cudaMemcpyAsync(c->tab.p, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream), "tab");
     if (!c->d_step.p) c->d_step.alloc(1);
-    ck(cudaMemsetAsync(c->d_step.p, 0, sizeof(int), c->stream), "step");
+    // the first kernel of every step advances the counter, so it starts one below step 0
+    ck(cudaMemsetAsync(c->d_step.p, 0xff, sizeof(int), c->stream), "step");
+    c->run_step = c->d_step.p;
+    struct Reset {
+        omx_ctx *c;
+        ~Reset() { c->run_step = nullptr; }
+    } reset{c};
     auto P = [&](int row) { return StepParam{0.0, c->tab.p + (size_t)row * nsteps, c->d_step.p}; };
     std::vector<StepParam> amps;
     for (int q = 0; q < nsrc; ++q) amps.push_back(P(4 + q));
-    auto one_step = [&]() {
-        do_H<R>(c);
-        do_sources<R>(c, amps);
-        do_E<R>(c, P(0), P(1));
+    const bool fused = std::is_same<R, float>::value && c->fused_ok;
+    auto tail = [&]() {
         for (auto &g : c->groups) do_group<R>(c, *g, P(2));
         if (has_det) do_sample<R>(c, P(3), P(0));
-        launch_step_advance(c->d_step.p, c->stream);
-        c->launches++;
     };
-    if (use_graph && !c->prof) {
+    auto one_step = [&]() {
+        if (fused) {
+            fused_step<R>(c);
+            do_sources<R>(c, amps);
+            do_inject<R>(c, P(0), P(1));
+        } else {
+            do_H<R>(c);
+            do_sources<R>(c, amps);
+            do_E<R>(c, P(0), P(1));
+        }
+        tail();
+    };
+    // the fused path alternates buffer sets, so a captured graph covers two steps
+    const int per_graph = fused ? 2 : 1;
+    if (use_graph && !c->prof && nsteps >= per_graph) {
         if (c->gexec) {
             cudaGraphExecDestroy(c->gexec);
             c->gexec = nullptr;
         }
         cudaGraph_t graph;
         const long long before = c->launches;
+        const int cur0 = c->cur;
         ck(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "capture");
-        one_step();
+        for (int q = 0; q < per_graph; ++q) one_step();
         ck(cudaStreamEndCapture(c->stream, &graph), "end capture");
-        const long long per_step = c->launches - before;
+        const long long per_launch = c->launches - before;
         c->launches = before;
+        c->cur = cur0;
         ck(cudaGraphInstantiate(&c->gexec, graph, 0), "instantiate");
         cudaGraphDestroy(graph);
-        for (int s = 0; s < nsteps; ++s) ck(cudaGraphLaunch(c->gexec, c->stream), "graph launch");
-        c->launches += per_step * nsteps;
+        const int ngraph = nsteps / per_graph;
+        for (int s = 0; s < ngraph; ++s) ck(cudaGraphLaunch(c->gexec, c->stream), "graph launch");
+        c->launches += per_launch * ngraph;
+        for (int s = ngraph * per_graph; s < nsteps; ++s) one_step();
     } else {
         for (int s = 0; s < nsteps; ++s) one_step();
     }
@@ -942,7 +1052,7 @@ template <class R> void read_field_impl(omx_ctx *c, int field, double *host)
     const int q = field_code_to_index(field);
     std::vector<R> tmp(c->felems);
     ck(cudaStreamSynchronize(c->stream), "sync");
-    ck(cudaMemcpy(tmp.data(), fields<R>(c)[q].p, c->felems * sizeof(R), cudaMemcpyDeviceToHost), "read field");
+    ck(cudaMemcpy(tmp.data(), field_ptrs<R>(c).f[q], c->felems * sizeof(R), cudaMemcpyDeviceToHost), "read field");
     long long o = 0;
     for (int k = lo[2]; k <= hi[2]; ++k)
         for (int j = lo[1]; j <= hi[1]; ++j)
@@ -964,12 +1074,12 @@ template <class R> void write_field_impl(omx_ctx *c, int field, const double *ho
     const int q = field_code_to_index(field);
     std::vector<R> tmp(c->felems);
     ck(cudaStreamSynchronize(c->stream), "sync");
-    ck(cudaMemcpy(tmp.data(), fields<R>(c)[q].p, c->felems * sizeof(R), cudaMemcpyDeviceToHost), "read field");
+    ck(cudaMemcpy(tmp.data(), field_ptrs<R>(c).f[q], c->felems * sizeof(R), cudaMemcpyDeviceToHost), "read field");
     long long o = 0;
     for (int k = lo[2]; k <= hi[2]; ++k)
         for (int j = lo[1]; j <= hi[1]; ++j)
             for (int i = lo[0]; i <= hi[0]; ++i) tmp[(size_t)eindex(c, i, j, k)] = (R)host[o++];
-    ck(cudaMemcpy(fields<R>(c)[q].p, tmp.data(), c->felems * sizeof(R), cudaMemcpyHostToDevice), "write field");
+    ck(cudaMemcpy(field_ptrs<R>(c).f[q], tmp.data(), c->felems * sizeof(R), cudaMemcpyHostToDevice), "write field");
 }
 
 }  // namespace
@@ -1218,6 +1328,7 @@ int omx_set_media(omx_ctx *c, int n_media, const omx_medium *media, const int32_
     if (c->fp32) build_media<float>(c, media_map, eps);
     else build_media<double>(c, media_map, eps);
     c->j_dirty = true;
+    c->fused_dirty = true;
     OMX_API_END(c)
 }
 
@@ -1326,6 +1437,7 @@ int omx_source_add(omx_ctx *c, const omx_source_desc *d, int *id)
                 req(ii >= 0 && ii <= N[0] + 1 && jj >= 0 && jj <= N[1] + 1 && kk >= 0 && kk <= N[2] + 1,
                     "source kernel extends outside the grid");
                 e.push_back(eindex(c, ii, jj, kk));
+                S->cells.push_back(make_int4(ii, jj, kk, d->dir == 'x' ? 0 : (d->dir == 'y' ? 1 : 2)));
                 ka.push_back(ker[(size_t)q]);
                 kb.push_back(S->avg ? (q + stride < npts ? ker[(size_t)(q + stride)] : 0.0) : 0.0);
             }
@@ -1334,6 +1446,7 @@ int omx_source_add(omx_ctx *c, const omx_source_desc *d, int *id)
     S->ka.upload(ka);
     S->kb.upload(kb);
     c->sources.push_back(std::move(S));
+    c->fused_dirty = true;
     if (id) *id = (int)c->sources.size() - 1;
     OMX_API_END(c)
 }
@@ -1353,6 +1466,7 @@ int omx_plane_source_add(omx_ctx *c, const omx_plane_source_desc *d, int *id)
     S->n = 0;
     S->c_src = c->desc.dt / omx::consts().eps0 / c->desc.dr / omx::consts().c0 / 2.0;
     c->sources.push_back(std::move(S));
+    c->fused_dirty = true;
     if (id) *id = (int)c->sources.size() - 1;
     OMX_API_END(c)
 }
@@ -1643,21 +1757,27 @@ int omx_algorithmic_bytes(const omx_ctx *c, int kc, double *bytes)
         psi_cells_h += layers * tr * pc;
         psi_cells_e += layers * tr * pc;
     }
+    double ade_bytes = 0.0;
+    if (c->has_ade) {
+        // dispersive component-cells and their state words
+        long long drude = 0, dl = 0;
+        for (int q = 0; q < 3; ++q)
+            for (size_t t = 0; t < c->host_mat[q].size(); ++t) {
+                const int ty = c->cls_type[c->host_mat[q][t]];
+                if (ty == CLS_DRUDE) drude++;
+                else if (ty == CLS_DL) dl++;
+            }
+        ade_bytes = (double)drude * 2.0 * w + (double)dl * (2.0 + 2.0 + 4.0 * c->P) * w;
+    }
+    const bool fused = c->fused_ok;   // FP32 2D TMz: one pass per step (class KC_E)
     if (kc == KC_H) {
-        b = cells * w * (ncomp_e + 2.0 * ncomp_h) + psi_cells_h * 2.0 * w;
+        b = fused ? 0.0 : cells * w * (ncomp_e + 2.0 * ncomp_h) + psi_cells_h * 2.0 * w;
     } else if (kc == KC_E) {
-        b = cells * w * (ncomp_h + 2.0 * ncomp_e) + psi_cells_e * 2.0 * w + (double)c->bbV * ncomp_e;
-        if (c->has_ade) {
-            // count dispersive component cells and their state words
-            long long drude = 0, dl = 0;
-            for (int q = 0; q < 3; ++q)
-                for (size_t t = 0; t < c->host_mat[q].size(); ++t) {
-                    const int ty = c->cls_type[c->host_mat[q][t]];
-                    if (ty == CLS_DRUDE) drude++;
-                    else if (ty == CLS_DL) dl++;
-                }
-            b += (double)drude * 2.0 * w + (double)dl * (2.0 + 2.0 + 4.0 * c->P) * w;
-        }
+        if (fused)   // each of Ez, Hx, Hy read once and written once
+            b = cells * w * 2.0 * (ncomp_e + ncomp_h) + (psi_cells_h + psi_cells_e) * 2.0 * w +
+                (double)c->bbV * ncomp_e + ade_bytes;
+        else
+            b = cells * w * (ncomp_h + 2.0 * ncomp_e) + psi_cells_e * 2.0 * w + (double)c->bbV * ncomp_e + ade_bytes;
     } else {
         b = 0.0;
     }

@@ -1,0 +1,225 @@
+// omx_fused2d.cuh -- FP32 fused time step for 2D TMz: the H update (mxll_2D_mod.f90:469-552) and
+// the E update (:661-748) of one step in a single pass over HBM.
+//
+// Each cell's Ez, Hx, Hy are read once and written once per step (6 words instead of the 9 of
+// two half-step passes).  The pass reads the "in" buffers and writes the "out" buffers
+// (ping-pong), because a block needs the new H of its left / lower neighbour cells, which it
+// recomputes from the old values rather than waiting for the neighbouring block: recomputing
+// from buffers nobody writes during the pass keeps blocks independent.  The CPML psi of H is
+// ping-ponged for the same reason; psi of E and the ADE state are touched by their owner only.
+//
+// Work split: one thread owns 4 consecutive cells along x (float4 rows, 128-byte aligned) and
+// marches JCH rows along y.  Hy_new(i-1) comes from the lower lane by a shuffle (lane 0
+// recomputes it); Hx_new(j-1) is carried from the previous row (the first row recomputes it).
+//
+// Dispersive cells, sources and the emitter current are applied afterwards to the out buffer
+// (k_ade_post, the source kernels, k_inject): they commute with the bulk update up to FP32
+// rounding.  The host enables this path only when no dispersive cell lies in a CPML slab and no
+// source point lies in a dispersive cell.
+#pragma once
+#include "omx_stencil.cuh"
+
+namespace omx {
+
+// H of one TMz cell from old values (the reference's expressions; c prefolded with 1/dr).
+__device__ __forceinline__ float fz_hx(float hx, float ez, float ez_jp, float dhy, float dt_mu0, int ly, float bh,
+                                       float ch, const float *psi_in, float *psi_out, long long p)
+{
+    float h = hx + dt_mu0 * ((ez - ez_jp) * dhy);
+    if (ly >= 0) {
+        const float v = bh * psi_in[p] + ch * (ez - ez_jp);
+        if (psi_out) psi_out[p] = v;
+        h = h + dt_mu0 * v;
+    }
+    return h;
+}
+__device__ __forceinline__ float fz_hy(float hy, float ez, float ez_ip, float dhx, float dt_mu0, int lx, float bh,
+                                       float ch, const float *psi_in, float *psi_out, long long p)
+{
+    float h = hy + dt_mu0 * ((ez_ip - ez) * dhx);
+    if (lx >= 0) {
+        const float v = bh * psi_in[p] + ch * (ez_ip - ez);
+        if (psi_out) psi_out[p] = v;
+        h = h + dt_mu0 * v;
+    }
+    return h;
+}
+
+template <int JCH, bool XCPML>
+__global__ void __launch_bounds__(128, 6) k_fused_tmz(Fused2Args A, GridArgs<float> G)
+{
+    const Lay L = G.L;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const int ib = 1 + 4 * t;                 // first of this thread's 4 cells
+    const bool active = ib <= L.nx;           // nx % 4 == 0 is required by the host
+    const int j0 = 1 + blockIdx.y * JCH;
+    if (G.step_inc && t == 0 && blockIdx.y == 0) *G.step_inc += 1;   // step counter of the device loop
+    if (j0 > L.ny) return;
+    const int j1 = min(L.ny, j0 + JCH - 1);
+    const float dt_mu0 = G.dt_mu0, dt_eps0 = G.dt_eps0;
+    const long long px = L.px;
+    const int ibc = active ? ib : 1;          // lanes past nx only join the shuffles
+    // per-column x factors: uniform 1/dr and no psi without an x CPML
+    float dhx[4], dex[4], bhx[4], chx[4], bex[4], cex[4];
+    int lhx[4], lex[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int i = XCPML ? min(ibc + q, L.nx) : 1;
+        dhx[q] = G.den_h[0][i];
+        dex[q] = G.den_e[0][i];
+        lhx[q] = XCPML ? G.lH[0][i] : -1;
+        lex[q] = XCPML ? G.lE[0][i] : -1;
+        bhx[q] = XCPML ? G.bH[0][i] : 0.f;
+        chx[q] = XCPML ? G.cH[0][i] : 0.f;
+        bex[q] = XCPML ? G.bE[0][i] : 0.f;
+        cex[q] = XCPML ? G.cE[0][i] : 0.f;
+    }
+    // left neighbour column (i = ib-1, or nx for a periodic wrap, or the PEC ghost); every
+    // index below uses the clamped ibc so that lanes past nx stay inside the arrays
+    const bool left_ghost = (ibc == 1) && !G.per[0];
+    const int il = (ibc == 1) ? L.nx : ibc - 1;
+    const float dhx_l = G.den_h[0][XCPML ? il : 1];
+    const int lhx_l = XCPML ? G.lH[0][il] : -1;
+    const float bhx_l = XCPML ? G.bH[0][il] : 0.f, chx_l = XCPML ? G.cH[0][il] : 0.f;
+    // right neighbour for Ez(i+4): ib+4 (<= nx+1) or 1 when periodic at the last group
+    const int iright = (ibc + 4 > L.nx && G.per[0]) ? 1 : ibc + 4;
+    const bool bb_i = G.bbV > 0 && (ibc + 3 >= G.bb0[0] && ibc <= G.bb1[0]);
+    const long long col = L.off + ibc;
+
+    // Hx_new(i, j0-1): recomputed from old values (0 at a PEC ghost row)
+    float hxp[4];
+    {
+        const int jm = j0 - 1;
+        if (jm == 0 && !G.per[1]) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) hxp[q] = 0.f;
+        } else {
+            const int jr = (jm == 0) ? L.ny : jm;                     // periodic wrap
+            const int jr1 = (jr == L.ny && G.per[1]) ? 1 : jr + 1;
+            const float4 e0 = *reinterpret_cast<const float4 *>(A.ez_in + col + px * jr);
+            const float4 e1 = *reinterpret_cast<const float4 *>(A.ez_in + col + px * jr1);
+            const float4 h0 = *reinterpret_cast<const float4 *>(A.hx_in + col + px * jr);
+            const float dhy = G.den_h[1][jr];
+            const int ly = G.lH[1][jr];
+            const float bh = G.bH[1][jr], ch = G.cH[1][jr];
+            const long long pb = (ibc - 1) + (long long)L.nx * ly;
+            hxp[0] = fz_hx(h0.x, e0.x, e1.x, dhy, dt_mu0, ly, bh, ch, A.psi_hxy_in, nullptr, pb + 0);
+            hxp[1] = fz_hx(h0.y, e0.y, e1.y, dhy, dt_mu0, ly, bh, ch, A.psi_hxy_in, nullptr, pb + 1);
+            hxp[2] = fz_hx(h0.z, e0.z, e1.z, dhy, dt_mu0, ly, bh, ch, A.psi_hxy_in, nullptr, pb + 2);
+            hxp[3] = fz_hx(h0.w, e0.w, e1.w, dhy, dt_mu0, ly, bh, ch, A.psi_hxy_in, nullptr, pb + 3);
+        }
+    }
+    // rows j and j+1 of Ez, row j of Hx / Hy in flight; the next row is fetched before the
+    // current one is computed so two rows of loads overlap
+    float4 ez_c = *reinterpret_cast<const float4 *>(A.ez_in + col + px * j0);
+    int jn = (j0 == L.ny && G.per[1]) ? 1 : j0 + 1;
+    float4 ez_n = *reinterpret_cast<const float4 *>(A.ez_in + col + px * jn);
+    float4 hx_o = *reinterpret_cast<const float4 *>(A.hx_in + col + px * j0);
+    float4 hy_o = *reinterpret_cast<const float4 *>(A.hy_in + col + px * j0);
+    for (int j = j0; j <= j1; ++j) {
+        const long long row = col + px * j;
+        float4 ez_nn = ez_n, hx_on = hx_o, hy_on = hy_o;
+        if (j < j1) {
+            const int jnn = (j + 1 == L.ny && G.per[1]) ? 1 : j + 2;
+            ez_nn = *reinterpret_cast<const float4 *>(A.ez_in + col + px * jnn);
+            hx_on = *reinterpret_cast<const float4 *>(A.hx_in + row + px);
+            hy_on = *reinterpret_cast<const float4 *>(A.hy_in + row + px);
+        }
+        // Ez(i+4, j): next lane's first element, or a load at the warp / row end
+        float ez_r = __shfl_down_sync(0xffffffffu, ez_c.x, 1);
+        if (lane == 31 || ibc + 4 > L.nx) ez_r = A.ez_in[L.off + iright + px * j];
+        const float dhy = G.den_h[1][j], dey = G.den_e[1][j];
+        const int ly = G.lH[1][j], lye = G.lE[1][j];
+        const float bhy = G.bH[1][j], chy = G.cH[1][j], bey = G.bE[1][j], cey = G.cE[1][j];
+        const float ez[5] = {ez_c.x, ez_c.y, ez_c.z, ez_c.w, ez_r};
+        const float ezn[4] = {ez_n.x, ez_n.y, ez_n.z, ez_n.w};
+        const float hxo[4] = {hx_o.x, hx_o.y, hx_o.z, hx_o.w};
+        const float hyo[4] = {hy_o.x, hy_o.y, hy_o.z, hy_o.w};
+        float hx[4], hy[4];
+        const long long pby = (ibc - 1) + (long long)L.nx * ly;
+        const long long pbx = (long long)G.L2 * (j - 1);
+        float *const psx_out = active ? A.psi_hxy_out : nullptr;   // lanes past nx only join shuffles
+        float *const psy_out = active ? A.psi_hyx_out : nullptr;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            hx[q] = fz_hx(hxo[q], ez[q], ezn[q], dhy, dt_mu0, ly, bhy, chy, A.psi_hxy_in, psx_out, pby + q);
+            hy[q] = fz_hy(hyo[q], ez[q], ez[q + 1], dhx[q], dt_mu0, lhx[q], bhx[q], chx[q], A.psi_hyx_in,
+                          psy_out, lhx[q] + pbx);
+        }
+        // Hy_new(i-1, j): previous lane's last cell, recomputed by lane 0
+        float hy_l = __shfl_up_sync(0xffffffffu, hy[3], 1);
+        if (active && (lane == 0 || ib == 1)) {
+            if (left_ghost) {
+                hy_l = 0.f;
+            } else {
+                const long long rl = L.off + il + px * j;
+                // Ez(il+1) is this thread's first cell (or its periodic image)
+                hy_l = fz_hy(A.hy_in[rl], A.ez_in[rl], ez[0], dhx_l, dt_mu0, lhx_l, bhx_l, chx_l, A.psi_hyx_in,
+                             nullptr, lhx_l + pbx);
+            }
+        }
+        if (active) {
+            *reinterpret_cast<float4 *>(A.hx_out + row) = make_float4(hx[0], hx[1], hx[2], hx[3]);
+            *reinterpret_cast<float4 *>(A.hy_out + row) = make_float4(hy[0], hy[1], hy[2], hy[3]);
+            if (G.per[0] && ib + 3 == L.nx) A.hy_out[row + 3 - L.nx] = hy[3];            // Hy(0,j) = Hy(nx,j)
+            if (G.per[1] && j == L.ny)
+                *reinterpret_cast<float4 *>(A.hx_out + row - px * L.ny) = make_float4(hx[0], hx[1], hx[2], hx[3]);
+            // E update of the 4 cells
+            const bool bb = bb_i && j >= G.bb0[1] && j <= G.bb1[1];
+            float eo[4];
+            const float hyl[4] = {hy_l, hy[0], hy[1], hy[2]};
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const float dyh = hy[q] - hyl[q];
+                const float dxh = hxp[q] - hx[q];
+                const float r = dyh * dex[q] + dxh * dey;
+                float e = ez[q];
+                if (bb && ibc + q >= G.bb0[0] && ibc + q <= G.bb1[0]) {
+                    const long long b = (ibc + q - G.bb0[0]) + (long long)G.bbd[0] * (j - G.bb0[1]);
+                    e = plain_update<float>(e, r, G.mat[2][b], G);
+                } else {
+                    e = e + dt_eps0 * r;
+                }
+                if (XCPML && lex[q] >= 0) {
+                    const long long p = lex[q] + pbx;
+                    const float v = bex[q] * A.psi_ezx[p] + cex[q] * dyh;
+                    A.psi_ezx[p] = v;
+                    e = e + dt_eps0 * v;
+                }
+                if (lye >= 0) {
+                    const long long p = (ibc + q - 1) + (long long)L.nx * lye;
+                    const float v = bey * A.psi_ezy[p] + cey * dxh;
+                    A.psi_ezy[p] = v;
+                    e = e + dt_eps0 * v;
+                }
+                eo[q] = e;
+            }
+            *reinterpret_cast<float4 *>(A.ez_out + row) = make_float4(eo[0], eo[1], eo[2], eo[3]);
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) hxp[q] = hx[q];
+        ez_c = ez_n;
+        ez_n = ez_nn;
+        hx_o = hx_on;
+        hy_o = hy_on;
+    }
+}
+
+// Dispersive cells after the fused pass: E_out = ADE(E_in, curl H_out) (no CPML term: the host
+// keeps dispersive cells out of the CPML slabs on this path).
+__global__ void k_ade_post(FieldPtrs<float> Fin, FieldPtrs<float> Fout, GridArgs<float> G)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= G.ade_n) return;
+    const int4 en = G.ade_ent[q];
+    const int b = G.ade_b[q];
+    const int c = en.w;
+    const float rot = curl_h<float>(Fout, G, c, en.x, en.y, en.z);
+    const Lay &L = G.L;
+    const long long idx = L.off + en.x + (long long)L.px * en.y + L.pz * en.z;
+    const ClsR<float> cl = G.cls[G.mat[c][b]];
+    Fout.f[c][idx] = ade_update<float>(Fin.f[c][idx], rot, cl, c, b, G);
+}
+
+}  // namespace omx

@@ -76,6 +76,8 @@ template <class R> struct GridArgs {
     int ade_n;
     const int4 *ade_ent;
     const int *ade_b;
+    // device-loop step counter, advanced by the first kernel of each step (null outside omx_run)
+    int *step_inc;
 };
 
 template <class R> struct FieldPtrs {
@@ -146,6 +148,16 @@ template <class R> void launch_emit(const FieldPtrs<R> &F, const Lay &L, const E
 void launch_scatter(const JState &J, const ScatArgs &S, StepParam move, void *stream);
 template <class R> void launch_sample(const FieldPtrs<R> &F, const DetArgs &D, StepParam slot, StepParam time, void *stream);
 void launch_step_advance(int *step, void *stream);
+// FP32 fused TMz step: reads the in buffers, writes the out buffers (see omx_fused2d.cuh)
+struct Fused2Args {
+    const float *ez_in, *hx_in, *hy_in;
+    float *ez_out, *hx_out, *hy_out;
+    const float *psi_hyx_in, *psi_hxy_in;   // x-face psi of Hy, y-face psi of Hx (old)
+    float *psi_hyx_out, *psi_hxy_out;
+    float *psi_ezx, *psi_ezy;               // E psi, updated in place
+};
+void launch_fused_tmz(const Fused2Args &A, const GridArgs<float> &G, void *stream);
+void launch_ade_post(const FieldPtrs<float> &Fin, const FieldPtrs<float> &Fout, const GridArgs<float> &G, void *stream);
 void launch_flush(float *buf, long long n, void *stream);
 
 }  // namespace omx

@@ -128,6 +128,7 @@ __global__ void __launch_bounds__(128) k_h3(FieldPtrs<R> F, GridArgs<R> G, int k
     const Lay L = G.L;
     const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
     const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+    if (G.step_inc && i == 1 && j == 1 && blockIdx.z == 0) *G.step_inc += 1;   // device-loop step counter
     if (i > L.nx || j > L.ny) return;
     const int k0 = 1 + blockIdx.z * kch;
     const int k1 = min(L.nz, k0 + kch - 1);
@@ -298,6 +299,7 @@ __global__ void __launch_bounds__(128) k_h2(FieldPtrs<R> F, GridArgs<R> G, int j
 {
     const Lay L = G.L;
     const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (G.step_inc && i == 1 && blockIdx.y == 0) *G.step_inc += 1;   // device-loop step counter
     if (i > L.nx) return;
     const int j0 = 1 + blockIdx.y * jch;
     const int j1 = min(L.ny, j0 + jch - 1);
@@ -462,6 +464,7 @@ __global__ void k_h1(FieldPtrs<R> F, GridArgs<R> G)
 {
     const Lay L = G.L;
     const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (G.step_inc && i == 1) *G.step_inc += 1;   // device-loop step counter
     if (i > L.nx - 1) return;
     R *__restrict__ Ex = F.f[0];
     R *__restrict__ Hy = F.f[4];

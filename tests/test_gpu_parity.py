@@ -177,3 +177,55 @@ def test_media_after_start_is_rejected(orc_mod):
         gpu.set_media([omx.medium_dielectric(2.0)], np.zeros((32, 32, 32, 3), np.int32))
     with pytest.raises(omx.OMXError):
         omx.TMxll(3, (40, 40, 40), 25, (3, 3, 3), deck["dt"], deck["dr"])   # two CPML slabs do not fit
+
+
+def tmz_variant_deck(nx, ny, bx, by, with_media=True, src="plane"):
+    """2D TMz scene for the FP32 fused step: Drude disc + dielectric block away from CPML,
+    a plane or radial Ez source, a material q-group, point detectors."""
+    d = decks._base(2, (nx, ny), 6, (bx, by, 1), 2.0, mode=1)
+    ev, fs = omx.UNITS["ev_to_au"], omx.UNITS["fs_to_au"]
+    if with_media:
+        I, J = np.meshgrid(np.arange(1, nx + 1), np.arange(1, ny + 1), indexing="ij")
+        disc = (I - nx * 0.6) ** 2 + (J - ny * 0.5) ** 2 <= (min(nx, ny) * 0.12) ** 2
+        block = (np.abs(I - nx * 0.3) < nx * 0.08) & (np.abs(J - ny * 0.55) < ny * 0.1)
+        d["media"].append(dict(kind="drude", omegaD=8.5, GammaD=0.2, eps_r=1.5))
+        d["voxels"].append(np.stack([decks._cell_nm(I[disc], nx, 2.0), decks._cell_nm(J[disc], ny, 2.0)], axis=1))
+        d["media"].append(dict(kind="dielectric", eps_r=3.0))
+        d["voxels"].append(np.stack([decks._cell_nm(I[block], nx, 2.0), decks._cell_nm(J[block], ny, 2.0)], axis=1))
+    tau = 2.0 * fs
+    if src == "plane":
+        d["plane_sources"].append(dict(comp=3, plane_axis=2, plane_index=9, j_amp=1.0, w0=2.8 * ev, t0=2.5 * tau,
+                                       tau=tau, t_init=0.0, t_final=1e30, phase=0.0, chirp=0.0))
+    else:
+        d["sources"].append(dict(dir="z", j_amp=1.0, w0=2.8 * ev, t0=2.5 * tau, tau=tau,
+                                 r0=[-nx * 0.3 * 2.0 * decks.NM, -ny * 0.3 * 2.0 * decks.NM], radius=2.5 * d["dr"],
+                                 t_init=0.0, t_final=1e30, phase=0.1, chirp=0.0))
+    rng = np.random.default_rng(nx + ny)
+    ne = 30
+    cells = np.stack([rng.integers(10, nx - 10, ne), rng.integers(ny // 2 + 12, ny - 10, ne)], axis=1).astype(np.int32)
+    par = np.stack([rng.normal(2.8, 0.05, ne) * ev, np.full(ne, 9 * decks.DEBYE), np.full(ne, 400 * fs),
+                    np.full(ne, 40 * fs), np.zeros(ne), np.zeros(ne), np.ones(ne)], axis=1)
+    d["groups"].append(dict(group_type=1, model=1, cells=cells, params=par, density=3e-3 / decks.NM ** 3, dt=d["dt"]))
+    for p in ([3, 5], [nx - 2, ny - 3], [nx // 2, 3 * ny // 4], [1, ny // 2], [nx, 1]):
+        for f in (3, 4, 5):
+            d["detectors"].append(dict(type=1, field=f, idx=np.array([p], np.int32)))
+    return d
+
+
+@pytest.mark.parametrize("shape,bx,by,src,steps", [
+    ((128, 96), 2, 3, "plane", 301),     # periodic x, CPML y (the benchmark's boundaries), odd steps
+    ((96, 64), 2, 2, "radial", 240),     # periodic x and y
+    ((128, 100), 3, 3, "plane", 250),    # CPML on both axes
+    ((64, 72), 1, 1, "radial", 200),     # closed (PEC) box
+    ((102, 80), 2, 3, "plane", 200),     # width not a multiple of 4: the unfused FP32 kernels
+])
+def test_fp32_fused_tmz_variants(orc_mod, shape, bx, by, src, steps):
+    deck = tmz_variant_deck(shape[0], shape[1], bx, by, src=src)
+    gpu, cpu, gg, cg, tc, tg = run_both(orc_mod, deck, steps, "fp32", "run", use_graph=True)
+    assert trace_error(tg, tc) <= FP32_TOL
+    assert compare_fields(gpu, cpu, deck) <= 10 * FP32_TOL
+    ga, cb = gg[0].read(), cpu.q_group_read(cg[0])
+    assert np.max(np.abs(ga["dipole"] - cb["dipole"])) / max(np.max(np.abs(cb["dipole"])), 1e-300) <= 1e-3
+    # the per-call API on the same FP32 context type agrees with the device loop
+    gpu2, cpu2, gg2, cg2, tc2, tg2 = run_both(orc_mod, deck, steps, "fp32", "calls")
+    assert trace_error(tg2, tc) <= FP32_TOL
