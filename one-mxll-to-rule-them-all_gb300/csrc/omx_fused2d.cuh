@@ -45,18 +45,15 @@ __device__ __forceinline__ float fz_hy(float hy, float ez, float ez_ip, float dh
     return h;
 }
 
-template <int JCH, bool XCPML>
-__global__ void __launch_bounds__(128, 6) k_fused_tmz(Fused2Args A, GridArgs<float> G)
+// Rows j0..j1 of one column strip (128 threads x 4 cells = 512 columns).
+template <bool XCPML>
+__device__ __forceinline__ void fused_tmz_rows(const Fused2Args &A, const GridArgs<float> &G, int strip, int j0, int j1)
 {
-    const Lay L = G.L;
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const Lay &L = G.L;
+    const int t = strip * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31;
     const int ib = 1 + 4 * t;                 // first of this thread's 4 cells
     const bool active = ib <= L.nx;           // nx % 4 == 0 is required by the host
-    const int j0 = 1 + blockIdx.y * JCH;
-    if (G.step_inc && t == 0 && blockIdx.y == 0) *G.step_inc += 1;   // step counter of the device loop
-    if (j0 > L.ny) return;
-    const int j1 = min(L.ny, j0 + JCH - 1);
     const float dt_mu0 = G.dt_mu0, dt_eps0 = G.dt_eps0;
     const long long px = L.px;
     const int ibc = active ? ib : 1;          // lanes past nx only join the shuffles
@@ -203,6 +200,26 @@ __global__ void __launch_bounds__(128, 6) k_fused_tmz(Fused2Args A, GridArgs<flo
         ez_n = ez_nn;
         hx_o = hx_on;
         hy_o = hy_on;
+    }
+}
+
+// Persistent launch: gridDim.x = SMs x resident blocks; the (strip, row) work is split into
+// gridDim.x contiguous, equal ranges so every block marches about the same number of rows and
+// no partial wave is left at the end.
+template <bool XCPML>
+__global__ void __launch_bounds__(128, 6) k_fused_tmz(Fused2Args A, GridArgs<float> G, int nstrip)
+{
+    if (G.step_inc && blockIdx.x == 0 && threadIdx.x == 0) *G.step_inc += 1;   // device-loop step counter
+    const long long ny = G.L.ny;
+    const long long total = (long long)nstrip * ny;
+    long long r = total * blockIdx.x / gridDim.x;
+    const long long r1 = total * (blockIdx.x + 1) / gridDim.x;
+    while (r < r1) {
+        const int strip = (int)(r / ny);
+        const int j0 = (int)(r % ny) + 1;
+        const int j1 = (int)min((long long)ny, (long long)j0 + (r1 - r) - 1);
+        fused_tmz_rows<XCPML>(A, G, strip, j0, j1);
+        r += j1 - j0 + 1;
     }
 }
 

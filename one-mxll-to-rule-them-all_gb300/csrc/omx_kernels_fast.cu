@@ -1,6 +1,8 @@
 // omx_kernels_fast.cu -- FP32 fused path of the Yee/CPML/ADE half-step kernels.  FP32 field
 // state with FP64-precomputed coefficients rounded once to FP32; multiply-adds contract to FMA.
 #include <cuda_runtime.h>
+
+#include <algorithm>
 #include "omx_fused2d.cuh"
 
 namespace omx {
@@ -14,13 +16,26 @@ template <> void launch_e<float>(const FieldPtrs<float> &F, const GridArgs<float
     launch_e_impl<float, false>(F, G, s);
 }
 
+static int persistent_blocks(const void *kernel)
+{
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 128, 0);
+    return (sms > 0 ? sms : 152) * (per_sm > 0 ? per_sm : 1);
+}
+
 void launch_fused_tmz(const Fused2Args &A, const GridArgs<float> &G, void *s)
 {
-    constexpr int JCH = 32;
-    const int threads = G.L.nx / 4;
-    dim3 b(128, 1, 1), g((threads + 127) / 128, (G.L.ny + JCH - 1) / JCH, 1);
-    if (A.psi_ezx) k_fused_tmz<JCH, true><<<g, b, 0, (cudaStream_t)s>>>(A, G);
-    else k_fused_tmz<JCH, false><<<g, b, 0, (cudaStream_t)s>>>(A, G);
+    const int nstrip = (G.L.nx / 4 + 127) / 128;
+    const void *k = A.psi_ezx ? (const void *)k_fused_tmz<true> : (const void *)k_fused_tmz<false>;
+    static int blocks_true = 0, blocks_false = 0;
+    int &nb = A.psi_ezx ? blocks_true : blocks_false;
+    if (nb == 0) nb = persistent_blocks(k);
+    const long long rows = (long long)nstrip * G.L.ny;
+    const int grid = (int)std::min<long long>(nb, rows);
+    if (A.psi_ezx) k_fused_tmz<true><<<grid, 128, 0, (cudaStream_t)s>>>(A, G, nstrip);
+    else k_fused_tmz<false><<<grid, 128, 0, (cudaStream_t)s>>>(A, G, nstrip);
 }
 
 void launch_ade_post(const FieldPtrs<float> &Fin, const FieldPtrs<float> &Fout, const GridArgs<float> &G, void *s)
