@@ -200,6 +200,37 @@ int omx_qgroup_read(omx_ctx *ctx, int group_id, double *dipole, double *dPt_dt, 
                     double *rho);
 int omx_qgroup_state_size(int model);
 
+/* ---- emitter step without allocation --------------------------------------------------------- */
+/* No counterpart in the reference (an addition of this library).
+ *
+ * For callers that cannot call cudaMalloc -- code that runs while a CUDA graph is being
+ * captured, or a host that owns all device memory through its own pool or device arrays and
+ * forbids the device-wide synchronisation of cudaMalloc / cudaFree in its time loop -- this
+ * entry point advances a batch of few-level emitters and updates their current arrays entirely
+ * in caller-provided device memory, and allocates nothing.  It computes what omx_qgroup_step does
+ * after its field gather, from the gathered E samples:
+ *   E       n_emitters x 3 device doubles, the E at each emitter (input)
+ *   params  n_emitters x 7 | 9 (model), as omx_qgroup_create (input)
+ *   rho     n_emitters x omx_qgroup_state_size(model), density matrices (in/out, start at zero)
+ *   dipole  n_emitters x 3 (in/out, start at zero)
+ *   winner, wk  n_points each: for every current point the index of the emitter that writes it
+ *           last (or -1) and its weight (density, or density * kernel weight)
+ *   J, J_old, dJ  3 x n_points (component-major): J in/out, J_old and dJ out, for the
+ *           components comp_first..comp_last (0-based)
+ * All pointers are device pointers; work is queued on `stream` (NULL = default stream).
+ * The dP/dt of the emitters, produced by the density-matrix step and consumed by the scatter,
+ * lives in a fixed device array of 3 * OMX_NOALLOC_MAX_EMITTERS doubles (1.5 MiB) that every GPU
+ * loading the library holds until the process exits.  n_emitters above
+ * OMX_NOALLOC_MAX_EMITTERS is rejected with OMX_ERR_ARG.  All calls share that array: calls
+ * that overlap on the GPU (other streams, other host threads) race and must be serialised by the
+ * caller.  The first call on each device looks the array's device address up (no allocation);
+ * make that first call before any stream capture.  Errors are read with omx_last_error(NULL). */
+#define OMX_NOALLOC_MAX_EMITTERS 65536
+int omx_emitter_step_noalloc(int model, int n_emitters, const double *E, const double *params,
+                             double *rho, double *dipole, int n_points, const int *winner,
+                             const double *wk, double *J, double *J_old, double *dJ,
+                             int comp_first, int comp_last, double dt, void *stream);
+
 /* ---- detectors (write_fields_subs_mod.f90 sampling stencils) ------------------------------- */
 /* indx_list: nd x dimensions (TDetector%indx_list, detector_mod.f90:21) */
 int omx_detector_add(omx_ctx *ctx, int detector_type, int field, int nd, const int32_t *indx_list,

@@ -20,6 +20,10 @@
 #include "omx_host.h"
 #include "omx_internal.h"
 
+namespace omx {
+void set_global_error(const std::string &msg);
+}
+
 using namespace omx;
 
 namespace {
@@ -1083,6 +1087,9 @@ template <class R> void write_field_impl(omx_ctx *c, int field, const double *ho
 }
 
 }  // namespace
+
+// message for calls without a context (omx_last_error(NULL))
+void omx::set_global_error(const std::string &msg) { g_last_error = msg; }
 
 // =================================================================================================
 extern "C" {

@@ -96,6 +96,7 @@ SIGNATURES = {
     "omx_qgroup_step": (_I, [_VP, _I, _I]),
     "omx_qgroup_read": (_I, [_VP, _I, _PD, _PD, _PD, _PD]),
     "omx_qgroup_state_size": (_I, [_I]),
+    "omx_emitter_step_noalloc": (_I, [_I, _I, _VP, _VP, _VP, _VP, _I, _VP, _VP, _VP, _VP, _VP, _I, _I, _D, _VP]),
     "omx_detector_add": (_I, [_VP, _I, _I, _I, _P32, _PI]),
     "omx_detectors_total_points": (_I, [_VP]),
     "omx_detectors_set_capacity": (_I, [_VP, _I]),
