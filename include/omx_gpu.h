@@ -246,8 +246,19 @@ int omx_detectors_drain(omx_ctx *ctx, double *times, double *values, int max_rec
 /* ---- whole driver loop on the device (mxim_mxll.f90:92-132) --------------------------------- */
 /* Runs steps tt = tt0 .. tt0+nsteps-1 with the reference's ordering: H, sources, E, q-groups
  * on q-steps, detector records every t_det_print steps (0 disables).  n_skip_steps as in
- * mxim_mxll.f90:73-83.  use_graph != 0 captures the step sequence in a CUDA graph. */
+ * mxim_mxll.f90:73-83.  use_graph != 0 runs the step sequence as a captured CUDA graph; the
+ * graph is kept and reused by later calls until a configuration call changes the context. */
 int omx_run(omx_ctx *ctx, int tt0, int nsteps, int n_skip_steps, int t_det_print, int use_graph);
+
+/* Launch-shape autotuner (no counterpart in the reference, whose loops have no launch shape).
+ * Times each candidate shape of this grid's field kernels `reps` times and keeps the fastest:
+ * the fused FP32 TMz kernel's form (0 register prefetch, 4/5/6/8 bulk-copy ring depth) or the
+ * planes / rows each thread marches in the unfused kernels.  The candidates run on the initial
+ * all-zero fields, which every kernel maps to zero, so the simulation state is unchanged: call it
+ * after the grid is configured and before the first step or omx_write_field (OMX_ERR_STATE
+ * otherwise); configuration calls are closed afterwards, as after a first step.  *choice (may
+ * be NULL) receives the chosen shape. */
+int omx_autotune(omx_ctx *ctx, int reps, int *choice);
 
 /* ---- field access (debug / parity) ---------------------------------------------------------- */
 /* Copies a field over the reference's bounds (e.g. 3D Ex(0:nx,1:ny+1,1:nz+1)) to/from host

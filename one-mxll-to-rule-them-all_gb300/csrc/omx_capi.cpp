@@ -98,7 +98,7 @@ struct GroupRec {
     omx_qgroup_desc d;
     int npar, nst;
     DevBuf<int> ci, cj, ck;
-    DevBuf<double> par, rho, E, dipole, dPdt;
+    DevBuf<double> par, rates, rho, E, dipole, dPdt;
     DevBuf<int> win;
     DevBuf<double> wk;
     std::vector<std::pair<long long, double>> pts;   // (cell key, wk) in write order
@@ -170,13 +170,36 @@ struct omx_ctx {
     bool det_dirty = false;
     // stepping state (mxim_mxll.f90:96-104)
     bool started = false;
+    bool fields_written = false;   // omx_write_field was called (the fields may be non-zero)
+    // launch shapes (omx_autotune): planes / rows per thread of the unfused kernels (0 = default)
+    // and the fused-kernel form (-1 = default)
+    int march = 0;
+    int fused_form = -1;
     int tq_step_old = 0;
     double t_skip = 0.0;
     // run tables
     DevBuf<double> tab;
     DevBuf<int> d_step;
-    // graph
-    cudaGraphExec_t gexec = nullptr;
+    DevBuf<int> d_err;     // kernel error word (bit 0: a bulk-copy wait of the fused kernel ran out)
+    int *h_err = nullptr;  // pinned host copy of it, read at every synchronisation
+    // pinned staging of the per-step table, two halves used alternately (an event per half
+    // marks when its last copy has been consumed)
+    struct HostStage {
+        double *p = nullptr;
+        size_t cap = 0;
+        cudaEvent_t ev = nullptr;
+    } tab_stage[2];
+    int tab_flip = 0;
+    // captured step graphs, valid while the configuration epoch is unchanged (kernel arguments
+    // hold device pointers and sizes that any configuration call may replace)
+    unsigned long long epoch = 1;
+    struct GraphRec {
+        unsigned long long epoch;
+        int steps, cur, W, has_det, fused, cur_after;
+        long long launches;
+        cudaGraphExec_t exec;
+    };
+    std::vector<GraphRec> graphs;
     // profiling
     bool prof = false;
     struct Ev { int cls; cudaEvent_t a, b; };
@@ -438,6 +461,7 @@ template <class R> GridArgs<R> grid_args(omx_ctx *c)
     G.ade_ent = c->ade_ent.p;
     G.ade_b = c->ade_b.p;
     G.step_inc = c->run_step;
+    G.march = c->march;
     return G;
 }
 
@@ -726,6 +750,7 @@ void ensure_rec_capacity(omx_ctx *c, int need)
 {
     const int npts = (int)c->tap_field.size();
     if (need <= c->rec_capacity) return;
+    c->epoch++;
     int cap = std::max(need, c->rec_capacity * 2);
     DevBuf<double> nrec, ntim;
     nrec.alloc((size_t)cap * std::max(npts, 1));
@@ -790,6 +815,7 @@ bool fused_eligible(const omx_ctx *c)
 
 void prepare(omx_ctx *c)
 {
+    if (c->j_dirty || c->det_dirty || c->fused_dirty) c->epoch++;
     if (c->j_dirty) rebuild_jpoints(c);
     if (c->det_dirty) rebuild_detectors(c);
     c->started = true;
@@ -802,10 +828,11 @@ void prepare(omx_ctx *c)
             if (c->field_used[q]) c->ff2[q].alloc(c->felems);
         for (int a = 0; a < 2; ++a)
             if (c->psif[a][1][0].p) c->psiH2[a][0].alloc(c->psif[a][1][0].n);
+        c->epoch++;
     }
 }
 
-StepParam imm(double v) { return StepParam{v, nullptr, nullptr}; }
+StepParam imm(double v) { return StepParam{v, nullptr, nullptr, 0}; }
 
 // ---- launch sequences (templated on the field precision) --------------------------------------
 template <class R> void do_H(omx_ctx *c)
@@ -885,11 +912,14 @@ template <class R> void do_group(omx_ctx *c, GroupRec &g, StepParam move)
     A.cj = g.cj.p;
     A.ck = g.ck.p;
     A.par = g.par.p;
+    A.rates = g.rates.p;
     A.rho = g.rho.p;
     A.E = g.E.p;
     A.dipole = g.dipole.p;
     A.dPdt = g.dPdt.p;
     A.dt = g.d.dt;
+    A.h2 = 0.5 * g.d.dt;
+    A.h6 = g.d.dt / 6.0;
     launch_emit<R>(field_ptrs<R>(c), c->L, A, move, c->stream);
     ScatArgs S;
     S.np = (int)c->jkeys.size();
@@ -935,10 +965,23 @@ template <> void fused_step<float>(omx_ctx *c)
     A.psi_hxy_out = in == 0 ? c->psiH2[1][0].p : c->psif[1][1][0].p;
     A.psi_ezx = G.psiE[0][0];
     A.psi_ezy = G.psiE[1][0];
-    launch_fused_tmz(A, G, c->stream);
+    A.err = c->d_err.p;
+    launch_fused_tmz(A, G, c->fused_form, c->stream);
     launch_ade_post(Fin, Fout, G, c->stream);
     c->launches += 1 + (c->ade_n > 0 ? 1 : 0);
     c->cur = out;
+}
+
+// Synchronise the stream and report a failure that a kernel recorded in the error word.
+void sync_checked(omx_ctx *c, const char *what)
+{
+    ck(cudaMemcpyAsync(c->h_err, c->d_err.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream), what);
+    ck(cudaStreamSynchronize(c->stream), what);
+    if (*c->h_err) {
+        *c->h_err = 0;
+        ck(cudaMemset(c->d_err.p, 0, sizeof(int)), what);
+        throw Fail{OMX_ERR_CUDA, "fused TMz kernel: a bulk-copy wait ran out; the fields of that step are invalid"};
+    }
 }
 
 double source_amp(const SourceRec &S, double time)
@@ -966,9 +1009,21 @@ template <class R> void run_impl(omx_ctx *c, int tt0, int nsteps, int n_skip, in
     prepare(c);
     const int nsrc = (int)c->sources.size();
     const bool has_det = !c->tap_field.empty() && t_det_print > 0;
-    // per-step scalars: time, t_skip, move, slot, amps...
+    // per-step scalars, step-major: time, t_skip, move, slot, amps...
     const int W = 4 + nsrc;
-    std::vector<double> tab((size_t)W * nsteps);
+    const size_t need = (size_t)W * nsteps;
+    omx_ctx::HostStage &hs = c->tab_stage[c->tab_flip];
+    c->tab_flip ^= 1;
+    if (hs.ev) ck(cudaEventSynchronize(hs.ev), "staging");   // its previous copy has been consumed
+    else ck(cudaEventCreateWithFlags(&hs.ev, cudaEventDisableTiming), "event");
+    if (hs.cap < need) {
+        if (hs.p) cudaFreeHost(hs.p);
+        hs.p = nullptr;
+        hs.cap = 0;
+        ck(cudaMallocHost(&hs.p, need * sizeof(double)), "pinned staging");
+        hs.cap = need;
+    }
+    double *tab = hs.p;
     const int tt_0 = (n_skip == 1) ? 1 : 0;
     int nrec = 0;
     for (int s = 0; s < nsteps; ++s) {
@@ -983,15 +1038,20 @@ template <class R> void run_impl(omx_ctx *c, int tt0, int nsteps, int n_skip, in
         }
         int slot = -1;
         if (has_det && tt % t_det_print == 0) slot = c->rec_count + nrec++;
-        tab[(size_t)0 * nsteps + s] = time;
-        tab[(size_t)1 * nsteps + s] = c->t_skip;
-        tab[(size_t)2 * nsteps + s] = move ? 1.0 : 0.0;
-        tab[(size_t)3 * nsteps + s] = (double)slot;
-        for (int q = 0; q < nsrc; ++q) tab[(size_t)(4 + q) * nsteps + s] = source_amp(*c->sources[q], time);
+        double *row = tab + (size_t)s * W;
+        row[0] = time;
+        row[1] = c->t_skip;
+        row[2] = move ? 1.0 : 0.0;
+        row[3] = (double)slot;
+        for (int q = 0; q < nsrc; ++q) row[4 + q] = source_amp(*c->sources[q], time);
     }
     if (has_det) ensure_rec_capacity(c, c->rec_count + nrec);
-    c->tab.alloc(tab.size(), false);
-    ck(cudaMemcpyAsync(c->tab.p, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream), "tab");
+    if (need > c->tab.n) {
+        c->tab.alloc(std::max(need, 2 * c->tab.n), false);
+        c->epoch++;
+    }
+    ck(cudaMemcpyAsync(c->tab.p, tab, need * sizeof(double), cudaMemcpyHostToDevice, c->stream), "tab");
+    ck(cudaEventRecord(hs.ev, c->stream), "staging");
     if (!c->d_step.p) c->d_step.alloc(1);
     // the first kernel of every step advances the counter, so it starts one below step 0
     ck(cudaMemsetAsync(c->d_step.p, 0xff, sizeof(int), c->stream), "step");
@@ -1000,7 +1060,7 @@ template <class R> void run_impl(omx_ctx *c, int tt0, int nsteps, int n_skip, in
         omx_ctx *c;
         ~Reset() { c->run_step = nullptr; }
     } reset{c};
-    auto P = [&](int row) { return StepParam{0.0, c->tab.p + (size_t)row * nsteps, c->d_step.p}; };
+    auto P = [&](int row) { return StepParam{0.0, c->tab.p + row, c->d_step.p, W}; };
     std::vector<StepParam> amps;
     for (int q = 0; q < nsrc; ++q) amps.push_back(P(4 + q));
     const bool fused = std::is_same<R, float>::value && c->fused_ok;
@@ -1020,33 +1080,99 @@ template <class R> void run_impl(omx_ctx *c, int tt0, int nsteps, int n_skip, in
         }
         tail();
     };
-    // the fused path alternates buffer sets, so a captured graph covers two steps
-    const int per_graph = fused ? 2 : 1;
-    if (use_graph && !c->prof && nsteps >= per_graph) {
-        if (c->gexec) {
-            cudaGraphExecDestroy(c->gexec);
-            c->gexec = nullptr;
+    // a captured graph of `steps` steps starting from the current buffer set, from the cache
+    // when the configuration is unchanged
+    auto launch_graph = [&](int steps, int times) {
+        omx_ctx::GraphRec *hit = nullptr;
+        for (auto &g : c->graphs)
+            if (g.epoch == c->epoch && g.steps == steps && g.cur == c->cur && g.W == W && g.has_det == (int)has_det &&
+                g.fused == (int)fused)
+                hit = &g;
+        if (!hit) {
+            for (auto &g : c->graphs)
+                if (g.epoch != c->epoch) cudaGraphExecDestroy(g.exec);
+            c->graphs.erase(std::remove_if(c->graphs.begin(), c->graphs.end(),
+                                           [&](const omx_ctx::GraphRec &g) { return g.epoch != c->epoch; }),
+                            c->graphs.end());
+            omx_ctx::GraphRec g{};
+            g.epoch = c->epoch;
+            g.steps = steps;
+            g.cur = c->cur;
+            g.W = W;
+            g.has_det = has_det;
+            g.fused = fused;
+            cudaGraph_t graph;
+            const long long before = c->launches;
+            ck(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "capture");
+            for (int q = 0; q < steps; ++q) one_step();
+            ck(cudaStreamEndCapture(c->stream, &graph), "end capture");
+            g.launches = c->launches - before;
+            c->launches = before;
+            g.cur_after = c->cur;
+            c->cur = g.cur;
+            const cudaError_t e = cudaGraphInstantiate(&g.exec, graph, 0);
+            cudaGraphDestroy(graph);
+            ck(e, "instantiate");
+            c->graphs.push_back(g);
+            hit = &c->graphs.back();
         }
-        cudaGraph_t graph;
-        const long long before = c->launches;
-        const int cur0 = c->cur;
-        ck(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "capture");
-        for (int q = 0; q < per_graph; ++q) one_step();
-        ck(cudaStreamEndCapture(c->stream, &graph), "end capture");
-        const long long per_launch = c->launches - before;
-        c->launches = before;
-        c->cur = cur0;
-        ck(cudaGraphInstantiate(&c->gexec, graph, 0), "instantiate");
-        cudaGraphDestroy(graph);
+        for (int s = 0; s < times; ++s) ck(cudaGraphLaunch(hit->exec, c->stream), "graph launch");
+        c->launches += hit->launches * times;
+        c->cur = hit->cur_after;   // after an even number of fused steps this is the starting set
+    };
+    // the fused path alternates buffer sets, so the main graph covers two steps
+    const int per_graph = fused ? 2 : 1;
+    if (use_graph && !c->prof) {
         const int ngraph = nsteps / per_graph;
-        for (int s = 0; s < ngraph; ++s) ck(cudaGraphLaunch(c->gexec, c->stream), "graph launch");
-        c->launches += per_launch * ngraph;
-        for (int s = ngraph * per_graph; s < nsteps; ++s) one_step();
+        if (ngraph > 0) launch_graph(per_graph, ngraph);
+        if (nsteps > ngraph * per_graph) launch_graph(1, 1);
     } else {
         for (int s = 0; s < nsteps; ++s) one_step();
     }
     ck(cudaPeekAtLastError(), "launch");
     c->rec_count += nrec;
+}
+
+// Time each candidate launch shape on the device and keep the fastest.  Runs on fields that are
+// still all zero: every kernel maps zero fields, zero psi and zero ADE state to zero, so the
+// candidates leave no trace in the simulation state.
+template <class R> int autotune_impl(omx_ctx *c, int reps)
+{
+    const bool fused = std::is_same<R, float>::value && c->fused_ok;
+    std::vector<int> cand;
+    if (fused) cand = {0, 4, 5, 6, 8};
+    else if (c->dims == 3) cand = {4, 8, 16, 32};
+    else if (c->dims == 2) cand = {8, 16, 32, 64};
+    else return 0;
+    float best = 0.f;
+    int pick = cand[0];
+    for (size_t k = 0; k < cand.size(); ++k) {
+        if (fused) c->fused_form = cand[k];
+        else c->march = cand[k];
+        auto once = [&]() {
+            if (fused) {
+                fused_step<R>(c);
+            } else {
+                do_H<R>(c);
+                do_E<R>(c, imm(0.0), imm(0.0));
+            }
+        };
+        once();   // first use of a form sets its kernel attributes
+        ck(cudaEventRecord(c->t0, c->stream), "autotune");
+        for (int r = 0; r < reps; ++r) once();
+        ck(cudaEventRecord(c->t1, c->stream), "autotune");
+        ck(cudaEventSynchronize(c->t1), "autotune");
+        float ms = 0.f;
+        ck(cudaEventElapsedTime(&ms, c->t0, c->t1), "autotune");
+        if (k == 0 || ms < best) {
+            best = ms;
+            pick = cand[k];
+        }
+    }
+    if (fused) c->fused_form = pick;
+    else c->march = pick;
+    ck(cudaPeekAtLastError(), "autotune");
+    return pick;
 }
 
 template <class R> void read_field_impl(omx_ctx *c, int field, double *host)
@@ -1055,7 +1181,7 @@ template <class R> void read_field_impl(omx_ctx *c, int field, double *host)
     req(bounds_of(c, field, lo, hi), "field not present in this grid/mode");
     const int q = field_code_to_index(field);
     std::vector<R> tmp(c->felems);
-    ck(cudaStreamSynchronize(c->stream), "sync");
+    sync_checked(c, "sync");
     ck(cudaMemcpy(tmp.data(), field_ptrs<R>(c).f[q], c->felems * sizeof(R), cudaMemcpyDeviceToHost), "read field");
     long long o = 0;
     for (int k = lo[2]; k <= hi[2]; ++k)
@@ -1077,7 +1203,7 @@ template <class R> void write_field_impl(omx_ctx *c, int field, const double *ho
     req(bounds_of(c, field, lo, hi), "field not present in this grid/mode");
     const int q = field_code_to_index(field);
     std::vector<R> tmp(c->felems);
-    ck(cudaStreamSynchronize(c->stream), "sync");
+    sync_checked(c, "sync");
     ck(cudaMemcpy(tmp.data(), field_ptrs<R>(c).f[q], c->felems * sizeof(R), cudaMemcpyDeviceToHost), "read field");
     long long o = 0;
     for (int k = lo[2]; k <= hi[2]; ++k)
@@ -1214,6 +1340,9 @@ int omx_create(const omx_grid_desc *d, omx_ctx **out)
         if (c->fp32) build_media<float>(c, nullptr, noeps);
         else build_media<double>(c, nullptr, noeps);
         c->jbuf.alloc(9);
+        c->d_err.alloc(1);
+        ck(cudaMallocHost(&c->h_err, sizeof(int)), "pinned error word");
+        *c->h_err = 0;
         ck(cudaEventCreate(&c->t0), "event");
         ck(cudaEventCreate(&c->t1), "event");
         *out = C.release();
@@ -1235,9 +1364,14 @@ int omx_destroy(omx_ctx *c)
         cudaEventDestroy(e.a);
         cudaEventDestroy(e.b);
     }
-    if (c->gexec) cudaGraphExecDestroy(c->gexec);
+    for (auto &g : c->graphs) cudaGraphExecDestroy(g.exec);
+    for (auto &h : c->tab_stage) {
+        if (h.p) cudaFreeHost(h.p);
+        if (h.ev) cudaEventDestroy(h.ev);
+    }
     if (c->t0) cudaEventDestroy(c->t0);
     if (c->t1) cudaEventDestroy(c->t1);
+    if (c->h_err) cudaFreeHost(c->h_err);
     cudaStream_t s = c->stream;
     delete c;
     if (s) cudaStreamDestroy(s);
@@ -1248,7 +1382,7 @@ int omx_synchronize(omx_ctx *c)
 {
     OMX_API_BEGIN
     req(c, "null context");
-    ck(cudaStreamSynchronize(c->stream), "synchronize");
+    sync_checked(c, "synchronize");
     OMX_API_END(c)
 }
 
@@ -1297,6 +1431,7 @@ int omx_set_cpml_tables(omx_ctx *c, const double *be, const double *ce, const do
 {
     OMX_API_BEGIN
     req(c, "null context");
+    c->epoch++;
     req(!c->started, "tables must be set before the first step", OMX_ERR_STATE);
     const int npml = c->desc.npml;
     if (be && ce && bh && ch && npml >= 2) {
@@ -1321,6 +1456,7 @@ int omx_set_media(omx_ctx *c, int n_media, const omx_medium *media, const int32_
 {
     OMX_API_BEGIN
     req(c, "null context");
+    c->epoch++;
     req(!c->started, "media must be set before the first step", OMX_ERR_STATE);
     req(n_media >= 0 && n_media < 255, "n_media out of range");
     req(n_media == 0 || media, "media descriptors missing");
@@ -1408,6 +1544,7 @@ int omx_source_add(omx_ctx *c, const omx_source_desc *d, int *id)
 {
     OMX_API_BEGIN
     req(c && d, "null argument");
+    c->epoch++;
     req(d->dir == 'x' || d->dir == 'y' || d->dir == 'z', "source direction must be x, y or z");
     if (c->dims == 1) req(d->dir == 'x', "1D sources must be along x (interactions_mod.f90:43-53)");
     if (c->dims == 2) {
@@ -1462,6 +1599,7 @@ int omx_plane_source_add(omx_ctx *c, const omx_plane_source_desc *d, int *id)
 {
     OMX_API_BEGIN
     req(c && d, "null argument");
+    c->epoch++;
     req(d->comp >= 1 && d->comp <= 3 && d->plane_axis >= 1 && d->plane_axis <= c->dims, "plane source axis/comp");
     req(c->field_used[d->comp - 1], "plane source component not present in this grid/mode");
     req(d->plane_index >= 1 && d->plane_index <= c->n[d->plane_axis - 1], "plane index");
@@ -1497,6 +1635,7 @@ int omx_qgroup_create(omx_ctx *c, const omx_qgroup_desc *d, const int32_t *cell,
 {
     OMX_API_BEGIN
     req(c && d && cell && params, "null argument");
+    c->epoch++;
     req(!c->started, "q-groups must be created before the first step", OMX_ERR_STATE);
     req(d->model == OMX_EMITTER_TWO_LEVEL || d->model == OMX_EMITTER_THREE_LEVEL, "emitter model");
     req(d->group_type == OMX_Q_MATERIAL || d->group_type == OMX_Q_SINGLE, "group type");
@@ -1519,6 +1658,14 @@ int omx_qgroup_create(omx_ctx *c, const omx_qgroup_desc *d, const int32_t *cell,
     G->ck.upload(ckk);
     std::vector<double> par(params, params + (size_t)n * G->npar);
     G->par.upload(par);
+    // decay rates 1/T1, 1/T2 (IEEE quotients, the same values the oracle forms every step)
+    std::vector<double> rates((size_t)2 * n);
+    const int it1 = d->model == OMX_EMITTER_TWO_LEVEL ? 2 : 4;
+    for (int e = 0; e < n; ++e) {
+        rates[2 * e] = 1.0 / par[(size_t)e * G->npar + it1];
+        rates[2 * e + 1] = 1.0 / par[(size_t)e * G->npar + it1 + 1];
+    }
+    G->rates.upload(rates);
     G->rho.alloc((size_t)n * G->nst);
     G->E.alloc((size_t)n * 3);
     G->dipole.alloc((size_t)n * 3);
@@ -1583,6 +1730,7 @@ int omx_detector_add(omx_ctx *c, int type, int field, int nd, const int32_t *idx
 {
     OMX_API_BEGIN
     req(c && idx && nd >= 1, "bad argument");
+    c->epoch++;
     req(type >= OMX_POINT_DETECTOR && type <= OMX_VOLUME_DETECTOR, "detector type");
     req(field >= OMX_EX_FIELD && field <= OMX_HZ_FIELD, "field");
     req(c->field_used[field - 1], "detector field not present in this grid/mode");
@@ -1638,6 +1786,7 @@ int omx_detectors_set_capacity(omx_ctx *c, int records)
 {
     OMX_API_BEGIN
     req(c && records >= 1, "bad argument");
+    c->epoch++;
     prepare(c);
     ensure_rec_capacity(c, records);
     OMX_API_END(c)
@@ -1661,7 +1810,7 @@ int omx_detectors_drain(omx_ctx *c, double *times, double *values, int max_recor
 {
     OMX_API_BEGIN
     req(c && n_records, "null argument");
-    ck(cudaStreamSynchronize(c->stream), "sync");
+    sync_checked(c, "sync");
     const int npts = (int)c->tap_field.size();
     const int n = std::min(c->rec_count, max_records);
     if (n > 0) {
@@ -1692,6 +1841,22 @@ int omx_run(omx_ctx *c, int tt0, int nsteps, int n_skip_steps, int t_det_print, 
     OMX_API_END(c)
 }
 
+int omx_autotune(omx_ctx *c, int reps, int *choice)
+{
+    OMX_API_BEGIN
+    req(c && reps >= 1, "bad argument");
+    req(!c->started && !c->fields_written,
+        "omx_autotune times kernels on the initial zero fields: call it after the grid is configured and "
+        "before the first step or field write", OMX_ERR_STATE);
+    req(!c->prof, "profiling is on");
+    prepare(c);
+    c->epoch++;
+    const int pick = c->fp32 ? autotune_impl<float>(c, reps) : autotune_impl<double>(c, reps);
+    sync_checked(c, "autotune");
+    if (choice) *choice = pick;
+    OMX_API_END(c)
+}
+
 int omx_field_bounds(const omx_ctx *c, int field, int lo[3], int hi[3])
 {
     OMX_API_BEGIN
@@ -1713,6 +1878,7 @@ int omx_write_field(omx_ctx *c, int field, const double *host)
 {
     OMX_API_BEGIN
     req(c && host, "null argument");
+    c->fields_written = true;
     if (c->fp32) write_field_impl<float>(c, field, host);
     else write_field_impl<double>(c, field, host);
     OMX_API_END(c)
@@ -1722,6 +1888,7 @@ int omx_profile_enable(omx_ctx *c, int on)
 {
     OMX_API_BEGIN
     req(c, "null context");
+    c->epoch++;
     prof_collect(c);
     c->prof = on != 0;
     for (int k = 0; k < KC_N; ++k) {

@@ -37,12 +37,13 @@ __device__ __forceinline__ void rhs3(const double *pr, double E_u, double g1r, d
     d[7] = -(de * a21) + g2 * a10 - g1 * a20 - b21 * g2r;
 }
 
+// One RK4 step with the decay rates g1 = 1/T1, g2 = 1/T2 and the step fractions h2 = dt/2,
+// h6 = dt/6 supplied by the caller (formed once, not per emitter and step).
 template <int NST>
-__device__ __forceinline__ void rk4(int model, const double *pr, double *rho, double E_u, double dt)
+__device__ __forceinline__ void rk4r(int model, const double *pr, double *rho, double E_u, double dt, double h2,
+                                     double h6, double g1, double g2)
 {
     double k1[NST], k2[NST], k3[NST], k4[NST], t[NST];
-    const double h2 = 0.5 * dt, h6 = dt / 6.0;
-    const double g1 = 1.0 / pr[model == 1 ? 2 : 4], g2 = 1.0 / pr[model == 1 ? 3 : 5];
     if (model == 1) rhs2(pr, E_u, g1, g2, rho, k1); else rhs3(pr, E_u, g1, g2, rho, k1);
 #pragma unroll
     for (int q = 0; q < NST; ++q) t[q] = rho[q] + h2 * k1[q];
@@ -55,6 +56,14 @@ __device__ __forceinline__ void rk4(int model, const double *pr, double *rho, do
     if (model == 1) rhs2(pr, E_u, g1, g2, t, k4); else rhs3(pr, E_u, g1, g2, t, k4);
 #pragma unroll
     for (int q = 0; q < NST; ++q) rho[q] = rho[q] + h6 * (k1[q] + 2.0 * k2[q] + 2.0 * k3[q] + k4[q]);
+}
+
+// Same step forming the rates and fractions itself.
+template <int NST>
+__device__ __forceinline__ void rk4(int model, const double *pr, double *rho, double E_u, double dt)
+{
+    const double g1 = 1.0 / pr[model == 1 ? 2 : 4], g2 = 1.0 / pr[model == 1 ? 3 : 5];
+    rk4r<NST>(model, pr, rho, E_u, dt, 0.5 * dt, dt / 6.0, g1, g2);
 }
 
 }  // namespace omx

@@ -18,6 +18,7 @@
 // source point lies in a dispersive cell.
 #pragma once
 #include "omx_stencil.cuh"
+#include "omx_tma.cuh"
 
 namespace omx {
 
@@ -220,6 +221,275 @@ __global__ void __launch_bounds__(128, 6) k_fused_tmz(Fused2Args A, GridArgs<flo
         const int j1 = (int)min((long long)ny, (long long)j0 + (r1 - r) - 1);
         fused_tmz_rows<XCPML>(A, G, strip, j0, j1);
         r += j1 - j0 + 1;
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Bulk-copy variant: the same arithmetic, with the rows of Ez / Hx / Hy staged into shared memory
+// by the TMA engine (cp.async.bulk, completion on an mbarrier per ring slot).  One thread issues
+// the copies D-1 rows ahead of the row being computed, so the bytes in flight per SM no longer
+// depend on registers.  A staged Ez / Hy row spans the strip's 512 columns plus 4 halo columns
+// on each side (the left neighbour of the first cell, Ez(i+4) of the last thread); since every
+// staged word is a copy of the same global address, results equal the register kernel's.
+//
+// Work items of one row segment (strip, rows j0..j1), in issue order:
+//   item 0          row j0-1  Ez, Hx  (recomputes Hx_new(j0-1); nothing at a PEC ghost row)
+//   items 1..n      rows j0..j1  Ez, Hx, Hy
+//   item n+1        row j1+1  Ez only
+// Step k (0..n) consumes items k and k+1, then releases item k (and item n+1 after step n).
+constexpr int FZ_W = 512;                     // columns per strip: 128 threads x 4 cells
+constexpr int FZ_EW = FZ_W + 8;               // Ez / Hy window with 4 halo columns each side
+struct FzStage {
+    float ez[FZ_EW];                          // columns ib0-4 .. ib0+515
+    float hy[FZ_EW];
+    float hx[FZ_W];                           // columns ib0 .. ib0+511
+};
+static_assert(sizeof(FzStage) % 16 == 0, "bulk copies need 16-byte aligned stage arrays");
+constexpr long long FZ_WAIT_CYCLES = 2000000000LL;   // about one second at the SM clock
+
+struct FzSeg {
+    int strip, j0, j1;
+};
+__device__ __forceinline__ FzSeg fz_segment(long long r, long long r1, long long ny)
+{
+    FzSeg s;
+    s.strip = (int)(r / ny);
+    s.j0 = (int)(r % ny) + 1;
+    s.j1 = (int)min(ny, (long long)s.j0 + (r1 - r) - 1);
+    return s;
+}
+
+// Issue the copies of item k of segment S into stage st; completes on bar (one arrival).
+__device__ __forceinline__ void fz_issue(const Fused2Args &A, const GridArgs<float> &G, const FzSeg &S, int k,
+                                         FzStage *st, uint64_t *bar)
+{
+    const Lay &L = G.L;
+    const int ib0 = 1 + FZ_W * S.strip;
+    const uint32_t ezb = 4u * (uint32_t)min(FZ_EW, L.nx - ib0 + 9);   // nx % 4 == 0: multiple of 16 B
+    const uint32_t hxb = 4u * (uint32_t)min(FZ_W, L.nx - ib0 + 1);
+    const int last = S.j1 - S.j0 + 2;
+    int row = S.j0 - 1 + k;
+    bool ld_ez = true, ld_hx = k < last, ld_hy = k > 0 && k < last;
+    if (k == 0 && row == 0) {
+        if (G.per[1]) row = L.ny;                                     // Hx_new(0) = Hx_new(ny)
+        else ld_ez = ld_hx = false;                                   // PEC ghost row: Hx_new = 0
+    }
+    if (k == last && row == L.ny + 1 && G.per[1]) row = 1;            // Ez(ny+1) = Ez(1)
+    const long long e0 = L.off + (ib0 - 4) + (long long)L.px * row;   // 16-byte aligned
+    const long long h0 = L.off + ib0 + (long long)L.px * row;         // 128-byte aligned
+    mbar_arrive_expect_tx(bar, (ld_ez ? ezb : 0u) + (ld_hx ? hxb : 0u) + (ld_hy ? ezb : 0u));
+    if (ld_ez) bulk_g2s(st->ez, A.ez_in + e0, ezb, bar);
+    if (ld_hx) bulk_g2s(st->hx, A.hx_in + h0, hxb, bar);
+    if (ld_hy) bulk_g2s(st->hy, A.hy_in + e0, ezb, bar);
+}
+
+template <bool XCPML, int D>
+__global__ void __launch_bounds__(128, 6) k_fused_tmz_tma(Fused2Args A, GridArgs<float> G, int nstrip)
+{
+    extern __shared__ __align__(128) unsigned char fz_smem[];
+    FzStage *stage = reinterpret_cast<FzStage *>(fz_smem);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(fz_smem + D * sizeof(FzStage));
+    const Lay &L = G.L;
+    const long long ny = L.ny;
+    const long long total = (long long)nstrip * ny;
+    const long long rb0 = total * blockIdx.x / gridDim.x;
+    const long long rb1 = total * (blockIdx.x + 1) / gridDim.x;
+    const int tl = threadIdx.x, lane = tl & 31;
+    if (tl == 0) {
+        if (G.step_inc && blockIdx.x == 0) *G.step_inc += 1;          // device-loop step counter
+        for (int s = 0; s < D; ++s) mbar_init(&bar[s], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    if (rb0 >= rb1) return;
+
+    // producer state (thread 0): the next item to issue and how many are issued / released
+    long long pr = rb0;
+    int pk = 0;
+    int issued = 0, released = 0;             // items: rows + 2 per segment (fits an int)
+    auto issue_more = [&]() {
+        while (pr < rb1 && issued < released + D) {
+            const FzSeg S = fz_segment(pr, rb1, ny);
+            const int slot = issued % D;
+            fz_issue(A, G, S, pk, &stage[slot], &bar[slot]);
+            ++issued;
+            if (++pk == S.j1 - S.j0 + 3) {
+                pk = 0;
+                pr += S.j1 - S.j0 + 1;
+            }
+        }
+    };
+    if (tl == 0) issue_more();
+
+    const float dt_mu0 = G.dt_mu0, dt_eps0 = G.dt_eps0;
+    const long long px = L.px;
+    bool fail = false;
+    int m = 0;                                // index of the current segment's item 0
+    for (long long r = rb0; r < rb1;) {
+        const FzSeg S = fz_segment(r, rb1, ny);
+        const int ib0 = 1 + FZ_W * S.strip;
+        const int ib = ib0 + 4 * tl;
+        const bool active = ib <= L.nx;
+        const int ibc = active ? ib : 1;      // lanes past nx only join the shuffles
+        float dhx[4], dex[4], bhx[4], chx[4], bex[4], cex[4];
+        int lhx[4], lex[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int i = XCPML ? min(ibc + q, L.nx) : 1;
+            dhx[q] = G.den_h[0][i];
+            dex[q] = G.den_e[0][i];
+            lhx[q] = XCPML ? G.lH[0][i] : -1;
+            lex[q] = XCPML ? G.lE[0][i] : -1;
+            bhx[q] = XCPML ? G.bH[0][i] : 0.f;
+            chx[q] = XCPML ? G.cH[0][i] : 0.f;
+            bex[q] = XCPML ? G.bE[0][i] : 0.f;
+            cex[q] = XCPML ? G.cE[0][i] : 0.f;
+        }
+        const bool left_ghost = (ibc == 1) && !G.per[0];
+        const int il = (ibc == 1) ? L.nx : ibc - 1;
+        const float dhx_l = G.den_h[0][XCPML ? il : 1];
+        const int lhx_l = XCPML ? G.lH[0][il] : -1;
+        const float bhx_l = XCPML ? G.bH[0][il] : 0.f, chx_l = XCPML ? G.cH[0][il] : 0.f;
+        const bool wrap_r = ibc + 4 > L.nx && G.per[0];
+        const bool bb_i = G.bbV > 0 && (ibc + 3 >= G.bb0[0] && ibc <= G.bb1[0]);
+        const long long col = L.off + ibc;
+        const int n = S.j1 - S.j0 + 1;
+
+        // step 0: Hx_new(j0-1) from items 0 and 1
+        float hxp[4] = {0.f, 0.f, 0.f, 0.f};
+        {
+            const int s0 = m % D, s1 = (m + 1) % D;
+            fail |= !mbar_wait_bounded(&bar[s0], (uint32_t)((m / D) & 1), FZ_WAIT_CYCLES);
+            fail |= !mbar_wait_bounded(&bar[s1], (uint32_t)(((m + 1) / D) & 1), FZ_WAIT_CYCLES);
+            fail = __any_sync(0xffffffffu, fail);   // warp-uniform, so the shuffles below stay converged
+            const int jm = S.j0 - 1;
+            if (!fail && !(jm == 0 && !G.per[1])) {
+                const int jr = (jm == 0) ? L.ny : jm;
+                const float4 e0 = *reinterpret_cast<const float4 *>(&stage[s0].ez[4 + 4 * tl]);
+                const float4 e1 = *reinterpret_cast<const float4 *>(&stage[s1].ez[4 + 4 * tl]);
+                const float4 h0 = *reinterpret_cast<const float4 *>(&stage[s0].hx[4 * tl]);
+                const float dhy = G.den_h[1][jr];
+                const int ly = G.lH[1][jr];
+                const float bh = G.bH[1][jr], ch = G.cH[1][jr];
+                const long long pb = (ibc - 1) + (long long)L.nx * ly;
+                hxp[0] = fz_hx(h0.x, e0.x, e1.x, dhy, dt_mu0, ly, bh, ch, A.psi_hxy_in, nullptr, pb + 0);
+                hxp[1] = fz_hx(h0.y, e0.y, e1.y, dhy, dt_mu0, ly, bh, ch, A.psi_hxy_in, nullptr, pb + 1);
+                hxp[2] = fz_hx(h0.z, e0.z, e1.z, dhy, dt_mu0, ly, bh, ch, A.psi_hxy_in, nullptr, pb + 2);
+                hxp[3] = fz_hx(h0.w, e0.w, e1.w, dhy, dt_mu0, ly, bh, ch, A.psi_hxy_in, nullptr, pb + 3);
+            }
+        }
+        if (__syncthreads_or(fail)) goto drain;
+        if (tl == 0) {
+            ++released;
+            issue_more();
+        }
+
+        // steps 1..n: row j = j0-1+k from items k (rows j) and k+1 (Ez of row j+1)
+        for (int k = 1; k <= n; ++k) {
+            const int j = S.j0 - 1 + k;
+            const int sc = (m + k) % D, sn = (m + k + 1) % D;
+            fail |= !mbar_wait_bounded(&bar[sn], (uint32_t)(((m + k + 1) / D) & 1), FZ_WAIT_CYCLES);
+            fail = __any_sync(0xffffffffu, fail);
+            if (!fail) {
+                const FzStage &C = stage[sc];
+                const float4 ez_c = *reinterpret_cast<const float4 *>(&C.ez[4 + 4 * tl]);
+                const float4 ez_n = *reinterpret_cast<const float4 *>(&stage[sn].ez[4 + 4 * tl]);
+                const float4 hx_o = *reinterpret_cast<const float4 *>(&C.hx[4 * tl]);
+                const float4 hy_o = *reinterpret_cast<const float4 *>(&C.hy[4 + 4 * tl]);
+                const long long row = col + px * j;
+                // Ez(i+4, j): next lane's first cell, the staged halo, or Ez(1, j) when periodic
+                float ez_r = __shfl_down_sync(0xffffffffu, ez_c.x, 1);
+                if (lane == 31 || ibc + 4 > L.nx) ez_r = wrap_r ? A.ez_in[L.off + 1 + px * j] : C.ez[8 + 4 * tl];
+                const float dhy = G.den_h[1][j], dey = G.den_e[1][j];
+                const int ly = G.lH[1][j], lye = G.lE[1][j];
+                const float bhy = G.bH[1][j], chy = G.cH[1][j], bey = G.bE[1][j], cey = G.cE[1][j];
+                const float ez[5] = {ez_c.x, ez_c.y, ez_c.z, ez_c.w, ez_r};
+                const float ezn[4] = {ez_n.x, ez_n.y, ez_n.z, ez_n.w};
+                const float hxo[4] = {hx_o.x, hx_o.y, hx_o.z, hx_o.w};
+                const float hyo[4] = {hy_o.x, hy_o.y, hy_o.z, hy_o.w};
+                float hx[4], hy[4];
+                const long long pby = (ibc - 1) + (long long)L.nx * ly;
+                const long long pbx = (long long)G.L2 * (j - 1);
+                float *const psx_out = active ? A.psi_hxy_out : nullptr;
+                float *const psy_out = active ? A.psi_hyx_out : nullptr;
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    hx[q] = fz_hx(hxo[q], ez[q], ezn[q], dhy, dt_mu0, ly, bhy, chy, A.psi_hxy_in, psx_out, pby + q);
+                    hy[q] = fz_hy(hyo[q], ez[q], ez[q + 1], dhx[q], dt_mu0, lhx[q], bhx[q], chx[q], A.psi_hyx_in,
+                                  psy_out, lhx[q] + pbx);
+                }
+                // Hy_new(i-1, j): previous lane's last cell; lane 0 recomputes it from the staged
+                // left column, or from global memory for the periodic image of column 1
+                float hy_l = __shfl_up_sync(0xffffffffu, hy[3], 1);
+                if (active && (lane == 0 || ib == 1)) {
+                    if (left_ghost) {
+                        hy_l = 0.f;
+                    } else if (ib == 1) {
+                        const long long rl = L.off + il + px * j;
+                        hy_l = fz_hy(A.hy_in[rl], A.ez_in[rl], ez[0], dhx_l, dt_mu0, lhx_l, bhx_l, chx_l,
+                                     A.psi_hyx_in, nullptr, lhx_l + pbx);
+                    } else {
+                        hy_l = fz_hy(C.hy[3 + 4 * tl], C.ez[3 + 4 * tl], ez[0], dhx_l, dt_mu0, lhx_l, bhx_l, chx_l,
+                                     A.psi_hyx_in, nullptr, lhx_l + pbx);
+                    }
+                }
+                if (active) {
+                    *reinterpret_cast<float4 *>(A.hx_out + row) = make_float4(hx[0], hx[1], hx[2], hx[3]);
+                    *reinterpret_cast<float4 *>(A.hy_out + row) = make_float4(hy[0], hy[1], hy[2], hy[3]);
+                    if (G.per[0] && ib + 3 == L.nx) A.hy_out[row + 3 - L.nx] = hy[3];            // Hy(0,j) = Hy(nx,j)
+                    if (G.per[1] && j == L.ny)
+                        *reinterpret_cast<float4 *>(A.hx_out + row - px * L.ny) = make_float4(hx[0], hx[1], hx[2], hx[3]);
+                    const bool bb = bb_i && j >= G.bb0[1] && j <= G.bb1[1];
+                    float eo[4];
+                    const float hyl[4] = {hy_l, hy[0], hy[1], hy[2]};
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        const float dyh = hy[q] - hyl[q];
+                        const float dxh = hxp[q] - hx[q];
+                        const float rr = dyh * dex[q] + dxh * dey;
+                        float e = ez[q];
+                        if (bb && ibc + q >= G.bb0[0] && ibc + q <= G.bb1[0]) {
+                            const long long b = (ibc + q - G.bb0[0]) + (long long)G.bbd[0] * (j - G.bb0[1]);
+                            e = plain_update<float>(e, rr, G.mat[2][b], G);
+                        } else {
+                            e = e + dt_eps0 * rr;
+                        }
+                        if (XCPML && lex[q] >= 0) {
+                            const long long p = lex[q] + pbx;
+                            const float v = bex[q] * A.psi_ezx[p] + cex[q] * dyh;
+                            A.psi_ezx[p] = v;
+                            e = e + dt_eps0 * v;
+                        }
+                        if (lye >= 0) {
+                            const long long p = (ibc + q - 1) + (long long)L.nx * lye;
+                            const float v = bey * A.psi_ezy[p] + cey * dxh;
+                            A.psi_ezy[p] = v;
+                            e = e + dt_eps0 * v;
+                        }
+                        eo[q] = e;
+                    }
+                    *reinterpret_cast<float4 *>(A.ez_out + row) = make_float4(eo[0], eo[1], eo[2], eo[3]);
+                }
+#pragma unroll
+                for (int q = 0; q < 4; ++q) hxp[q] = hx[q];
+            }
+            if (__syncthreads_or(fail)) goto drain;
+            if (tl == 0) {
+                released += (k == n) ? 2 : 1;     // the last step also frees the Ez-only item
+                issue_more();
+            }
+        }
+        m += n + 2;
+        r += n;
+    }
+    return;
+drain:
+    // a wait ran out: flag it, give the copies still in flight a bounded time to land (so that no
+    // copy writes this block's shared memory after it exits) and leave
+    if (tl == 0) {
+        atomicOr(A.err, 1);
+        for (int q = released; q < issued; ++q)
+            mbar_wait_bounded(&bar[q % D], (uint32_t)((q / D) & 1), FZ_WAIT_CYCLES);
     }
 }
 

@@ -29,11 +29,13 @@ struct Lay {
     long long off;    // element offset of (0,0,0)
 };
 
-// Scalar that is either an immediate value or table[*step] on the device (for graphs).
+// Scalar that is either an immediate value or tab[*step * stride] on the device (for graphs:
+// the run's per-step table is step-major, one row of `stride` scalars per step).
 struct StepParam {
     double val;
     const double *tab;
     const int *step;
+    int stride;
 };
 
 enum ClsType { CLS_PLAIN = 0, CLS_DRUDE = 1, CLS_DL = 2 };
@@ -78,6 +80,8 @@ template <class R> struct GridArgs {
     const int *ade_b;
     // device-loop step counter, advanced by the first kernel of each step (null outside omx_run)
     int *step_inc;
+    // planes (3D) or rows (2D) marched per thread by the unfused kernels; 0 = default
+    int march;
 };
 
 template <class R> struct FieldPtrs {
@@ -115,8 +119,9 @@ struct EmitArgs {
     int n, model, npar, nst, dims, mode2d;
     const int *ci, *cj, *ck;
     const double *par;
+    const double *rates;      // (1/T1, 1/T2) per emitter, formed at group creation
     double *rho, *E, *dipole, *dPdt;
-    double dt;
+    double dt, h2, h6;        // dt, dt/2, dt/6
 };
 
 struct ScatArgs {
@@ -155,8 +160,10 @@ struct Fused2Args {
     const float *psi_hyx_in, *psi_hxy_in;   // x-face psi of Hy, y-face psi of Hx (old)
     float *psi_hyx_out, *psi_hxy_out;
     float *psi_ezx, *psi_ezy;               // E psi, updated in place
+    int *err;                               // device error word (bit 0: a bulk-copy wait ran out)
 };
-void launch_fused_tmz(const Fused2Args &A, const GridArgs<float> &G, void *stream);
+// form: 0 register prefetch, 4/5/6/8 bulk-copy ring depth, < 0 the default
+void launch_fused_tmz(const Fused2Args &A, const GridArgs<float> &G, int form, void *stream);
 void launch_ade_post(const FieldPtrs<float> &Fin, const FieldPtrs<float> &Fout, const GridArgs<float> &G, void *stream);
 void launch_flush(float *buf, long long n, void *stream);
 

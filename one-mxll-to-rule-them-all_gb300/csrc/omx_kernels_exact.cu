@@ -39,12 +39,13 @@ template <class R> void launch_inject(const FieldPtrs<R> &F, const JState &J, co
 template <class R> void launch_emit(const FieldPtrs<R> &F, const Lay &L, const EmitArgs &A, StepParam move, void *s)
 {
     if (A.n <= 0) return;
-    k_emit<R><<<(A.n + 127) / 128, 128, 0, (cudaStream_t)s>>>(F, L, A, move);
+    // one warp per block: the FP64 work of a few thousand emitters spreads over every SM
+    k_emit<R><<<(A.n + 31) / 32, 32, 0, (cudaStream_t)s>>>(F, L, A, move);
 }
 void launch_scatter(const JState &J, const ScatArgs &S, StepParam move, void *s)
 {
     if (S.np <= 0) return;
-    k_scatter<<<(S.np + 127) / 128, 128, 0, (cudaStream_t)s>>>(J, S, move);
+    k_scatter<<<(S.np + 63) / 64, 64, 0, (cudaStream_t)s>>>(J, S, move);
 }
 template <class R> void launch_sample(const FieldPtrs<R> &F, const DetArgs &D, StepParam slot, StepParam time, void *s)
 {

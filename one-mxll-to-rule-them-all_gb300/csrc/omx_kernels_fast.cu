@@ -2,6 +2,9 @@
 // state with FP64-precomputed coefficients rounded once to FP32; multiply-adds contract to FMA.
 #include <cuda_runtime.h>
 
+#include <stdlib.h>
+#include <string.h>
+
 #include <algorithm>
 #include "omx_fused2d.cuh"
 
@@ -16,26 +19,79 @@ template <> void launch_e<float>(const FieldPtrs<float> &F, const GridArgs<float
     launch_e_impl<float, false>(F, G, s);
 }
 
-static int persistent_blocks(const void *kernel)
+static int persistent_blocks(const void *kernel, size_t smem)
 {
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 128, smem);
     return (sms > 0 ? sms : 152) * (per_sm > 0 ? per_sm : 1);
 }
 
-void launch_fused_tmz(const Fused2Args &A, const GridArgs<float> &G, void *s)
+// Default fused-kernel form: "regs" (register prefetch of the next row) or "tmaD" (rows staged
+// by bulk copies into a D-slot shared-memory ring).  OMX_FUSED_KERNEL overrides the default;
+// omx_autotune picks a form per grid.
+static int default_fused_form()
+{
+    static int form = -1;
+    if (form < 0) {
+        form = 5;
+        if (const char *v = getenv("OMX_FUSED_KERNEL")) {
+            if (!strcmp(v, "regs")) form = 0;
+            else if (!strcmp(v, "tma4")) form = 4;
+            else if (!strcmp(v, "tma5")) form = 5;
+            else if (!strcmp(v, "tma6")) form = 6;
+            else if (!strcmp(v, "tma8")) form = 8;
+        }
+    }
+    return form;
+}
+
+constexpr int FZ_MAX_DEV = 64;
+
+template <bool X, int D> static void launch_tma(const Fused2Args &A, const GridArgs<float> &G, int nstrip, cudaStream_t s)
+{
+    const size_t smem = D * sizeof(FzStage) + D * sizeof(uint64_t);
+    static int nb[FZ_MAX_DEV] = {};       // persistent grid per device (the smem opt-in is per device)
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int &n = nb[dev < FZ_MAX_DEV ? dev : 0];
+    if (n == 0) {
+        cudaFuncSetAttribute(k_fused_tmz_tma<X, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        n = persistent_blocks((const void *)k_fused_tmz_tma<X, D>, smem);
+    }
+    const int grid = (int)std::min<long long>(n, (long long)nstrip * G.L.ny);
+    k_fused_tmz_tma<X, D><<<grid, 128, smem, s>>>(A, G, nstrip);
+}
+
+template <bool X> static void launch_regs(const Fused2Args &A, const GridArgs<float> &G, int nstrip, cudaStream_t s)
+{
+    static int nb[FZ_MAX_DEV] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int &n = nb[dev < FZ_MAX_DEV ? dev : 0];
+    if (n == 0) n = persistent_blocks((const void *)k_fused_tmz<X>, 0);
+    const int grid = (int)std::min<long long>(n, (long long)nstrip * G.L.ny);
+    k_fused_tmz<X><<<grid, 128, 0, s>>>(A, G, nstrip);
+}
+
+template <bool X>
+static void launch_form(const Fused2Args &A, const GridArgs<float> &G, int form, int nstrip, cudaStream_t s)
+{
+    switch (form >= 0 ? form : default_fused_form()) {
+    case 0: launch_regs<X>(A, G, nstrip, s); break;
+    case 4: launch_tma<X, 4>(A, G, nstrip, s); break;
+    case 6: launch_tma<X, 6>(A, G, nstrip, s); break;
+    case 8: launch_tma<X, 8>(A, G, nstrip, s); break;
+    default: launch_tma<X, 5>(A, G, nstrip, s); break;
+    }
+}
+
+void launch_fused_tmz(const Fused2Args &A, const GridArgs<float> &G, int form, void *s)
 {
     const int nstrip = (G.L.nx / 4 + 127) / 128;
-    const void *k = A.psi_ezx ? (const void *)k_fused_tmz<true> : (const void *)k_fused_tmz<false>;
-    static int blocks_true = 0, blocks_false = 0;
-    int &nb = A.psi_ezx ? blocks_true : blocks_false;
-    if (nb == 0) nb = persistent_blocks(k);
-    const long long rows = (long long)nstrip * G.L.ny;
-    const int grid = (int)std::min<long long>(nb, rows);
-    if (A.psi_ezx) k_fused_tmz<true><<<grid, 128, 0, (cudaStream_t)s>>>(A, G, nstrip);
-    else k_fused_tmz<false><<<grid, 128, 0, (cudaStream_t)s>>>(A, G, nstrip);
+    if (A.psi_ezx) launch_form<true>(A, G, form, nstrip, (cudaStream_t)s);
+    else launch_form<false>(A, G, form, nstrip, (cudaStream_t)s);
 }
 
 void launch_ade_post(const FieldPtrs<float> &Fin, const FieldPtrs<float> &Fout, const GridArgs<float> &G, void *s)

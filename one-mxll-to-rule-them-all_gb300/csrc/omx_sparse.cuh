@@ -10,7 +10,7 @@ namespace omx {
 
 __device__ __forceinline__ double sp_get(const StepParam &p)
 {
-    return p.tab ? p.tab[*p.step] : p.val;
+    return p.tab ? p.tab[(long long)(*p.step) * p.stride] : p.val;
 }
 
 // ---- source_interactions (interactions_mod.f90:21-163) ----------------------------------------
@@ -117,17 +117,18 @@ __global__ void k_emit(FieldPtrs<R> F, Lay L, EmitArgs A, StepParam move_p)
     double rho[8];
     double *st = A.rho + (long long)n * A.nst;
     double d;
+    const double g1 = A.rates[2 * n], g2 = A.rates[2 * n + 1];
     if (A.model == 1) {
 #pragma unroll
         for (int q = 0; q < 3; ++q) rho[q] = st[q];
-        rk4<3>(1, pr, rho, E_u, A.dt);
+        rk4r<3>(1, pr, rho, E_u, A.dt, A.h2, A.h6, g1, g2);
 #pragma unroll
         for (int q = 0; q < 3; ++q) st[q] = rho[q];
         d = 2.0 * pr[1] * rho[1];
     } else {
 #pragma unroll
         for (int q = 0; q < 8; ++q) rho[q] = st[q];
-        rk4<8>(2, pr, rho, E_u, A.dt);
+        rk4r<8>(2, pr, rho, E_u, A.dt, A.h2, A.h6, g1, g2);
 #pragma unroll
         for (int q = 0; q < 8; ++q) st[q] = rho[q];
         d = 2.0 * pr[2] * rho[2] + 2.0 * pr[3] * rho[4];

@@ -517,11 +517,13 @@ void launch_h_impl(const FieldPtrs<R> &F, const GridArgs<R> &G, void *stream)
     cudaStream_t s = (cudaStream_t)stream;
     const Lay &L = G.L;
     if (L.dims == 3) {
-        dim3 b(32, 4, 1), g((L.nx + 31) / 32, (L.ny + 3) / 4, (L.nz + KCH3 - 1) / KCH3);
-        k_h3<R, EXACT><<<g, b, 0, s>>>(F, G, KCH3);
+        const int m = G.march > 0 ? G.march : KCH3;
+        dim3 b(32, 4, 1), g((L.nx + 31) / 32, (L.ny + 3) / 4, (L.nz + m - 1) / m);
+        k_h3<R, EXACT><<<g, b, 0, s>>>(F, G, m);
     } else if (L.dims == 2) {
-        dim3 b(128, 1, 1), g((L.nx + 127) / 128, (L.ny + JCH2 - 1) / JCH2, 1);
-        k_h2<R, EXACT><<<g, b, 0, s>>>(F, G, JCH2);
+        const int m = G.march > 0 ? G.march : JCH2;
+        dim3 b(128, 1, 1), g((L.nx + 127) / 128, (L.ny + m - 1) / m, 1);
+        k_h2<R, EXACT><<<g, b, 0, s>>>(F, G, m);
     } else {
         k_h1<R, EXACT><<<(L.nx + 127) / 128, 128, 0, s>>>(F, G);
     }
@@ -534,11 +536,13 @@ void launch_e_impl(const FieldPtrs<R> &F, const GridArgs<R> &G, void *stream)
     const Lay &L = G.L;
     if (G.ade_n > 0) k_ade<R><<<(G.ade_n + 127) / 128, 128, 0, s>>>(F, G);
     if (L.dims == 3) {
-        dim3 b(32, 4, 1), g((L.nx + 31) / 32, (L.ny + 3) / 4, (L.nz + KCH3 - 1) / KCH3);
-        k_e3<R, EXACT><<<g, b, 0, s>>>(F, G, KCH3);
+        const int m = G.march > 0 ? G.march : KCH3;
+        dim3 b(32, 4, 1), g((L.nx + 31) / 32, (L.ny + 3) / 4, (L.nz + m - 1) / m);
+        k_e3<R, EXACT><<<g, b, 0, s>>>(F, G, m);
     } else if (L.dims == 2) {
-        dim3 b(128, 1, 1), g((L.nx + 127) / 128, (L.ny + JCH2 - 1) / JCH2, 1);
-        k_e2<R, EXACT><<<g, b, 0, s>>>(F, G, JCH2);
+        const int m = G.march > 0 ? G.march : JCH2;
+        dim3 b(128, 1, 1), g((L.nx + 127) / 128, (L.ny + m - 1) / m, 1);
+        k_e2<R, EXACT><<<g, b, 0, s>>>(F, G, m);
     } else {
         k_e1<R, EXACT><<<(L.nx + 127) / 128, 128, 0, s>>>(F, G);
     }

@@ -252,6 +252,13 @@ class TMxll:
         self._chk(lib().omx_run(self._ctx, int(tt0), int(nsteps), int(n_skip_steps), int(t_det_print),
                                 1 if use_graph else 0))
 
+    def autotune(self, reps=20):
+        """Pick this grid's kernel launch shape by timing the candidates on the initial zero
+        fields (before the first step); returns the chosen shape."""
+        choice = C.c_int()
+        self._chk(lib().omx_autotune(self._ctx, int(reps), C.byref(choice)))
+        return choice.value
+
     # -- field access ----------------------------------------------------------------------------
     def field_bounds(self, field):
         lo = (C.c_int * 3)()

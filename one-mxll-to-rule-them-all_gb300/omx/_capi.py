@@ -103,6 +103,7 @@ SIGNATURES = {
     "omx_detectors_record": (_I, [_VP, _D]),
     "omx_detectors_drain": (_I, [_VP, _PD, _PD, _I, _PI]),
     "omx_run": (_I, [_VP, _I, _I, _I, _I, _I]),
+    "omx_autotune": (_I, [_VP, _I, _PI]),
     "omx_field_bounds": (_I, [_VP, _I, _PI, _PI]),
     "omx_read_field": (_I, [_VP, _I, _PD]),
     "omx_write_field": (_I, [_VP, _I, _PD]),
