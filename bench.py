@@ -43,7 +43,8 @@ def parse():
     p.add_argument("--steps", type=int, default=2000)
     p.add_argument("--warmup", type=int, default=20)
     p.add_argument("--impl", default="omx", choices=["omx", "reference"])
-    p.add_argument("--config", default="cfg2", choices=["cfg1", "cfg2", "cfg3"])
+    p.add_argument("--config", default="cfg2", choices=["cfg1", "cfg2", "cfg3", "cfg5"])
+    p.add_argument("--instances", type=int, default=64, help="cfg5: number of grids in the batched sweep")
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--skip-plain", action="store_true")
     p.add_argument("--error-steps", type=int, default=None,
@@ -270,7 +271,13 @@ def cpu_run(deck, seconds, max_steps=None):
 def reference_arm(args, dist):
     if dist.rank != 0:
         return
-    deck, desc = make_deck(args.config)
+    if args.config == "cfg5":
+        # the sweep's grids are independent: the sample is its smallest grid
+        dks, sides = cfg5_decks(args.instances)
+        k = min(range(len(dks)), key=lambda q: sides[q])
+        deck, desc = dks[k], "cfg5 sample: the sweep's smallest grid (side %d) of %d" % (sides[k], len(dks))
+    else:
+        deck, desc = make_deck(args.config)
     cells = cells_of(deck)
     # W warm-up steps and K timed steps of the CPU restatement, each bounded: the whole run is
     # sized to finish within a few minutes (about 2 s per timed step at most).
@@ -438,12 +445,122 @@ def gpu_arm(args, dist):
         print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------------- cfg5: sweep
+CFG5_SEED = 20261208
+
+
+def cfg5_decks(count):
+    """The batched inverse-design sweep: `count` cubic 3D grids whose side is drawn per grid,
+    uniformly in [64, 256] (the side, not the volume, is uniform), each with its own seeded
+    binary permittivity map, dipole source and Ez detector."""
+    import numpy as np
+
+    from omx import decks
+
+    rng = np.random.default_rng(CFG5_SEED)
+    sides = [int(x) for x in rng.integers(64, 257, count)]
+    return [decks.deck_cfg5_instance(n, seed=CFG5_SEED + 1 + k) for k, n in enumerate(sides)], sides
+
+
+def gpu_arm_cfg5(args, dist):
+    import numpy as np
+
+    import omx
+
+    if dist.world > 1:
+        omx.select_device(dist.local_rank % max(1, omx.device_count()))
+    dks, sides = cfg5_decks(args.instances)
+    cells = sum(cells_of(d) for d in dks)
+    K, W = args.steps, max(3, args.warmup)
+    tdp = 1
+    # ---- batched: one persistent launch per pass over all grids, the step in a CUDA graph
+    grids = [build_gpu(d, "fp32")[0] for d in dks]
+    batch = omx.Batch(grids)
+    kch = batch.autotune(reps=3)
+    batch.run(1, W, 1, tdp, use_graph=True)
+    dist.barrier()
+    clocks = ClockSampler(dist.local_rank)
+    clocks.start()
+    l0 = batch.launch_count()
+    t0 = time.perf_counter()
+    batch.run(1 + W, K, 1, tdp, use_graph=True)       # ends with a stream synchronisation
+    t_batch = time.perf_counter() - t0
+    launches = batch.launch_count() - l0
+    clk = clocks.stop()
+    t_batch = dist.max(t_batch)
+    traces_b = [g.drain_detectors()[1] for g in grids]
+    alg = sum(g.algorithmic_bytes(omx.KC_H) + g.algorithmic_bytes(omx.KC_E) for g in grids)
+    batch.kill()
+    for g in grids:
+        g.kill()
+    # ---- the same grids one at a time (each its own omx_run, CUDA graph per grid)
+    t_solo, same = 0.0, True
+    for d, tb in zip(dks, traces_b):
+        g = build_gpu(d, "fp32")[0]
+        g.run(1, W, 1, tdp, use_graph=True)
+        g.synchronize()
+        t0 = time.perf_counter()
+        g.run(1 + W, K, 1, tdp, use_graph=True)
+        g.synchronize()
+        t_solo += time.perf_counter() - t0
+        ts = g.drain_detectors()[1]
+        same = same and ts.shape == tb.shape and bool(np.array_equal(ts, tb))
+        g.kill()
+    t_solo = dist.max(t_solo)
+    value = dist.world * cells * K / t_batch / 1e9
+    solo_value = dist.world * cells * K / t_solo / 1e9
+    peak, peak_kind = peaks()
+    achieved = alg * K / t_batch / 1e9
+    cpu = None
+    if dist.rank == 0:
+        small = sorted(range(len(dks)), key=lambda k: sides[k])[:2]
+        done, el_total, cores, cc = 0, 0.0, 1, 0
+        for k in small:
+            n, el, cores = cpu_run(dks[k], seconds=args.cpu_seconds / 2)
+            done += n * cells_of(dks[k])
+            el_total += el
+        cpu = {"value": done / el_total / 1e9, "unit": "Gcell-updates/s", "cores": cores, "kind": "port",
+               "sample": "FP64 oracle on the two smallest grids of the sweep (sides %s), %.0f s" %
+                         ([sides[k] for k in small], el_total)}
+    if dist.rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "Gcell-updates/s", "n_gpus": dist.world, "steps": K,
+            "warmup": W, "ms_per_step": t_batch / K * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded decks of the configuration's shape)",
+            "config": {"workload": "cfg5: %d 3D grids, cubic, side uniform in [64, 256] per grid (seed %d), "
+                                   "8-cell CPML, binary eps 1 / 12.1 map (fill 0.4) in the central 50%%, "
+                                   "1.55 um dipole source, one Ez detector each" % (len(dks), CFG5_SEED),
+                       "cells": cells, "sides": sides, "precision": "fp32",
+                       "parallelism": f"replicas x{dist.world}" if dist.world > 1 else "single GPU",
+                       "l2": "working set %.1f GB > 126 MB L2, no flush" % (cells * 6 * 4 / 1e9),
+                       "loop": "omx_batch_run: one persistent launch per pass over all grids' tiles, the step "
+                               "captured in a CUDA graph; tile depth %d from omx_batch_autotune" % kch,
+                       "timing": "wall clock around omx_batch_run, which ends with a stream synchronisation"},
+            "one_at_a_time": {"value": solo_value, "unit": "Gcell-updates/s",
+                              "how": "the same grids, each its own omx_run (CUDA graph), run one after another",
+                              "batch_speedup": value / solo_value,
+                              "detector_traces_bit_identical": same},
+            "roofline": {"bound": "hbm", "kernel": "k_batch3 (H and bulk E passes over all grids)",
+                         "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": None, "peak_source": peak_kind,
+                         "algorithmic_bytes_per_step": alg,
+                         "note": "achieved over the whole step time (sources and detectors included)"},
+            "cpu_baseline": cpu,
+            "e2e": None,
+            "gpu_launches": launches,
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     dist = Dist()
     try:
         if args.impl == "reference":
             reference_arm(args, dist)
+        elif args.config == "cfg5":
+            gpu_arm_cfg5(args, dist)
         else:
             gpu_arm(args, dist)
     finally:

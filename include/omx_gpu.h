@@ -252,13 +252,34 @@ int omx_run(omx_ctx *ctx, int tt0, int nsteps, int n_skip_steps, int t_det_print
 
 /* Launch-shape autotuner (no counterpart in the reference, whose loops have no launch shape).
  * Times each candidate shape of this grid's field kernels `reps` times and keeps the fastest:
- * the fused FP32 TMz kernel's form (0 register prefetch, 4/5/6/8 bulk-copy ring depth) or the
+ * the fused FP32 TMz kernel's form (0 register prefetch, 4/5/6/8 bulk-copy ring depth, 14/15/16
+ * ring depth 4/5/6 filled by a dedicated copy warp) or the
  * planes / rows each thread marches in the unfused kernels.  The candidates run on the initial
  * all-zero fields, which every kernel maps to zero, so the simulation state is unchanged: call it
  * after the grid is configured and before the first step or omx_write_field (OMX_ERR_STATE
  * otherwise); configuration calls are closed afterwards, as after a first step.  *choice (may
  * be NULL) receives the chosen shape. */
 int omx_autotune(omx_ctx *ctx, int reps, int *choice);
+
+/* ---- batched multi-grid runs (no counterpart in the reference: it runs one grid per process) -
+ * A batch groups n configured 3D contexts of one precision on the current device (for example
+ * the instances of a parameter sweep).  omx_batch_run advances all of them together: each step
+ * runs ONE persistent launch for the H pass of every grid (its blocks walk a list of all grids'
+ * tiles), one launch per round of radial sources (round r: source r of every grid), the
+ * dispersive cells, ONE launch for the bulk E pass of every grid, the per-grid emitter work and
+ * one launch for the detectors of every grid; use_graph != 0 captures that step once and
+ * replays it.  Every grid computes exactly what omx_run computes for it alone (same kernels,
+ * same per-grid order).  The contexts stay owned by the caller and must outlive the batch; while
+ * omx_batch_run executes, their launches go to the batch's stream. */
+typedef struct omx_batch omx_batch;
+int omx_batch_create(omx_ctx *const *ctxs, int n, omx_batch **out);
+/* Tile depth (z planes per tile: 4, 8, 16 or 32) of the batched passes, timed `reps` times each
+ * on the initial zero fields; same preconditions as omx_autotune.  *choice may be NULL. */
+int omx_batch_autotune(omx_batch *batch, int reps, int *choice);
+int omx_batch_run(omx_batch *batch, int tt0, int nsteps, int n_skip_steps, int t_det_print,
+                  int use_graph);
+long long omx_batch_launch_count(const omx_batch *batch);   /* kernels launched by the batch */
+int omx_batch_destroy(omx_batch *batch);
 
 /* ---- field access (debug / parity) ---------------------------------------------------------- */
 /* Copies a field over the reference's bounds (e.g. 3D Ex(0:nx,1:ny+1,1:nz+1)) to/from host

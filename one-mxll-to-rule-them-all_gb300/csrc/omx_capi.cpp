@@ -180,6 +180,7 @@ struct omx_ctx {
     // run tables
     DevBuf<double> tab;
     DevBuf<int> d_step;
+    DevBuf<float> rowc;    // packed per-row y coefficients of the fused FP32 TMz kernel
     DevBuf<int> d_err;     // kernel error word (bit 0: a bulk-copy wait of the fused kernel ran out)
     int *h_err = nullptr;  // pinned host copy of it, read at every synchronisation
     // pinned staging of the per-step table, two halves used alternately (an event per half
@@ -382,6 +383,24 @@ template <class R> void upload_axis_tables(omx_ctx *c)
         tb[5].upload(cH);
         c->tl[a][0].upload(lE);
         c->tl[a][1].upload(lH);
+        if (!exact && a == 1) {
+            // packed y coefficients of the fused FP32 TMz kernel: (den_h, den_e, bH, cH) and
+            // (bE, cE, H layer, E layer) per row, the layers as int bit patterns
+            std::vector<float> rc((size_t)8 * (na + 2));
+            for (int p = 0; p < na + 2; ++p) {
+                const int lh = lH[p], le = lE[p];
+                float *o = &rc[(size_t)8 * p];
+                o[0] = (float)dh[p];
+                o[1] = (float)de[p];
+                o[2] = (float)bH[p];
+                o[3] = (float)cH[p];
+                o[4] = (float)bE[p];
+                o[5] = (float)cE[p];
+                std::memcpy(&o[6], &lh, sizeof(int));
+                std::memcpy(&o[7], &le, sizeof(int));
+            }
+            c->rowc.upload(rc);
+        }
     }
 }
 
@@ -842,32 +861,40 @@ template <class R> void do_H(omx_ctx *c)
     c->launches++;
 }
 
+SrcArgs src_args(const SourceRec &S)
+{
+    SrcArgs a;
+    a.n = S.n;
+    a.eidx = S.eidx.p;
+    a.ka = S.ka.p;
+    a.kb = S.kb.p;
+    a.comp = S.comp;
+    a.avg = S.avg;
+    a.c_src = S.c_src;
+    return a;
+}
+
+template <class R> void launch_one_source(omx_ctx *c, size_t s, StepParam amp)
+{
+    const FieldPtrs<R> F = field_ptrs<R>(c);
+    SourceRec &S = *c->sources[s];
+    if (S.kind == 0) {
+        launch_src<R>(F, src_args(S), amp, c->stream);
+    } else {
+        PlaneArgs p;
+        p.comp = S.pd.comp - 1;
+        p.axis = S.pd.plane_axis - 1;
+        p.index = S.pd.plane_index;
+        p.c_src = S.c_src;
+        launch_plane<R>(F, c->L, p, amp, c->stream);
+    }
+    c->launches++;
+}
+
 template <class R> void do_sources(omx_ctx *c, const std::vector<StepParam> &amps)
 {
     ProfScope ps(c, KC_SRC);
-    const FieldPtrs<R> F = field_ptrs<R>(c);
-    for (size_t s = 0; s < c->sources.size(); ++s) {
-        SourceRec &S = *c->sources[s];
-        if (S.kind == 0) {
-            SrcArgs a;
-            a.n = S.n;
-            a.eidx = S.eidx.p;
-            a.ka = S.ka.p;
-            a.kb = S.kb.p;
-            a.comp = S.comp;
-            a.avg = S.avg;
-            a.c_src = S.c_src;
-            launch_src<R>(F, a, amps[s], c->stream);
-        } else {
-            PlaneArgs p;
-            p.comp = S.pd.comp - 1;
-            p.axis = S.pd.plane_axis - 1;
-            p.index = S.pd.plane_index;
-            p.c_src = S.c_src;
-            launch_plane<R>(F, c->L, p, amps[s], c->stream);
-        }
-        c->launches++;
-    }
+    for (size_t s = 0; s < c->sources.size(); ++s) launch_one_source<R>(c, s, amps[s]);
 }
 
 template <class R> void do_inject(omx_ctx *c, StepParam time, StepParam t_skip);
@@ -966,6 +993,7 @@ template <> void fused_step<float>(omx_ctx *c)
     A.psi_ezx = G.psiE[0][0];
     A.psi_ezy = G.psiE[1][0];
     A.err = c->d_err.p;
+    A.rowc = reinterpret_cast<const float4 *>(c->rowc.p);
     launch_fused_tmz(A, G, c->fused_form, c->stream);
     launch_ade_post(Fin, Fout, G, c->stream);
     c->launches += 1 + (c->ade_n > 0 ? 1 : 0);
@@ -1004,7 +1032,15 @@ double source_amp(const SourceRec &S, double time)
     return j_amp * envelope * cos_t;
 }
 
-template <class R> void run_impl(omx_ctx *c, int tt0, int nsteps, int n_skip, int t_det_print, int use_graph)
+// Per-step table of a device-loop run (step-major: time, t_skip, move, slot, amps...), copied
+// from pinned staging to the device, and the step counter reset; the stepping state advances as
+// the reference's loop does (mxim_mxll.f90:92-104).  Sets run_step; the caller clears it.
+struct RunPlan {
+    int W = 0;
+    bool has_det = false;
+    int nrec = 0;
+};
+RunPlan stage_run(omx_ctx *c, int tt0, int nsteps, int n_skip, int t_det_print)
 {
     prepare(c);
     const int nsrc = (int)c->sources.size();
@@ -1056,10 +1092,26 @@ template <class R> void run_impl(omx_ctx *c, int tt0, int nsteps, int n_skip, in
     // the first kernel of every step advances the counter, so it starts one below step 0
     ck(cudaMemsetAsync(c->d_step.p, 0xff, sizeof(int), c->stream), "step");
     c->run_step = c->d_step.p;
+    RunPlan plan;
+    plan.W = W;
+    plan.has_det = has_det;
+    plan.nrec = nrec;
+    return plan;
+}
+
+StepParam plan_param(omx_ctx *c, const RunPlan &plan, int row) { return StepParam{0.0, c->tab.p + row, c->d_step.p, plan.W}; }
+
+template <class R> void run_impl(omx_ctx *c, int tt0, int nsteps, int n_skip, int t_det_print, int use_graph)
+{
+    const RunPlan plan = stage_run(c, tt0, nsteps, n_skip, t_det_print);
     struct Reset {
         omx_ctx *c;
         ~Reset() { c->run_step = nullptr; }
     } reset{c};
+    const int W = plan.W;
+    const bool has_det = plan.has_det;
+    const int nrec = plan.nrec;
+    const int nsrc = (int)c->sources.size();
     auto P = [&](int row) { return StepParam{0.0, c->tab.p + row, c->d_step.p, W}; };
     std::vector<StepParam> amps;
     for (int q = 0; q < nsrc; ++q) amps.push_back(P(4 + q));
@@ -1140,7 +1192,7 @@ template <class R> int autotune_impl(omx_ctx *c, int reps)
 {
     const bool fused = std::is_same<R, float>::value && c->fused_ok;
     std::vector<int> cand;
-    if (fused) cand = {0, 4, 5, 6, 8};
+    if (fused) cand = {0, 4, 5, 6, 8, 14, 15, 16};
     else if (c->dims == 3) cand = {4, 8, 16, 32};
     else if (c->dims == 2) cand = {8, 16, 32, 64};
     else return 0;
@@ -1855,6 +1907,348 @@ int omx_autotune(omx_ctx *c, int reps, int *choice)
     sync_checked(c, "autotune");
     if (choice) *choice = pick;
     OMX_API_END(c)
+}
+
+}  // extern "C"
+
+// ---- batched multi-grid runs ------------------------------------------------------------------
+struct omx_batch {
+    std::vector<omx_ctx *> ctx;
+    bool fp32 = false;
+    cudaStream_t stream = nullptr;
+    int kch = 0;            // z planes per tile of the batched passes (0 = the default)
+    int blocks = 0;         // persistent grid of the batched passes
+    long long launches = 0;
+    DevBuf<unsigned char> dgrid, dsrc, ddet;
+    cudaEvent_t done = nullptr;   // recorded after a batched call; member streams wait on it
+};
+
+namespace {
+
+constexpr int BATCH_DEFAULT_KCH = 16;
+
+// Device tables of one batched run: the grids' tile list, the radial sources in rounds (round r
+// holds source r of every grid, so one grid's sources keep their order) and the detectors.
+template <class R> struct BatchTables {
+    const BatchGrid<R> *grids = nullptr;
+    long long tiles = 0;
+    std::vector<const BatchSrc<R> *> src;
+    std::vector<int> nsrc;
+    std::vector<long long> src_pts;
+    std::vector<std::vector<std::pair<int, int>>> planes;   // (grid, source) launched on their own
+    const BatchDet<R> *dets = nullptr;
+    int ndet = 0;
+    long long det_pts = 0;
+};
+
+template <class T> size_t pad16(size_t n) { return (n * sizeof(T) + 15) / 16 * 16; }
+
+template <class R>
+BatchTables<R> batch_tables(omx_batch *b, const std::vector<RunPlan> *plans, int kch)
+{
+    const int n = (int)b->ctx.size();
+    BatchTables<R> T;
+    std::vector<BatchGrid<R>> grids(n);
+    long long t0 = 0;
+    size_t rounds = 0;
+    for (int i = 0; i < n; ++i) {
+        omx_ctx *c = b->ctx[i];
+        std::memset(&grids[i], 0, sizeof(BatchGrid<R>));
+        grids[i].G = grid_args<R>(c);
+        grids[i].F = field_ptrs<R>(c);
+        grids[i].tx = (c->L.nx + 31) / 32;
+        grids[i].ty = (c->L.ny + 3) / 4;
+        grids[i].tile0 = t0;
+        t0 += (long long)grids[i].tx * grids[i].ty * ((c->L.nz + kch - 1) / kch);
+        rounds = std::max(rounds, c->sources.size());
+    }
+    T.tiles = t0;
+    std::vector<std::vector<BatchSrc<R>>> rs(rounds);
+    T.planes.resize(rounds);
+    std::vector<BatchDet<R>> dets;
+    if (plans) {
+        for (int i = 0; i < n; ++i) {
+            omx_ctx *c = b->ctx[i];
+            const RunPlan &P = (*plans)[i];
+            for (size_t q = 0; q < c->sources.size(); ++q) {
+                const SourceRec &S = *c->sources[q];
+                if (S.kind != 0) {
+                    T.planes[q].push_back({i, (int)q});
+                    continue;
+                }
+                BatchSrc<R> e;
+                std::memset(&e, 0, sizeof(e));
+                e.F = field_ptrs<R>(c);
+                e.S = src_args(S);
+                e.amp = plan_param(c, P, 4 + (int)q);
+                rs[q].push_back(e);
+            }
+            if (P.has_det) {
+                BatchDet<R> e;
+                std::memset(&e, 0, sizeof(e));
+                e.F = field_ptrs<R>(c);
+                e.D = det_args(c);
+                e.slot = plan_param(c, P, 3);
+                e.time = plan_param(c, P, 0);
+                dets.push_back(e);
+            }
+        }
+    }
+    // points: a source entry covers its S.n points, a detector entry max(n, 1) (the first thread
+    // also writes the record time)
+    for (auto &r : rs) {
+        long long p = 0;
+        for (auto &e : r) {
+            e.p0 = p;
+            p += e.S.n;
+        }
+        T.src_pts.push_back(p);
+        T.nsrc.push_back((int)r.size());
+    }
+    long long dp = 0;
+    for (auto &e : dets) {
+        e.p0 = dp;
+        dp += std::max(e.D.n, 1);
+    }
+    T.det_pts = dp;
+    T.ndet = (int)dets.size();
+    // one upload per table
+    size_t gbytes = pad16<BatchGrid<R>>(n);
+    b->dgrid.alloc(gbytes, false);
+    ck(cudaMemcpyAsync(b->dgrid.p, grids.data(), sizeof(BatchGrid<R>) * n, cudaMemcpyHostToDevice, b->stream), "batch");
+    T.grids = reinterpret_cast<const BatchGrid<R> *>(b->dgrid.p);
+    size_t sbytes = 0;
+    std::vector<size_t> soff;
+    for (auto &r : rs) {
+        soff.push_back(sbytes);
+        sbytes += pad16<BatchSrc<R>>(r.size());
+    }
+    if (sbytes) {
+        b->dsrc.alloc(sbytes, false);
+        for (size_t q = 0; q < rs.size(); ++q)
+            if (!rs[q].empty())
+                ck(cudaMemcpyAsync(b->dsrc.p + soff[q], rs[q].data(), sizeof(BatchSrc<R>) * rs[q].size(),
+                                   cudaMemcpyHostToDevice, b->stream), "batch");
+    }
+    for (size_t q = 0; q < rs.size(); ++q)
+        T.src.push_back(rs[q].empty() ? nullptr : reinterpret_cast<const BatchSrc<R> *>(b->dsrc.p + soff[q]));
+    if (!dets.empty()) {
+        b->ddet.alloc(pad16<BatchDet<R>>(dets.size()), false);
+        ck(cudaMemcpyAsync(b->ddet.p, dets.data(), sizeof(BatchDet<R>) * dets.size(), cudaMemcpyHostToDevice,
+                           b->stream), "batch");
+        T.dets = reinterpret_cast<const BatchDet<R> *>(b->ddet.p);
+    }
+    // the host vectors die here: wait for the copies that read them
+    ck(cudaStreamSynchronize(b->stream), "batch");
+    return T;
+}
+
+// Route every member's launches to the batch stream for the duration of a batched call (their
+// own streams are drained first), and restore streams and run state afterwards; work a member
+// stream receives later waits for the batched work (an event, no host synchronisation).
+struct BatchStreams {
+    omx_batch *b;
+    std::vector<cudaStream_t> saved;
+    explicit BatchStreams(omx_batch *bb) : b(bb)
+    {
+        for (auto *c : b->ctx) ck(cudaStreamSynchronize(c->stream), "sync");
+        for (auto *c : b->ctx) {
+            saved.push_back(c->stream);
+            c->stream = b->stream;
+        }
+    }
+    ~BatchStreams()
+    {
+        const bool ev = b->done && cudaEventRecord(b->done, b->stream) == cudaSuccess;
+        for (size_t i = 0; i < saved.size(); ++i) {
+            b->ctx[i]->stream = saved[i];
+            b->ctx[i]->run_step = nullptr;
+            if (ev) cudaStreamWaitEvent(saved[i], b->done, 0);
+            else cudaStreamSynchronize(b->stream);
+        }
+    }
+};
+
+// One batched step: H of every grid in one launch, the sources, the dispersive cells and the
+// bulk E of every grid in one launch, the per-grid emitter work, the detectors in one launch.
+template <class R> long long batch_step(omx_batch *b, const BatchTables<R> &T, const std::vector<RunPlan> &plans,
+                                        int kch)
+{
+    const int n = (int)b->ctx.size();
+    long long k = 0;
+    launch_batch3<R>(0, T.grids, n, T.tiles, kch, b->blocks, b->stream);
+    ++k;
+    for (size_t r = 0; r < T.src.size(); ++r) {
+        if (T.nsrc[r] > 0) {
+            launch_src_batch<R>(T.src[r], T.nsrc[r], T.src_pts[r], b->stream);
+            ++k;
+        }
+        for (auto &gp : T.planes[r]) {
+            omx_ctx *c = b->ctx[gp.first];
+            launch_one_source<R>(c, (size_t)gp.second, plan_param(c, plans[gp.first], 4 + gp.second));
+            ++k;
+        }
+    }
+    for (auto *c : b->ctx)
+        if (c->ade_n > 0) {
+            launch_ade<R>(field_ptrs<R>(c), grid_args<R>(c), b->stream);
+            ++k;
+        }
+    launch_batch3<R>(1, T.grids, n, T.tiles, kch, b->blocks, b->stream);
+    ++k;
+    for (int i = 0; i < n; ++i) {
+        omx_ctx *c = b->ctx[i];
+        const long long before = c->launches;
+        do_inject<R>(c, plan_param(c, plans[i], 0), plan_param(c, plans[i], 1));
+        for (auto &g : c->groups) do_group<R>(c, *g, plan_param(c, plans[i], 2));
+        k += c->launches - before;
+    }
+    if (T.ndet > 0) {
+        launch_sample_batch<R>(T.dets, T.ndet, T.det_pts, b->stream);
+        ++k;
+    }
+    return k;
+}
+
+template <class R> void batch_run_impl(omx_batch *b, int tt0, int nsteps, int n_skip, int t_det_print, int use_graph)
+{
+    BatchStreams streams(b);
+    std::vector<RunPlan> plans;
+    for (auto *c : b->ctx) plans.push_back(stage_run(c, tt0, nsteps, n_skip, t_det_print));
+    const int kch = b->kch > 0 ? b->kch : BATCH_DEFAULT_KCH;
+    if (b->blocks == 0) b->blocks = batch3_blocks<R>();
+    const BatchTables<R> T = batch_tables<R>(b, &plans, kch);
+    if (use_graph) {
+        cudaGraph_t graph;
+        ck(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "capture");
+        const long long per = batch_step<R>(b, T, plans, kch);
+        ck(cudaStreamEndCapture(b->stream, &graph), "end capture");
+        cudaGraphExec_t exec = nullptr;
+        const cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        ck(e, "instantiate");
+        struct Destroy {
+            cudaGraphExec_t x;
+            ~Destroy() { cudaGraphExecDestroy(x); }
+        } destroy{exec};
+        for (int s = 0; s < nsteps; ++s) ck(cudaGraphLaunch(exec, b->stream), "graph launch");
+        b->launches += per * nsteps;   // (an executable graph destroyed in flight is freed on completion)
+    } else {
+        for (int s = 0; s < nsteps; ++s) b->launches += batch_step<R>(b, T, plans, kch);
+    }
+    ck(cudaPeekAtLastError(), "launch");
+    for (size_t i = 0; i < b->ctx.size(); ++i) b->ctx[i]->rec_count += plans[i].nrec;
+}
+
+// Tile depth of the batched passes, timed on the zero initial fields (which every pass maps to
+// zero, so nothing of the simulation state changes).
+template <class R> int batch_autotune_impl(omx_batch *b, int reps)
+{
+    BatchStreams streams(b);
+    if (b->blocks == 0) b->blocks = batch3_blocks<R>();
+    const int n = (int)b->ctx.size();
+    cudaEvent_t e0, e1;
+    ck(cudaEventCreate(&e0), "event");
+    ck(cudaEventCreate(&e1), "event");
+    float best = 0.f;
+    int pick = BATCH_DEFAULT_KCH;
+    const int cand[4] = {4, 8, 16, 32};
+    for (int k = 0; k < 4; ++k) {
+        const BatchTables<R> T = batch_tables<R>(b, nullptr, cand[k]);
+        auto once = [&]() {
+            launch_batch3<R>(0, T.grids, n, T.tiles, cand[k], b->blocks, b->stream);
+            for (auto *c : b->ctx)
+                if (c->ade_n > 0) launch_ade<R>(field_ptrs<R>(c), grid_args<R>(c), b->stream);
+            launch_batch3<R>(1, T.grids, n, T.tiles, cand[k], b->blocks, b->stream);
+        };
+        once();
+        cudaEventRecord(e0, b->stream);
+        for (int r = 0; r < reps; ++r) once();
+        cudaEventRecord(e1, b->stream);
+        const cudaError_t err = cudaEventSynchronize(e1);
+        float ms = 0.f;
+        if (err == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+        if (err != cudaSuccess) {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            ck(err, "batch autotune");
+        }
+        if (k == 0 || ms < best) {
+            best = ms;
+            pick = cand[k];
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    b->kch = pick;
+    return pick;
+}
+
+}  // namespace
+
+extern "C" {
+
+int omx_batch_create(omx_ctx *const *ctxs, int n, omx_batch **out)
+{
+    OMX_API_BEGIN
+    req(ctxs && out && n >= 1, "bad argument");
+    *out = nullptr;
+    std::unique_ptr<omx_batch> b(new omx_batch);
+    for (int i = 0; i < n; ++i) {
+        omx_ctx *c = ctxs[i];
+        req(c != nullptr, "null context in the batch");
+        req(c->dims == 3, "batched runs take 3D grids");
+        req(c->fp32 == ctxs[0]->fp32, "the grids of a batch share one precision");
+        req(!c->prof, "profiling is on for a member of the batch");
+        for (int k = 0; k < i; ++k) req(ctxs[k] != c, "a context appears twice in the batch");
+        b->ctx.push_back(c);
+    }
+    b->fp32 = ctxs[0]->fp32;
+    ck(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "stream");
+    ck(cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming), "event");
+    *out = b.release();
+    OMX_API_END(nullptr)
+}
+
+int omx_batch_autotune(omx_batch *b, int reps, int *choice)
+{
+    OMX_API_BEGIN
+    req(b && reps >= 1, "bad argument");
+    for (auto *c : b->ctx)
+        req(!c->started && !c->fields_written,
+            "omx_batch_autotune times the passes on the initial zero fields: call it after the grids are "
+            "configured and before their first step or field write", OMX_ERR_STATE);
+    for (auto *c : b->ctx) {
+        prepare(c);
+        c->epoch++;
+    }
+    const int pick = b->fp32 ? batch_autotune_impl<float>(b, reps) : batch_autotune_impl<double>(b, reps);
+    if (choice) *choice = pick;
+    OMX_API_END(nullptr)
+}
+
+int omx_batch_run(omx_batch *b, int tt0, int nsteps, int n_skip_steps, int t_det_print, int use_graph)
+{
+    OMX_API_BEGIN
+    req(b && nsteps >= 0 && n_skip_steps >= 1 && tt0 >= 1, "bad argument");
+    for (auto *c : b->ctx) req(!c->prof, "profiling is on for a member of the batch");
+    if (nsteps == 0) return OMX_OK;
+    if (b->fp32) batch_run_impl<float>(b, tt0, nsteps, n_skip_steps, t_det_print, use_graph);
+    else batch_run_impl<double>(b, tt0, nsteps, n_skip_steps, t_det_print, use_graph);
+    OMX_API_END(nullptr)
+}
+
+long long omx_batch_launch_count(const omx_batch *b) { return b ? b->launches : 0; }
+
+int omx_batch_destroy(omx_batch *b)
+{
+    if (!b) return OMX_OK;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->done) cudaEventDestroy(b->done);
+    cudaStream_t s = b->stream;
+    delete b;
+    if (s) cudaStreamDestroy(s);
+    return OMX_OK;
 }
 
 int omx_field_bounds(const omx_ctx *c, int field, int lo[3], int hi[3])

@@ -493,6 +493,239 @@ drain:
     }
 }
 
+// ---------------------------------------------------------------------------------------------
+// Warp-specialised bulk-copy variant.  Four consumer warps compute; a fifth warp issues the
+// copies.  Every ring slot has a "full" barrier (one arrival plus the copy bytes) and an "empty"
+// barrier (one arrival per consumer warp), so the consumer warps never wait for one another and
+// the copy warp refills a slot as soon as the last consumer has read it: no block-wide barrier
+// per row.  The copy warp follows the block's segments incrementally (no 64-bit division per
+// item), and the y coefficients of a row come from the packed row table (two float4 loads).
+constexpr int FZ_CONSUMERS = 4;
+
+template <bool XCPML, int D>
+__global__ void __launch_bounds__(160, 5) k_fused_tmz_ws(Fused2Args A, GridArgs<float> G, int nstrip)
+{
+    extern __shared__ __align__(128) unsigned char fz_smem[];
+    FzStage *stage = reinterpret_cast<FzStage *>(fz_smem);
+    uint64_t *full = reinterpret_cast<uint64_t *>(fz_smem + D * sizeof(FzStage));
+    uint64_t *empty = full + D;
+    const Lay &L = G.L;
+    const long long ny = L.ny;
+    const long long total = (long long)nstrip * ny;
+    const long long rb0 = total * blockIdx.x / gridDim.x;
+    const long long rb1 = total * (blockIdx.x + 1) / gridDim.x;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) {
+        if (G.step_inc && blockIdx.x == 0) *G.step_inc += 1;          // device-loop step counter
+        for (int s = 0; s < D; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], FZ_CONSUMERS);
+        }
+        mbar_fence_init();
+    }
+    __syncthreads();
+    if (rb0 >= rb1) return;
+
+    if (warp == FZ_CONSUMERS) {
+        // ---- copy warp: lane 0 issues every item of the block's range in order
+        if (lane != 0) return;
+        FzSeg S = fz_segment(rb0, rb1, ny);
+        long long r = rb0;
+        int k = 0, q = 0;
+        bool ok = true;
+        for (;;) {
+            const int slot = q % D;
+            // item q reuses the slot of item q-D: wait until every consumer warp released it
+            if (q >= D && !mbar_wait_bounded(&empty[slot], (uint32_t)(((q / D) - 1) & 1), FZ_WAIT_CYCLES)) {
+                ok = false;
+                break;
+            }
+            fz_issue(A, G, S, k, &stage[slot], &full[slot]);
+            ++q;
+            if (++k == S.j1 - S.j0 + 3) {
+                k = 0;
+                r += S.j1 - S.j0 + 1;
+                if (r >= rb1) break;
+                // a segment ends at its strip's last row or at the range end: the next one
+                // starts at row 1 of the next strip
+                S.strip += 1;
+                S.j0 = 1;
+                S.j1 = (int)min(ny, rb1 - r);
+            }
+        }
+        if (!ok) {
+            // a consumer stopped: flag it, let the copies in flight land, leave
+            atomicOr(A.err, 1);
+            for (int p = max(0, q - D); p < q; ++p)
+                mbar_wait_bounded(&full[p % D], (uint32_t)((p / D) & 1), FZ_WAIT_CYCLES);
+        }
+        return;
+    }
+
+    // ---- consumer warps: the arithmetic of k_fused_tmz_tma, rows from the ring
+    const int tl = threadIdx.x;
+    const float dt_mu0 = G.dt_mu0, dt_eps0 = G.dt_eps0;
+    const long long px = L.px;
+    int m = 0;                                // index of the current segment's item 0
+    for (long long r = rb0; r < rb1;) {
+        const FzSeg S = fz_segment(r, rb1, ny);
+        const int ib0 = 1 + FZ_W * S.strip;
+        const int ib = ib0 + 4 * tl;
+        const bool active = ib <= L.nx;
+        const int ibc = active ? ib : 1;      // lanes past nx only join the shuffles
+        float dhx[4], dex[4], bhx[4], chx[4], bex[4], cex[4];
+        int lhx[4], lex[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int i = XCPML ? min(ibc + q, L.nx) : 1;
+            dhx[q] = G.den_h[0][i];
+            dex[q] = G.den_e[0][i];
+            lhx[q] = XCPML ? G.lH[0][i] : -1;
+            lex[q] = XCPML ? G.lE[0][i] : -1;
+            bhx[q] = XCPML ? G.bH[0][i] : 0.f;
+            chx[q] = XCPML ? G.cH[0][i] : 0.f;
+            bex[q] = XCPML ? G.bE[0][i] : 0.f;
+            cex[q] = XCPML ? G.cE[0][i] : 0.f;
+        }
+        const bool left_ghost = (ibc == 1) && !G.per[0];
+        const int il = (ibc == 1) ? L.nx : ibc - 1;
+        const float dhx_l = G.den_h[0][XCPML ? il : 1];
+        const int lhx_l = XCPML ? G.lH[0][il] : -1;
+        const float bhx_l = XCPML ? G.bH[0][il] : 0.f, chx_l = XCPML ? G.cH[0][il] : 0.f;
+        const bool wrap_r = ibc + 4 > L.nx && G.per[0];
+        const bool bb_i = G.bbV > 0 && (ibc + 3 >= G.bb0[0] && ibc <= G.bb1[0]);
+        const long long col = L.off + ibc;
+        const int n = S.j1 - S.j0 + 1;
+        bool fail = false;
+
+        // step 0: Hx_new(j0-1) from items 0 and 1
+        float hxp[4] = {0.f, 0.f, 0.f, 0.f};
+        {
+            const int s0 = m % D, s1 = (m + 1) % D;
+            fail |= !mbar_wait_bounded(&full[s0], (uint32_t)((m / D) & 1), FZ_WAIT_CYCLES);
+            fail |= !mbar_wait_bounded(&full[s1], (uint32_t)(((m + 1) / D) & 1), FZ_WAIT_CYCLES);
+            fail = __any_sync(0xffffffffu, fail);
+            if (fail) {
+                if (lane == 0) atomicOr(A.err, 1);
+                return;
+            }
+            const int jm = S.j0 - 1;
+            if (!(jm == 0 && !G.per[1])) {
+                const int jr = (jm == 0) ? L.ny : jm;
+                const float4 c0 = A.rowc[2 * jr], c1 = A.rowc[2 * jr + 1];
+                const float4 e0 = *reinterpret_cast<const float4 *>(&stage[s0].ez[4 + 4 * tl]);
+                const float4 e1 = *reinterpret_cast<const float4 *>(&stage[s1].ez[4 + 4 * tl]);
+                const float4 h0 = *reinterpret_cast<const float4 *>(&stage[s0].hx[4 * tl]);
+                const int ly = __float_as_int(c1.z);
+                const long long pb = (ibc - 1) + (long long)L.nx * ly;
+                hxp[0] = fz_hx(h0.x, e0.x, e1.x, c0.x, dt_mu0, ly, c0.z, c0.w, A.psi_hxy_in, nullptr, pb + 0);
+                hxp[1] = fz_hx(h0.y, e0.y, e1.y, c0.x, dt_mu0, ly, c0.z, c0.w, A.psi_hxy_in, nullptr, pb + 1);
+                hxp[2] = fz_hx(h0.z, e0.z, e1.z, c0.x, dt_mu0, ly, c0.z, c0.w, A.psi_hxy_in, nullptr, pb + 2);
+                hxp[3] = fz_hx(h0.w, e0.w, e1.w, c0.x, dt_mu0, ly, c0.z, c0.w, A.psi_hxy_in, nullptr, pb + 3);
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&empty[s0]);                // item 0 is done
+        }
+
+        // steps 1..n: row j = j0-1+k from items k (row j) and k+1 (Ez of row j+1)
+        for (int k = 1; k <= n; ++k) {
+            const int j = S.j0 - 1 + k;
+            const int sc = (m + k) % D, sn = (m + k + 1) % D;
+            fail = !mbar_wait_bounded(&full[sn], (uint32_t)(((m + k + 1) / D) & 1), FZ_WAIT_CYCLES);
+            fail = __any_sync(0xffffffffu, fail);
+            if (fail) {
+                if (lane == 0) atomicOr(A.err, 1);
+                return;
+            }
+            const FzStage &C = stage[sc];
+            const float4 ez_c = *reinterpret_cast<const float4 *>(&C.ez[4 + 4 * tl]);
+            const float4 ez_n = *reinterpret_cast<const float4 *>(&stage[sn].ez[4 + 4 * tl]);
+            const float4 hx_o = *reinterpret_cast<const float4 *>(&C.hx[4 * tl]);
+            const float4 hy_o = *reinterpret_cast<const float4 *>(&C.hy[4 + 4 * tl]);
+            const long long row = col + px * j;
+            float ez_r = __shfl_down_sync(0xffffffffu, ez_c.x, 1);
+            if (lane == 31 || ibc + 4 > L.nx) ez_r = wrap_r ? A.ez_in[L.off + 1 + px * j] : C.ez[8 + 4 * tl];
+            const float4 c0 = A.rowc[2 * j], c1 = A.rowc[2 * j + 1];
+            const float dhy = c0.x, dey = c0.y, bhy = c0.z, chy = c0.w, bey = c1.x, cey = c1.y;
+            const int ly = __float_as_int(c1.z), lye = __float_as_int(c1.w);
+            const float ez[5] = {ez_c.x, ez_c.y, ez_c.z, ez_c.w, ez_r};
+            const float ezn[4] = {ez_n.x, ez_n.y, ez_n.z, ez_n.w};
+            const float hxo[4] = {hx_o.x, hx_o.y, hx_o.z, hx_o.w};
+            const float hyo[4] = {hy_o.x, hy_o.y, hy_o.z, hy_o.w};
+            float hx[4], hy[4];
+            const long long pby = (ibc - 1) + (long long)L.nx * ly;
+            const long long pbx = (long long)G.L2 * (j - 1);
+            float *const psx_out = active ? A.psi_hxy_out : nullptr;
+            float *const psy_out = active ? A.psi_hyx_out : nullptr;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                hx[q] = fz_hx(hxo[q], ez[q], ezn[q], dhy, dt_mu0, ly, bhy, chy, A.psi_hxy_in, psx_out, pby + q);
+                hy[q] = fz_hy(hyo[q], ez[q], ez[q + 1], dhx[q], dt_mu0, lhx[q], bhx[q], chx[q], A.psi_hyx_in,
+                              psy_out, lhx[q] + pbx);
+            }
+            float hy_l = __shfl_up_sync(0xffffffffu, hy[3], 1);
+            if (active && (lane == 0 || ib == 1)) {
+                if (left_ghost) {
+                    hy_l = 0.f;
+                } else if (ib == 1) {
+                    const long long rl = L.off + il + px * j;
+                    hy_l = fz_hy(A.hy_in[rl], A.ez_in[rl], ez[0], dhx_l, dt_mu0, lhx_l, bhx_l, chx_l, A.psi_hyx_in,
+                                 nullptr, lhx_l + pbx);
+                } else {
+                    hy_l = fz_hy(C.hy[3 + 4 * tl], C.ez[3 + 4 * tl], ez[0], dhx_l, dt_mu0, lhx_l, bhx_l, chx_l,
+                                 A.psi_hyx_in, nullptr, lhx_l + pbx);
+                }
+            }
+            __syncwarp();
+            if (lane == 0) {
+                mbar_arrive(&empty[sc]);                           // row j is read
+                if (k == n) mbar_arrive(&empty[sn]);               // and the Ez-only item after it
+            }
+            if (active) {
+                *reinterpret_cast<float4 *>(A.hx_out + row) = make_float4(hx[0], hx[1], hx[2], hx[3]);
+                *reinterpret_cast<float4 *>(A.hy_out + row) = make_float4(hy[0], hy[1], hy[2], hy[3]);
+                if (G.per[0] && ib + 3 == L.nx) A.hy_out[row + 3 - L.nx] = hy[3];            // Hy(0,j) = Hy(nx,j)
+                if (G.per[1] && j == L.ny)
+                    *reinterpret_cast<float4 *>(A.hx_out + row - px * L.ny) = make_float4(hx[0], hx[1], hx[2], hx[3]);
+                const bool bb = bb_i && j >= G.bb0[1] && j <= G.bb1[1];
+                float eo[4];
+                const float hyl[4] = {hy_l, hy[0], hy[1], hy[2]};
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const float dyh = hy[q] - hyl[q];
+                    const float dxh = hxp[q] - hx[q];
+                    const float rr = dyh * dex[q] + dxh * dey;
+                    float e = ez[q];
+                    if (bb && ibc + q >= G.bb0[0] && ibc + q <= G.bb1[0]) {
+                        const long long b = (ibc + q - G.bb0[0]) + (long long)G.bbd[0] * (j - G.bb0[1]);
+                        e = plain_update<float>(e, rr, G.mat[2][b], G);
+                    } else {
+                        e = e + dt_eps0 * rr;
+                    }
+                    if (XCPML && lex[q] >= 0) {
+                        const long long p = lex[q] + pbx;
+                        const float v = bex[q] * A.psi_ezx[p] + cex[q] * dyh;
+                        A.psi_ezx[p] = v;
+                        e = e + dt_eps0 * v;
+                    }
+                    if (lye >= 0) {
+                        const long long p = (ibc + q - 1) + (long long)L.nx * lye;
+                        const float v = bey * A.psi_ezy[p] + cey * dxh;
+                        A.psi_ezy[p] = v;
+                        e = e + dt_eps0 * v;
+                    }
+                    eo[q] = e;
+                }
+                *reinterpret_cast<float4 *>(A.ez_out + row) = make_float4(eo[0], eo[1], eo[2], eo[3]);
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) hxp[q] = hx[q];
+        }
+        m += n + 2;
+        r += n;
+    }
+}
+
 // Dispersive cells after the fused pass: E_out = ADE(E_in, curl H_out) (no CPML term: the host
 // keeps dispersive cells out of the CPML slabs on this path).
 __global__ void k_ade_post(FieldPtrs<float> Fin, FieldPtrs<float> Fout, GridArgs<float> G)

@@ -161,10 +161,41 @@ struct Fused2Args {
     float *psi_hyx_out, *psi_hxy_out;
     float *psi_ezx, *psi_ezy;               // E psi, updated in place
     int *err;                               // device error word (bit 0: a bulk-copy wait ran out)
+    // per-row y coefficients, two float4 per row j = 0..ny+1: (den_h, den_e, bH, cH) and
+    // (bE, cE, H psi layer, E psi layer) with the layers stored as int bit patterns
+    const float4 *rowc;
 };
-// form: 0 register prefetch, 4/5/6/8 bulk-copy ring depth, < 0 the default
+// form: 0 register prefetch, 4/5/6/8 bulk-copy ring depth, 14/15/16 ring depth 4/5/6 with a
+// dedicated copy warp; < 0 the default
 void launch_fused_tmz(const Fused2Args &A, const GridArgs<float> &G, int form, void *stream);
 void launch_ade_post(const FieldPtrs<float> &Fin, const FieldPtrs<float> &Fout, const GridArgs<float> &G, void *stream);
 void launch_flush(float *buf, long long n, void *stream);
+
+// ---- batched multi-grid launches (3D): one launch per pass over several grids ----------------
+template <class R> struct BatchGrid {
+    GridArgs<R> G;
+    FieldPtrs<R> F;
+    long long tile0;   // first tile of this grid in the concatenated tile list
+    int tx, ty;        // tiles along x (32 cells) and y (4 cells); along z: kch planes each
+};
+template <class R> struct BatchSrc {     // one radial source of one grid
+    FieldPtrs<R> F;
+    SrcArgs S;
+    StepParam amp;
+    long long p0;      // first point of this entry in the concatenated point list
+};
+template <class R> struct BatchDet {     // the detectors of one grid
+    FieldPtrs<R> F;
+    DetArgs D;
+    StepParam slot, time;
+    long long p0;
+};
+// pass 0: H, pass 1: bulk E (dispersive cells before it with launch_ade)
+template <class R> void launch_batch3(int pass, const BatchGrid<R> *grids, int n, long long total, int kch,
+                                      int blocks, void *stream);
+template <class R> int batch3_blocks();   // persistent grid: SMs x resident blocks
+template <class R> void launch_ade(const FieldPtrs<R> &F, const GridArgs<R> &G, void *stream);
+template <class R> void launch_src_batch(const BatchSrc<R> *e, int n, long long total, void *stream);
+template <class R> void launch_sample_batch(const BatchDet<R> *e, int n, long long total, void *stream);
 
 }  // namespace omx

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include "omx_stencil.cuh"
 #include "omx_sparse.cuh"
+#include "omx_batch.cuh"
 
 namespace omx {
 
@@ -14,6 +15,27 @@ template <> void launch_h<double>(const FieldPtrs<double> &F, const GridArgs<dou
 template <> void launch_e<double>(const FieldPtrs<double> &F, const GridArgs<double> &G, void *s)
 {
     launch_e_impl<double, true>(F, G, s);
+}
+
+template <> void launch_batch3<double>(int pass, const BatchGrid<double> *g, int n, long long total, int kch,
+                                      int blocks, void *s)
+{
+    launch_batch3_impl<double, true>(pass, g, n, total, kch, blocks, s);
+}
+template <> int batch3_blocks<double>() { return batch3_blocks_impl<double, true>(); }
+template <> void launch_ade<double>(const FieldPtrs<double> &F, const GridArgs<double> &G, void *s)
+{
+    if (G.ade_n > 0) k_ade<double><<<(G.ade_n + 127) / 128, 128, 0, (cudaStream_t)s>>>(F, G);
+}
+template <class R> void launch_src_batch(const BatchSrc<R> *e, int n, long long total, void *s)
+{
+    if (n <= 0 || total <= 0) return;
+    k_src_batch<R><<<(unsigned)((total + 127) / 128), 128, 0, (cudaStream_t)s>>>(e, n, total);
+}
+template <class R> void launch_sample_batch(const BatchDet<R> *e, int n, long long total, void *s)
+{
+    if (n <= 0 || total <= 0) return;
+    k_sample_batch<R><<<(unsigned)((total + 127) / 128), 128, 0, (cudaStream_t)s>>>(e, n, total);
 }
 
 template <class R> void launch_src(const FieldPtrs<R> &F, const SrcArgs &S, StepParam amp, void *s)
@@ -67,7 +89,9 @@ void launch_flush(float *buf, long long n, void *s)
     template void launch_inject<R>(const FieldPtrs<R> &, const JState &, const InjArgs &, StepParam,      \
                                    StepParam, double, void *);                                           \
     template void launch_emit<R>(const FieldPtrs<R> &, const Lay &, const EmitArgs &, StepParam, void *); \
-    template void launch_sample<R>(const FieldPtrs<R> &, const DetArgs &, StepParam, StepParam, void *);
+    template void launch_sample<R>(const FieldPtrs<R> &, const DetArgs &, StepParam, StepParam, void *); \
+    template void launch_src_batch<R>(const BatchSrc<R> *, int, long long, void *);                      \
+    template void launch_sample_batch<R>(const BatchDet<R> *, int, long long, void *);
 OMX_INST(float)
 OMX_INST(double)
 

@@ -6,6 +6,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include "omx_batch.cuh"
 #include "omx_fused2d.cuh"
 
 namespace omx {
@@ -19,29 +20,34 @@ template <> void launch_e<float>(const FieldPtrs<float> &F, const GridArgs<float
     launch_e_impl<float, false>(F, G, s);
 }
 
-static int persistent_blocks(const void *kernel, size_t smem)
+static int persistent_blocks(const void *kernel, size_t smem, int threads = 128)
 {
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 128, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
     return (sms > 0 ? sms : 152) * (per_sm > 0 ? per_sm : 1);
 }
 
-// Default fused-kernel form: "regs" (register prefetch of the next row) or "tmaD" (rows staged
-// by bulk copies into a D-slot shared-memory ring).  OMX_FUSED_KERNEL overrides the default;
+// Fused-kernel forms: "regs" (register prefetch of the next row), "tmaD" (rows staged by bulk
+// copies into a D-slot shared-memory ring, one block barrier per row) and "wsD" (the same ring
+// filled by a dedicated copy warp, full / empty barriers per slot).  The default is ws4, the
+// fastest on the 4096^2 TMz workload; OMX_FUSED_KERNEL overrides it for the process and
 // omx_autotune picks a form per grid.
 static int default_fused_form()
 {
     static int form = -1;
     if (form < 0) {
-        form = 5;
+        form = 14;
         if (const char *v = getenv("OMX_FUSED_KERNEL")) {
             if (!strcmp(v, "regs")) form = 0;
             else if (!strcmp(v, "tma4")) form = 4;
             else if (!strcmp(v, "tma5")) form = 5;
             else if (!strcmp(v, "tma6")) form = 6;
             else if (!strcmp(v, "tma8")) form = 8;
+            else if (!strcmp(v, "ws4")) form = 14;
+            else if (!strcmp(v, "ws5")) form = 15;
+            else if (!strcmp(v, "ws6")) form = 16;
         }
     }
     return form;
@@ -64,6 +70,21 @@ template <bool X, int D> static void launch_tma(const Fused2Args &A, const GridA
     k_fused_tmz_tma<X, D><<<grid, 128, smem, s>>>(A, G, nstrip);
 }
 
+template <bool X, int D> static void launch_ws(const Fused2Args &A, const GridArgs<float> &G, int nstrip, cudaStream_t s)
+{
+    const size_t smem = D * sizeof(FzStage) + 2 * D * sizeof(uint64_t);
+    static int nb[FZ_MAX_DEV] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int &n = nb[dev < FZ_MAX_DEV ? dev : 0];
+    if (n == 0) {
+        cudaFuncSetAttribute(k_fused_tmz_ws<X, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        n = persistent_blocks((const void *)k_fused_tmz_ws<X, D>, smem, 32 * (FZ_CONSUMERS + 1));
+    }
+    const int grid = (int)std::min<long long>(n, (long long)nstrip * G.L.ny);
+    k_fused_tmz_ws<X, D><<<grid, 32 * (FZ_CONSUMERS + 1), smem, s>>>(A, G, nstrip);
+}
+
 template <bool X> static void launch_regs(const Fused2Args &A, const GridArgs<float> &G, int nstrip, cudaStream_t s)
 {
     static int nb[FZ_MAX_DEV] = {};
@@ -83,7 +104,10 @@ static void launch_form(const Fused2Args &A, const GridArgs<float> &G, int form,
     case 4: launch_tma<X, 4>(A, G, nstrip, s); break;
     case 6: launch_tma<X, 6>(A, G, nstrip, s); break;
     case 8: launch_tma<X, 8>(A, G, nstrip, s); break;
-    default: launch_tma<X, 5>(A, G, nstrip, s); break;
+    case 16: launch_ws<X, 6>(A, G, nstrip, s); break;
+    case 5: launch_tma<X, 5>(A, G, nstrip, s); break;
+    case 15: launch_ws<X, 5>(A, G, nstrip, s); break;
+    default: launch_ws<X, 4>(A, G, nstrip, s); break;
     }
 }
 
@@ -92,6 +116,17 @@ void launch_fused_tmz(const Fused2Args &A, const GridArgs<float> &G, int form, v
     const int nstrip = (G.L.nx / 4 + 127) / 128;
     if (A.psi_ezx) launch_form<true>(A, G, form, nstrip, (cudaStream_t)s);
     else launch_form<false>(A, G, form, nstrip, (cudaStream_t)s);
+}
+
+template <> void launch_batch3<float>(int pass, const BatchGrid<float> *g, int n, long long total, int kch,
+                                     int blocks, void *s)
+{
+    launch_batch3_impl<float, false>(pass, g, n, total, kch, blocks, s);
+}
+template <> int batch3_blocks<float>() { return batch3_blocks_impl<float, false>(); }
+template <> void launch_ade<float>(const FieldPtrs<float> &F, const GridArgs<float> &G, void *s)
+{
+    if (G.ade_n > 0) k_ade<float><<<(G.ade_n + 127) / 128, 128, 0, (cudaStream_t)s>>>(F, G);
 }
 
 void launch_ade_post(const FieldPtrs<float> &Fin, const FieldPtrs<float> &Fout, const GridArgs<float> &G, void *s)

@@ -17,10 +17,8 @@ __device__ __forceinline__ double sp_get(const StepParam &p)
 // J_mat = amp*ker (amp = j_amp*envelope*cos, computed on the host with the reference's libm
 // calls); J_av = 0.5*(J_mat(p) + J_mat(p+1 along dir)); E += c_src*J_av.
 template <class R>
-__global__ void k_src(FieldPtrs<R> F, SrcArgs S, StepParam amp_p)
+__device__ __forceinline__ void src_point(const FieldPtrs<R> &F, const SrcArgs &S, const StepParam &amp_p, int q)
 {
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= S.n) return;
     const double amp = sp_get(amp_p);
     const double ja = amp * S.ka[q];
     double jav;
@@ -33,6 +31,12 @@ __global__ void k_src(FieldPtrs<R> F, SrcArgs S, StepParam amp_p)
     R *E = F.f[S.comp];
     const long long e = S.eidx[q];
     E[e] = (R)((double)E[e] + S.c_src * jav);
+}
+template <class R>
+__global__ void k_src(FieldPtrs<R> F, SrcArgs S, StepParam amp_p)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < S.n) src_point<R>(F, S, amp_p, q);
 }
 
 // Plane-wave soft source (extension): E_comp += c_src*amp on one plane of cells.
@@ -163,11 +167,11 @@ __global__ void k_scatter(JState J, ScatArgs S, StepParam move_p)
 
 // ---- detector sampling (write_fields_subs_mod.f90 stencils) -------------------------------
 template <class R>
-__global__ void k_sample(FieldPtrs<R> F, DetArgs D, StepParam slot_p, StepParam time_p)
+__device__ __forceinline__ void sample_point(const FieldPtrs<R> &F, const DetArgs &D, const StepParam &slot_p,
+                                             const StepParam &time_p, int s)
 {
     const int slot = (int)sp_get(slot_p);
     if (slot < 0) return;
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s == 0) D.times[slot] = sp_get(time_p);
     if (s >= D.n) return;
     const R *a = F.f[D.field[s]];
@@ -183,6 +187,11 @@ __global__ void k_sample(FieldPtrs<R> F, DetArgs D, StepParam slot_p, StepParam 
     }
     D.rec[(long long)slot * D.n + s] = v;
 }
+template <class R>
+__global__ void k_sample(FieldPtrs<R> F, DetArgs D, StepParam slot_p, StepParam time_p)
+{
+    sample_point<R>(F, D, slot_p, time_p, blockIdx.x * blockDim.x + threadIdx.x);
+}
 
 __global__ void k_step_advance(int *step)
 {
@@ -193,6 +202,35 @@ __global__ void k_flush(float *buf, long long n)
 {
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x)
         buf[q] = buf[q] * 0.5f + 1.0f;
+}
+
+// ---- batched forms for several grids (one launch for the sources / detectors of all grids) ----
+// entry of point q in a list of entries with ascending first points p0
+template <class E> __device__ __forceinline__ int batch_entry(const E *e, int n, long long q)
+{
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (e[mid].p0 <= q) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+template <class R> __global__ void k_src_batch(const BatchSrc<R> *__restrict__ e, int n, long long total)
+{
+    const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (q >= total) return;
+    const int k = batch_entry(e, n, q);
+    src_point<R>(e[k].F, e[k].S, e[k].amp, (int)(q - e[k].p0));
+}
+
+template <class R> __global__ void k_sample_batch(const BatchDet<R> *__restrict__ e, int n, long long total)
+{
+    const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (q >= total) return;
+    const int k = batch_entry(e, n, q);
+    sample_point<R>(e[k].F, e[k].D, e[k].slot, e[k].time, (int)(q - e[k].p0));
 }
 
 }  // namespace omx

@@ -122,15 +122,17 @@ __global__ void k_ade(FieldPtrs<R> F, GridArgs<R> G)
 }
 
 // ===================================================================================== 3D
+// One 32 x 4 x kch tile of the pass at block coordinates (bx, by, bz): the single-grid
+// kernel passes its block index, the batched kernel a tile of its work list.
 template <class R, bool EXACT>
-__global__ void __launch_bounds__(128) k_h3(FieldPtrs<R> F, GridArgs<R> G, int kch)
+__device__ __forceinline__ void h3_tile(const FieldPtrs<R> &F, const GridArgs<R> &G, int kch, int bx, int by, int bz)
 {
     const Lay L = G.L;
-    const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
-    if (G.step_inc && i == 1 && j == 1 && blockIdx.z == 0) *G.step_inc += 1;   // device-loop step counter
+    const int i = 1 + bx * blockDim.x + threadIdx.x;
+    const int j = 1 + by * blockDim.y + threadIdx.y;
+    if (G.step_inc && i == 1 && j == 1 && bz == 0) *G.step_inc += 1;   // device-loop step counter
     if (i > L.nx || j > L.ny) return;
-    const int k0 = 1 + blockIdx.z * kch;
+    const int k0 = 1 + bz * kch;
     const int k1 = min(L.nz, k0 + kch - 1);
     R *__restrict__ Ex = F.f[0];
     R *__restrict__ Ey = F.f[1];
@@ -210,13 +212,21 @@ __global__ void __launch_bounds__(128) k_h3(FieldPtrs<R> F, GridArgs<R> G, int k
 }
 
 template <class R, bool EXACT>
-__global__ void __launch_bounds__(128) k_e3(FieldPtrs<R> F, GridArgs<R> G, int kch)
+__global__ void __launch_bounds__(128) k_h3(FieldPtrs<R> F, GridArgs<R> G, int kch)
+{
+    h3_tile<R, EXACT>(F, G, kch, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+// One 32 x 4 x kch tile of the pass at block coordinates (bx, by, bz): the single-grid
+// kernel passes its block index, the batched kernel a tile of its work list.
+template <class R, bool EXACT>
+__device__ __forceinline__ void e3_tile(const FieldPtrs<R> &F, const GridArgs<R> &G, int kch, int bx, int by, int bz)
 {
     const Lay L = G.L;
-    const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+    const int i = 1 + bx * blockDim.x + threadIdx.x;
+    const int j = 1 + by * blockDim.y + threadIdx.y;
     if (i > L.nx || j > L.ny) return;
-    const int k0 = 1 + blockIdx.z * kch;
+    const int k0 = 1 + bz * kch;
     const int k1 = min(L.nz, k0 + kch - 1);
     R *__restrict__ Ex = F.f[0];
     R *__restrict__ Ey = F.f[1];
@@ -289,6 +299,12 @@ __global__ void __launch_bounds__(128) k_e3(FieldPtrs<R> F, GridArgs<R> G, int k
         hx_km = hx_c;
         hy_km = hy_c;
     }
+}
+
+template <class R, bool EXACT>
+__global__ void __launch_bounds__(128) k_e3(FieldPtrs<R> F, GridArgs<R> G, int kch)
+{
+    e3_tile<R, EXACT>(F, G, kch, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
 // ===================================================================================== 2D

@@ -329,3 +329,39 @@ def device_count():
     n = C.c_int()
     A.check(lib().omx_device_count(C.byref(n)))
     return n.value
+
+
+class Batch:
+    """Several configured 3D grids of one precision advanced together (omx_batch_*): one
+    persistent launch per pass over all grids' tiles, the step captured in a CUDA graph.  Each
+    grid computes exactly what its own `run` would."""
+
+    def __init__(self, grids):
+        self.grids = list(grids)
+        arr = (C.c_void_p * len(self.grids))(*[g._ctx.value for g in self.grids])
+        self._b = C.c_void_p()
+        A.check(lib().omx_batch_create(arr, len(self.grids), C.byref(self._b)))
+
+    def autotune(self, reps=10):
+        """Tile depth of the batched passes, timed on the zero initial fields; returns it."""
+        choice = C.c_int()
+        A.check(lib().omx_batch_autotune(self._b, int(reps), C.byref(choice)))
+        return choice.value
+
+    def run(self, tt0, nsteps, n_skip_steps=1, t_det_print=0, use_graph=True):
+        A.check(lib().omx_batch_run(self._b, int(tt0), int(nsteps), int(n_skip_steps), int(t_det_print),
+                                    1 if use_graph else 0))
+
+    def launch_count(self):
+        return int(lib().omx_batch_launch_count(self._b))
+
+    def kill(self):
+        if self._b:
+            lib().omx_batch_destroy(self._b)
+            self._b = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.kill()
+        except Exception:
+            pass

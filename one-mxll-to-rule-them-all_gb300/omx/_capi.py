@@ -104,6 +104,11 @@ SIGNATURES = {
     "omx_detectors_drain": (_I, [_VP, _PD, _PD, _I, _PI]),
     "omx_run": (_I, [_VP, _I, _I, _I, _I, _I]),
     "omx_autotune": (_I, [_VP, _I, _PI]),
+    "omx_batch_create": (_I, [C.POINTER(_VP), _I, C.POINTER(_VP)]),
+    "omx_batch_autotune": (_I, [_VP, _I, _PI]),
+    "omx_batch_run": (_I, [_VP, _I, _I, _I, _I, _I]),
+    "omx_batch_launch_count": (C.c_longlong, [_VP]),
+    "omx_batch_destroy": (_I, [_VP]),
     "omx_field_bounds": (_I, [_VP, _I, _PI, _PI]),
     "omx_read_field": (_I, [_VP, _I, _PD]),
     "omx_write_field": (_I, [_VP, _I, _PD]),

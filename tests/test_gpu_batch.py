@@ -1,0 +1,72 @@
+"""Batched multi-grid runs (omx_batch_*): several 3D instances of the inverse-design sweep advance
+together through one persistent launch per pass; every grid must equal its own solo run bit for
+bit (same kernels, same per-grid order), with and without the graph and after the batch
+autotuner.  Calls go through the C-ABI."""
+import numpy as np
+import pytest
+
+import omx
+from omx import decks
+
+pytestmark = pytest.mark.gpu
+
+SIZES = (36, 44, 29, 52)     # uneven sides, one not a multiple of the 32 x 4 tile
+
+
+def build(n, seed, precision):
+    d = decks.deck_cfg5_instance(n, seed=seed, npml=6)
+    g = omx.TMxll(3, d["grid_Ndims"], d["npml"], d["boundaries"], d["dt"], d["dr"], precision=precision)
+    decks.apply_deck(g, d, omx, decks.media_map(d, omx.media_map_from_voxels))
+    for det in d["detectors"]:
+        g.add_detector(det["type"], det["field"], det["idx"])
+    return d, g
+
+
+def fields(g):
+    return [g.read_field(f) for f in (1, 2, 3, 4, 5, 6)]
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+@pytest.mark.parametrize("use_graph,autotune", [(True, False), (False, False), (True, True)])
+def test_batch_equals_solo_runs(precision, use_graph, autotune):
+    steps = 70
+    solo, batch = [], []
+    for k, n in enumerate(SIZES):
+        d, g = build(n, 100 + k, precision)
+        g.run(1, steps, d["n_skip"], d["t_det_print"], use_graph=True)
+        solo.append((fields(g), g.drain_detectors()[1]))
+        g.kill()
+        batch.append(build(n, 100 + k, precision))
+    b = omx.Batch([g for _, g in batch])
+    if autotune:
+        assert b.autotune(reps=2) in (4, 8, 16, 32)
+    d0 = batch[0][0]
+    b.run(1, 30, d0["n_skip"], d0["t_det_print"], use_graph=use_graph)   # two calls: the stepping state carries over
+    b.run(31, steps - 30, d0["n_skip"], d0["t_det_print"], use_graph=use_graph)
+    assert b.launch_count() > 0
+    for (d, g), (f_solo, tr_solo) in zip(batch, solo):
+        tr = g.drain_detectors()[1]
+        assert tr.shape == tr_solo.shape and np.max(np.abs(tr_solo)) > 0
+        assert np.array_equal(tr, tr_solo)
+        for a, s in zip(fields(g), f_solo):
+            assert np.array_equal(a, s)
+    b.kill()
+    for _, g in batch:
+        g.kill()
+
+
+def test_batch_rejects_bad_members():
+    d, g3 = build(32, 1, "fp32")
+    _, g64 = build(32, 2, "fp64")
+    d2 = decks.deck_cfg2(nx=64, ny=48, n_emitters=4, npml=6, pitch_nm=60.0, hole_nm=20.0, film_nm=10.0)
+    g2 = omx.TMxll(2, d2["grid_Ndims"], d2["npml"], d2["boundaries"], d2["dt"], d2["dr"], mode=omx.TMZ)
+    for members in ([g3, g64], [g3, g3], [g3, g2]):
+        with pytest.raises(omx.OMXError):
+            omx.Batch(members)
+    g3.run(1, 2, 1, 0)
+    b = omx.Batch([g3])
+    with pytest.raises(omx.OMXError):
+        b.autotune(reps=1)                    # after a first step: refused
+    b.kill()
+    for g in (g3, g64, g2):
+        g.kill()

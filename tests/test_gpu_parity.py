@@ -208,7 +208,7 @@ def test_fp32_fused_tmz_variants(orc_mod, shape, bx, by, src, steps):
     assert trace_error(tg2, tc) <= FP32_TOL
 
 
-FORMS = ("regs", "tma4", "tma5", "tma6", "tma8")
+FORMS = ("regs", "tma4", "tma5", "tma6", "tma8", "ws4", "ws5", "ws6")
 
 
 @pytest.mark.parametrize("shape,bx,by,src,steps", [
@@ -218,7 +218,7 @@ FORMS = ("regs", "tma4", "tma5", "tma6", "tma8")
 ])
 def test_fused_forms_bit_identical(tmp_path, shape, bx, by, src, steps):
     """Every form of the fused TMz kernel (register prefetch, bulk copies into rings of 4-8
-    slots) performs the same arithmetic on the same words: fields and detector traces agree
+    slots, with or without a dedicated copy warp) performs the same arithmetic on the same words: fields and detector traces agree
     bit for bit.  Each form runs in its own process (the form is chosen once per process)."""
     out = {}
     for form in FORMS:
