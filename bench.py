@@ -210,6 +210,16 @@ def peaks():
         return 6800.0, "fallback"
 
 
+def recorded_traffic(key):
+    """DRAM bytes per launch of a kernel from the committed ncu summaries (None if absent)."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as f:
+            e = json.load(f)[key]
+        return float(e["dram_bytes_read"] + e["dram_bytes_write"]), e["summary"]
+    except (OSError, KeyError, ValueError):
+        return None, None
+
+
 def rel_err(a, b):
     import numpy as np
 
@@ -344,8 +354,11 @@ def gpu_arm(args, dist):
     if per["H"]["launches"] == 0:      # FP32 2D TMz: one fused pass per step
         per["fused_HE"] = per.pop("E")
         per.pop("H")
-        dom, kernel_name = "fused_HE", "k_fused_tmz (H+E step in one pass)"
+        dom, kernel_name = "fused_HE", "k_fused_tmz_* (H+E step in one pass; form from OMX_FUSED_KERNEL, default ws4)"
     alg_bytes = gpu.algorithmic_bytes(kc_dom)
+    traffic, traffic_src = (None, None)
+    if dom == "fused_HE" and args.config == "cfg2" and os.environ.get("OMX_FUSED_KERNEL", "ws4") == "ws4":
+        traffic, traffic_src = recorded_traffic("k_fused_tmz_ws<0, 4> tmz4096")
     avg_s = per[dom]["ms_total"] / per[dom]["launches"] / 1e3
     peak, peak_kind = peaks()
     achieved = alg_bytes / avg_s / 1e9
@@ -425,8 +438,8 @@ def gpu_arm(args, dist):
                        "loop": "device-side loop captured in a CUDA graph, one graph launch per step"},
             "emitter_steps_per_s": emitter_rate,
             "roofline": {"bound": "hbm", "kernel": kernel_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
-                         "algorithmic_bytes_per_launch": alg_bytes},
+                         "frac": achieved / peak, "traffic": traffic, "traffic_source": traffic_src,
+                         "peak_source": peak_kind, "algorithmic_bytes_per_launch": alg_bytes},
             "kernels": per,
             "plain_fp64": plain,
             "cpu_baseline": cpu,
@@ -478,12 +491,14 @@ def gpu_arm_cfg5(args, dist):
     batch = omx.Batch(grids)
     kch = batch.autotune(reps=3)
     batch.run(1, W, 1, tdp, use_graph=True)
+    batch.synchronize()
     dist.barrier()
     clocks = ClockSampler(dist.local_rank)
     clocks.start()
     l0 = batch.launch_count()
     t0 = time.perf_counter()
-    batch.run(1 + W, K, 1, tdp, use_graph=True)       # ends with a stream synchronisation
+    batch.run(1 + W, K, 1, tdp, use_graph=True)
+    batch.synchronize()
     t_batch = time.perf_counter() - t0
     launches = batch.launch_count() - l0
     clk = clocks.stop()
@@ -535,7 +550,7 @@ def gpu_arm_cfg5(args, dist):
                        "l2": "working set %.1f GB > 126 MB L2, no flush" % (cells * 6 * 4 / 1e9),
                        "loop": "omx_batch_run: one persistent launch per pass over all grids' tiles, the step "
                                "captured in a CUDA graph; tile depth %d from omx_batch_autotune" % kch,
-                       "timing": "wall clock around omx_batch_run, which ends with a stream synchronisation"},
+                       "timing": "wall clock around omx_batch_run + omx_batch_synchronize"},
             "one_at_a_time": {"value": solo_value, "unit": "Gcell-updates/s",
                               "how": "the same grids, each its own omx_run (CUDA graph), run one after another",
                               "batch_speedup": value / solo_value,

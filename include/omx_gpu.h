@@ -279,6 +279,8 @@ int omx_batch_autotune(omx_batch *batch, int reps, int *choice);
 int omx_batch_run(omx_batch *batch, int tt0, int nsteps, int n_skip_steps, int t_det_print,
                   int use_graph);
 long long omx_batch_launch_count(const omx_batch *batch);   /* kernels launched by the batch */
+/* omx_batch_run returns once the work is queued; this waits for it (and reports kernel errors). */
+int omx_batch_synchronize(omx_batch *batch);
 int omx_batch_destroy(omx_batch *batch);
 
 /* ---- field access (debug / parity) ---------------------------------------------------------- */
@@ -305,6 +307,37 @@ int omx_timer_start(omx_ctx *ctx);
 int omx_timer_stop(omx_ctx *ctx, float *ms);
 /* flush L2 by writing a scratch buffer larger than L2 on the context stream */
 int omx_flush_l2(omx_ctx *ctx);
+
+/* ---- learned emitter closure: building blocks ----------------------------------------------- */
+/* BF16 GEMM on the tensor cores (tcgen05 MMA, TMA-staged operands, FP32 accumulation in tensor
+ * memory), the building block of the closure's training and inference; exposed on host arrays for
+ * validation.  D[M x N] = act(alpha * A[M x K] * B[N x K]^T + bias[N]) with A, B raw BF16 bits,
+ * row-major, K contiguous (K a multiple of 8); bias may be NULL; act: 0 none, 1 tanh,
+ * 2 logistic sigmoid, 3 relu.  No reference counterpart. */
+int omx_tc_gemm_bf16(const uint16_t *A, const uint16_t *B, const float *bias, float *D, int M, int N, int K,
+                     float alpha, int act);
+
+/* The closure network (no reference counterpart).  Per emitter and quantum step: a GRU (hidden
+ * 128) over the last 32 samples of the local field on the emitter's dipole axis, a tanh MLP
+ * (3 layers of 256) and a linear read-out of the dipole on that axis; BF16 tensor-core GEMMs
+ * with FP32 accumulation, FP32 state and master weights, Adam.  Sequences are e[B][T + 31]
+ * (scaled field samples, step t sees e[b][t .. t+31]) and y / target[T][B] (scaled dipoles);
+ * B must be a multiple of 8.  Parameters are a flat FP32 vector of omx_closure_n_params()
+ * values in the order Wg[512 x 160], bg[512], W1[256 x 128], b1, W2[256 x 256], b2, W3, b3,
+ * w4[256], b4[1]; e_scale / d_scale record the field and dipole units of the scaled data. */
+typedef struct omx_closure omx_closure;
+int omx_closure_create(omx_closure **out);
+int omx_closure_destroy(omx_closure *cl);
+long long omx_closure_n_params(void);
+int omx_closure_set_params(omx_closure *cl, const float *params, double e_scale, double d_scale);
+int omx_closure_get_params(omx_closure *cl, float *params, double *e_scale, double *d_scale);
+int omx_closure_forward(omx_closure *cl, const float *e, int B, int T, float *y);
+/* loss = mean over t >= skip of (y - target)^2 and its gradient (no update) */
+int omx_closure_gradient(omx_closure *cl, const float *e, const float *target, int B, int T, int skip,
+                         float *grad, double *loss);
+/* one Adam step (beta 0.9 / 0.999) on that loss; *loss is the loss before the step */
+int omx_closure_train_step(omx_closure *cl, const float *e, const float *target, int B, int T, int skip,
+                           float lr, double *loss);
 
 #ifdef __cplusplus
 }

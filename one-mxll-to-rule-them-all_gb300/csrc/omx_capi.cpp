@@ -180,6 +180,12 @@ struct omx_ctx {
     // run tables
     DevBuf<double> tab;
     DevBuf<int> d_step;
+    // overlapped schedule of the fused path (graphs only): a side stream runs step s's detector
+    // sampling and emitter work while the main stream runs step s+1's fused pass; the side
+    // stream's kernels read their step's scalars through their own counter
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    DevBuf<int> d_step2;
     DevBuf<float> rowc;    // packed per-row y coefficients of the fused FP32 TMz kernel
     DevBuf<int> d_err;     // kernel error word (bit 0: a bulk-copy wait of the fused kernel ran out)
     int *h_err = nullptr;  // pinned host copy of it, read at every synchronisation
@@ -1091,6 +1097,8 @@ RunPlan stage_run(omx_ctx *c, int tt0, int nsteps, int n_skip, int t_det_print)
     if (!c->d_step.p) c->d_step.alloc(1);
     // the first kernel of every step advances the counter, so it starts one below step 0
     ck(cudaMemsetAsync(c->d_step.p, 0xff, sizeof(int), c->stream), "step");
+    if (!c->d_step2.p) c->d_step2.alloc(1);
+    ck(cudaMemsetAsync(c->d_step2.p, 0xff, sizeof(int), c->stream), "step");
     c->run_step = c->d_step.p;
     RunPlan plan;
     plan.W = W;
@@ -1132,6 +1140,28 @@ template <class R> void run_impl(omx_ctx *c, int tt0, int nsteps, int n_skip, in
         }
         tail();
     };
+    // Fused path inside a graph: step s's detector sampling, emitter step and current scatter
+    // run on the side stream, concurrently with step s+1's fused pass (which reads step s's
+    // buffer set and writes the other one, and touches no emitter state); the emitter current
+    // of step s+1 waits for step s's scatter.  Sampling goes first on the side stream, so that
+    // the wait on the scatter also orders it before the pass that overwrites its buffer set.
+    // Same operations on the same values as one_step: results are identical.
+    auto P2 = [&](int row) { return StepParam{0.0, c->tab.p + row, c->d_step2.p, W}; };
+    auto overlapped_step = [&](bool wait_prev) {
+        fused_step<R>(c);
+        do_sources<R>(c, amps);
+        if (wait_prev) ck(cudaStreamWaitEvent(c->stream, c->ev_join, 0), "wait");
+        do_inject<R>(c, P(0), P(1));
+        ck(cudaEventRecord(c->ev_fork, c->stream), "fork");
+        ck(cudaStreamWaitEvent(c->side, c->ev_fork, 0), "fork");
+        std::swap(c->stream, c->side);
+        launch_step_advance(c->d_step2.p, c->stream);
+        c->launches++;
+        if (has_det) do_sample<R>(c, P2(3), P2(0));
+        for (auto &g : c->groups) do_group<R>(c, *g, P2(2));
+        std::swap(c->stream, c->side);
+        ck(cudaEventRecord(c->ev_join, c->side), "join");
+    };
     // a captured graph of `steps` steps starting from the current buffer set, from the cache
     // when the configuration is unchanged
     auto launch_graph = [&](int steps, int times) {
@@ -1156,7 +1186,12 @@ template <class R> void run_impl(omx_ctx *c, int tt0, int nsteps, int n_skip, in
             cudaGraph_t graph;
             const long long before = c->launches;
             ck(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "capture");
-            for (int q = 0; q < steps; ++q) one_step();
+            if (fused && (has_det || !c->groups.empty())) {
+                for (int q = 0; q < steps; ++q) overlapped_step(q > 0);
+                ck(cudaStreamWaitEvent(c->stream, c->ev_join, 0), "join");   // the last side sequence
+            } else {
+                for (int q = 0; q < steps; ++q) one_step();
+            }
             ck(cudaStreamEndCapture(c->stream, &graph), "end capture");
             g.launches = c->launches - before;
             c->launches = before;
@@ -1172,12 +1207,15 @@ template <class R> void run_impl(omx_ctx *c, int tt0, int nsteps, int n_skip, in
         c->launches += hit->launches * times;
         c->cur = hit->cur_after;   // after an even number of fused steps this is the starting set
     };
-    // the fused path alternates buffer sets, so the main graph covers two steps
-    const int per_graph = fused ? 2 : 1;
+    // the fused path alternates buffer sets, so its graphs cover an even number of steps; long
+    // graphs keep the side stream's work overlapped across all but one step boundary per graph
+    const int per_graph = fused ? (nsteps >= 16 ? 16 : 2) : 1;
     if (use_graph && !c->prof) {
         const int ngraph = nsteps / per_graph;
         if (ngraph > 0) launch_graph(per_graph, ngraph);
-        if (nsteps > ngraph * per_graph) launch_graph(1, 1);
+        int left = nsteps - ngraph * per_graph;
+        if (left >= 2) launch_graph(2, left / 2);
+        if (left % 2) launch_graph(1, 1);
     } else {
         for (int s = 0; s < nsteps; ++s) one_step();
     }
@@ -1347,6 +1385,9 @@ int omx_create(const omx_grid_desc *d, omx_ctx **out)
                 if (c->cpml_axis[a]) req(c->n[a] >= 2 * d->npml, "grid too small for two CPML slabs");
         }
         ck(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream");
+        ck(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking), "stream");
+        ck(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming), "event");
+        ck(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming), "event");
         // layout
         const int align = c->fp32 ? 32 : 16;
         Lay &L = c->L;
@@ -1424,6 +1465,12 @@ int omx_destroy(omx_ctx *c)
     if (c->t0) cudaEventDestroy(c->t0);
     if (c->t1) cudaEventDestroy(c->t1);
     if (c->h_err) cudaFreeHost(c->h_err);
+    if (c->side) {
+        cudaStreamSynchronize(c->side);
+        cudaStreamDestroy(c->side);
+    }
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    if (c->ev_join) cudaEventDestroy(c->ev_join);
     cudaStream_t s = c->stream;
     delete c;
     if (s) cudaStreamDestroy(s);
@@ -2239,6 +2286,15 @@ int omx_batch_run(omx_batch *b, int tt0, int nsteps, int n_skip_steps, int t_det
 }
 
 long long omx_batch_launch_count(const omx_batch *b) { return b ? b->launches : 0; }
+
+int omx_batch_synchronize(omx_batch *b)
+{
+    OMX_API_BEGIN
+    req(b, "null batch");
+    ck(cudaStreamSynchronize(b->stream), "synchronize");
+    for (auto *c : b->ctx) sync_checked(c, "synchronize");
+    OMX_API_END(nullptr)
+}
 
 int omx_batch_destroy(omx_batch *b)
 {

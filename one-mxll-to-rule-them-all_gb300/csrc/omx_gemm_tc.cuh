@@ -1,0 +1,168 @@
+// omx_gemm_tc.cuh -- BF16 GEMM on the 5th-generation tensor cores (tcgen05), FP32 accumulation
+// in tensor memory, for the learned emitter closure.
+//
+//   D[M x N] = act(alpha * A[M x K] * B[N x K]^T + bias[N])      (A, B row-major, K contiguous)
+//
+// Optional epilogue factor (1 - a^2) from an FP32 array a of the same shape (the derivative of a
+// tanh layer, for back-propagation).  Split-K: blockIdx.z takes K blocks [z*kpz, (z+1)*kpz) and
+// writes its partial sums at d_f32 + z * split_stride (reduced afterwards in a fixed order).
+//
+// One CTA computes a 128 x BN tile.  Warp 0 (one lane) streams 128 x 64 tiles of A and BN x 64
+// tiles of B into a STAGES-deep ring with 2D TMA loads (128-byte swizzle, out-of-range rows and
+// columns read as zero); warp 1 (one lane) issues four K=16 MMAs per 64-wide K block into the
+// TMEM accumulator and commits each stage back to its "empty" barrier, then the whole tile to
+// the "accumulated" barrier; all four warps then read their 32 accumulator rows with tcgen05.ld
+// and apply the epilogue.  Every wait is bounded; a wait that runs out sets bit 1 of *err and
+// the CTA leaves (after freeing its TMEM) without writing D.
+#pragma once
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <stdint.h>
+#include "omx_tc.cuh"
+
+namespace omx {
+
+constexpr long long TC_WAIT_CYCLES = 2000000000LL;
+
+struct GemmEpi {
+    float *d_f32;          // optional FP32 output (row stride ld_f32)
+    uint16_t *d_bf16;      // optional BF16 output (row stride ld_bf16)
+    const float *bias;     // optional, per output column
+    const float *dtanh;    // optional: multiply by (1 - a^2), a = dtanh[row * ld_dtanh + col]
+    int ld_f32, ld_bf16, ld_dtanh;
+    int kpz;               // K blocks (of 64) per split (gridDim.z splits)
+    long long split_stride;
+    int act;               // 0 none, 1 tanh, 2 sigmoid, 3 relu
+    float alpha;
+    int M, N;
+    int *err;
+};
+
+__device__ __forceinline__ uint16_t f32_to_bf16_rn(float f)
+{
+    return __bfloat16_as_ushort(__float2bfloat16_rn(f));
+}
+
+__device__ __forceinline__ float epi_act(float v, int act)
+{
+    if (act == 1) return tanhf(v);
+    if (act == 2) return 1.0f / (1.0f + expf(-v));
+    if (act == 3) return v > 0.f ? v : 0.f;
+    return v;
+}
+
+template <int BN, int STAGES> struct GemmSmem {
+    static constexpr int A_BYTES = 128 * 128;          // 128 rows x 64 BF16
+    static constexpr int B_BYTES = BN * 128;           // BN rows x 64 BF16
+    static constexpr int STAGE = A_BYTES + B_BYTES;
+    static constexpr int BARS = STAGES * STAGE;        // offset of the barriers
+    static constexpr int BYTES = BARS + (2 * STAGES + 1) * 8 + 16 + 1024;   // + alignment slack
+    static constexpr uint32_t TMEM_COLS = BN <= 32 ? 32 : (BN <= 64 ? 64 : (BN <= 128 ? 128 : 256));
+};
+
+template <int BN, int STAGES>
+__global__ void __launch_bounds__(128, 1) k_gemm_tc(const __grid_constant__ CUtensorMap tmA,
+                                                    const __grid_constant__ CUtensorMap tmB, int K, GemmEpi E)
+{
+    using S = GemmSmem<BN, STAGES>;
+    extern __shared__ unsigned char gemm_smem_raw[];
+    unsigned char *sm = reinterpret_cast<unsigned char *>(
+        (reinterpret_cast<uintptr_t>(gemm_smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
+    uint64_t *full = reinterpret_cast<uint64_t *>(sm + S::BARS);
+    uint64_t *empty = full + STAGES;
+    uint64_t *accd = empty + STAGES;
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(accd + 1);
+    __shared__ int s_fail;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int m0 = blockIdx.x * 128, n0 = blockIdx.y * BN;
+    const int nk_all = (K + 63) / 64;
+    const int kb0 = gridDim.z > 1 ? (int)blockIdx.z * E.kpz : 0;
+    const int nk = gridDim.z > 1 ? min(E.kpz, nk_all - kb0) : nk_all;
+    if (threadIdx.x == 0) {
+        s_fail = 0;
+        for (int s = 0; s < STAGES; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(accd, 1);
+        mbar_fence_init();
+    }
+    if (warp == 0) tmem_alloc(tslot, S::TMEM_COLS);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t taddr = *tslot;
+
+    if (warp == 0 && lane == 0) {
+        // ---- TMA producer
+        for (int kb = 0; kb < nk; ++kb) {
+            const int s = kb % STAGES;
+            if (kb >= STAGES &&
+                !mbar_wait_bounded(&empty[s], (uint32_t)(((kb / STAGES) - 1) & 1), TC_WAIT_CYCLES)) {
+                atomicExch(&s_fail, 1);
+                break;
+            }
+            unsigned char *a = sm + s * S::STAGE;
+            mbar_arrive_expect_tx(&full[s], (uint32_t)S::STAGE);
+            tma_load_2d(a, &tmA, (kb0 + kb) * 64, m0, &full[s]);
+            tma_load_2d(a + S::A_BYTES, &tmB, (kb0 + kb) * 64, n0, &full[s]);
+        }
+    } else if (warp == 1 && lane == 0) {
+        // ---- MMA issuer
+        constexpr uint32_t idesc = tc_idesc_bf16(BN);
+        for (int kb = 0; kb < nk; ++kb) {
+            const int s = kb % STAGES;
+            if (!mbar_wait_bounded(&full[s], (uint32_t)((kb / STAGES) & 1), TC_WAIT_CYCLES)) {
+                atomicExch(&s_fail, 1);
+                break;
+            }
+            tc_fence_after();
+            const uint32_t a = smem_u32(sm + s * S::STAGE);
+            const uint32_t b = a + S::A_BYTES;
+#pragma unroll
+            for (int k16 = 0; k16 < 4; ++k16)
+                tc_mma_bf16(taddr, tc_smem_desc_sw128(a + 32 * k16), tc_smem_desc_sw128(b + 32 * k16), idesc,
+                            (kb | k16) != 0 ? 1u : 0u);
+            tc_commit(&empty[s]);          // the stage is free once these MMAs have read it
+        }
+        tc_commit(accd);                   // all MMAs of the tile are complete
+    }
+    // ---- epilogue: warp w owns accumulator rows 32w .. 32w+31 (TMEM lanes)
+    const bool ok = mbar_wait_bounded(accd, 0u, TC_WAIT_CYCLES);
+    if (!ok) atomicExch(&s_fail, 1);
+    __syncwarp();
+    tc_fence_after();
+    const bool write = __syncthreads_or(s_fail) == 0;
+    if (write) {
+        const int row = m0 + warp * 32 + lane;
+        float *const dout = E.d_f32 ? E.d_f32 + (long long)blockIdx.z * E.split_stride : nullptr;
+#pragma unroll 1
+        for (int c0 = 0; c0 < BN; c0 += 16) {
+            float v[16];
+            tmem_ld16(taddr + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+            if (row < E.M) {
+#pragma unroll
+                for (int q = 0; q < 16; ++q) {
+                    const int col = n0 + c0 + q;
+                    if (col >= E.N) break;
+                    float x = E.alpha * v[q];
+                    if (E.bias) x += E.bias[col];
+                    x = epi_act(x, E.act);
+                    if (E.dtanh) {
+                        const float a = E.dtanh[(long long)row * E.ld_dtanh + col];
+                        x *= 1.0f - a * a;
+                    }
+                    if (dout) dout[(long long)row * E.ld_f32 + col] = x;
+                    if (E.d_bf16) E.d_bf16[(long long)row * E.ld_bf16 + col] = f32_to_bf16_rn(x);
+                }
+            }
+        }
+    } else if (threadIdx.x == 0) {
+        atomicOr(E.err, 2);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(taddr, S::TMEM_COLS);
+}
+
+}  // namespace omx

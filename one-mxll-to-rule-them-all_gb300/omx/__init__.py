@@ -355,10 +355,75 @@ class Batch:
     def launch_count(self):
         return int(lib().omx_batch_launch_count(self._b))
 
+    def synchronize(self):
+        A.check(lib().omx_batch_synchronize(self._b))
+
     def kill(self):
         if self._b:
             lib().omx_batch_destroy(self._b)
             self._b = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.kill()
+        except Exception:
+            pass
+
+
+def _fptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+class Closure:
+    """The learned emitter closure (omx_closure_*): GRU(128) + MLP(3 x 256) trained and run on the
+    tensor cores in BF16 with FP32 accumulation."""
+
+    def __init__(self, params=None, e_scale=1.0, d_scale=1.0):
+        self._c = C.c_void_p()
+        A.check(lib().omx_closure_create(C.byref(self._c)))
+        self.n_params = int(lib().omx_closure_n_params())
+        if params is not None:
+            self.set_params(params, e_scale, d_scale)
+
+    def set_params(self, params, e_scale=1.0, d_scale=1.0):
+        p = np.ascontiguousarray(params, np.float32)
+        assert p.size == self.n_params
+        A.check(lib().omx_closure_set_params(self._c, _fptr(p), float(e_scale), float(d_scale)))
+
+    def get_params(self):
+        p = np.zeros(self.n_params, np.float32)
+        es, ds = C.c_double(), C.c_double()
+        A.check(lib().omx_closure_get_params(self._c, _fptr(p), C.byref(es), C.byref(ds)))
+        return p, es.value, ds.value
+
+    def forward(self, e, T):
+        e = np.ascontiguousarray(e, np.float32)
+        B = e.shape[0]
+        y = np.zeros((T, B), np.float32)
+        A.check(lib().omx_closure_forward(self._c, _fptr(e), B, int(T), _fptr(y)))
+        return y
+
+    def gradient(self, e, target, skip=0):
+        e = np.ascontiguousarray(e, np.float32)
+        t = np.ascontiguousarray(target, np.float32)
+        g = np.zeros(self.n_params, np.float32)
+        loss = C.c_double()
+        A.check(lib().omx_closure_gradient(self._c, _fptr(e), _fptr(t), e.shape[0], t.shape[0], int(skip), _fptr(g),
+                                           C.byref(loss)))
+        return loss.value, g
+
+    def train_step(self, e, target, lr, skip=0):
+        e = np.ascontiguousarray(e, np.float32)
+        t = np.ascontiguousarray(target, np.float32)
+        loss = C.c_double()
+        A.check(lib().omx_closure_train_step(self._c, _fptr(e), _fptr(t), e.shape[0], t.shape[0], int(skip),
+                                             float(lr), C.byref(loss)))
+        return loss.value
+
+    def kill(self):
+        if self._c:
+            lib().omx_closure_destroy(self._c)
+            self._c = C.c_void_p()
 
     def __del__(self):
         try:

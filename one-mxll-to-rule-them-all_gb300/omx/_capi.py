@@ -69,6 +69,7 @@ _D = C.c_double
 _PD = C.POINTER(C.c_double)
 _PI = C.POINTER(C.c_int)
 _P32 = C.POINTER(C.c_int32)
+_PF = C.POINTER(C.c_float)
 
 SIGNATURES = {
     "omx_select_device": (_I, [_I]),
@@ -108,6 +109,16 @@ SIGNATURES = {
     "omx_batch_autotune": (_I, [_VP, _I, _PI]),
     "omx_batch_run": (_I, [_VP, _I, _I, _I, _I, _I]),
     "omx_batch_launch_count": (C.c_longlong, [_VP]),
+    "omx_batch_synchronize": (_I, [_VP]),
+    "omx_tc_gemm_bf16": (_I, [C.POINTER(C.c_uint16), C.POINTER(C.c_uint16), _PF, _PF, _I, _I, _I, C.c_float, _I]),
+    "omx_closure_create": (_I, [C.POINTER(_VP)]),
+    "omx_closure_destroy": (_I, [_VP]),
+    "omx_closure_n_params": (C.c_longlong, []),
+    "omx_closure_set_params": (_I, [_VP, _PF, _D, _D]),
+    "omx_closure_get_params": (_I, [_VP, _PF, _PD, _PD]),
+    "omx_closure_forward": (_I, [_VP, _PF, _I, _I, _PF]),
+    "omx_closure_gradient": (_I, [_VP, _PF, _PF, _I, _I, _I, _PF, _PD]),
+    "omx_closure_train_step": (_I, [_VP, _PF, _PF, _I, _I, _I, C.c_float, _PD]),
     "omx_batch_destroy": (_I, [_VP]),
     "omx_field_bounds": (_I, [_VP, _I, _PI, _PI]),
     "omx_read_field": (_I, [_VP, _I, _PD]),
