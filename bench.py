@@ -43,8 +43,10 @@ def parse():
     p.add_argument("--steps", type=int, default=2000)
     p.add_argument("--warmup", type=int, default=20)
     p.add_argument("--impl", default="omx", choices=["omx", "reference"])
-    p.add_argument("--config", default="cfg2", choices=["cfg1", "cfg2", "cfg3", "cfg5"])
+    p.add_argument("--config", default="cfg2", choices=["cfg1", "cfg2", "cfg3", "cfg4", "cfg5"])
     p.add_argument("--instances", type=int, default=64, help="cfg5: number of grids in the batched sweep")
+    p.add_argument("--train-steps", type=int, default=300, help="cfg4: Adam steps of the closure training")
+    p.add_argument("--trajectories", type=int, default=16384, help="cfg4: training trajectories (plain propagator)")
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--skip-plain", action="store_true")
     p.add_argument("--error-steps", type=int, default=None,
@@ -568,6 +570,111 @@ def gpu_arm_cfg5(args, dist):
         print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------------- cfg4: closure
+CL_FLOPS_TRAIN = 3 * 2 * (512 * 160 + 256 * 128 + 2 * 256 * 256 + 16 * 256)   # fwd + 2x bwd, per sample-step
+CL_FLOPS_INFER = 2 * (512 * 160 + 256 * 128 + 2 * 256 * 256 + 16 * 256)
+
+
+def gpu_arm_cfg4(args, dist):
+    """The learned closure: training throughput of the tensor-core training step on plain-propagator
+    trajectories, then the 384^3 grid with 1e6 three-level emitters run with the plain FP64
+    propagator and with the trained closure (1 % spot-check subset on the plain propagator)."""
+    import numpy as np
+
+    import omx
+    from omx import closure_train as ct
+    from omx import decks
+
+    if dist.world > 1:
+        omx.select_device(dist.local_rank % max(1, omx.device_count()))
+    deck = decks.deck_cfg3(n=384, n_emitters=1_000_000)
+    dt = deck["dt"] * deck["n_skip"]
+    # ---- training data and training throughput
+    t0 = time.perf_counter()
+    L = 160
+    e, d = ct.make_data(args.trajectories, L, dt, seed=CFG5_SEED + 4)
+    t_gen = time.perf_counter() - t0
+    cl = ct.new_closure(seed=1)
+    B, T, skip = 1024, 16, 4
+    ct.train(cl, e, d, 5, B, T, 1e-3, skip, seed=1)
+    t0 = time.perf_counter()
+    losses = ct.train(cl, e, d, args.train_steps, B, T, 1e-3, skip, seed=2)
+    t_train = time.perf_counter() - t0
+    samples = args.train_steps * B * T
+    # held-out error of the trained network on fresh trajectories (window predictions)
+    eh, dh = ct.make_data(1024, L, dt, seed=CFG5_SEED + 5)
+    gen = ct.batches(eh, dh, 1024, T, np.random.default_rng(3))
+    eb, db = next(gen)
+    yb = cl.forward(eb, T)
+    held = float(np.max(np.abs(yb[skip:] - db[skip:])) / max(np.max(np.abs(db[skip:])), 1e-30))
+    cells = cells_of(deck)
+    ne = n_emitters(deck)
+    K, W = min(args.steps, 200), max(3, args.warmup)
+
+    def timed(g):
+        g.run(1, W, deck["n_skip"], 0, use_graph=True)
+        g.synchronize()
+        dist.barrier()
+        g.timer_start()
+        g.run(1 + W, K, deck["n_skip"], 0, use_graph=True)
+        return dist.max(g.timer_stop())
+
+    # ---- plain FP64 density matrices
+    g, groups = build_gpu(deck, "fp32")
+    ms_plain = timed(g)
+    g.kill()
+    # ---- the closure (network on the tensor cores, 1 % spot check, fallback above 1e-3)
+    g, groups = build_gpu(deck, "fp32")
+    groups[0].attach_closure(cl, check_fraction=0.01, tol=1e-3, check_every=16)
+    clocks = ClockSampler(dist.local_rank)
+    clocks.start()
+    l0 = g.launch_count()
+    ms_cl = timed(g)
+    launches = g.launch_count() - l0
+    clk = clocks.stop()
+    status = groups[0].closure_status()
+    g.kill()
+    # the same with the spot check never falling back, so that the network path is what is timed
+    g, groups = build_gpu(deck, "fp32")
+    groups[0].attach_closure(cl, check_fraction=0.01, tol=1e30, check_every=16)
+    ms_cl_nofb = timed(g)
+    status_nofb = groups[0].closure_status()
+    g.kill()
+    cl.kill()
+    if dist.rank == 0:
+        value = dist.world * cells * K / (ms_cl_nofb / 1e3) / 1e9
+        line = {
+            "metric": METRIC, "value": value, "unit": "Gcell-updates/s", "n_gpus": dist.world, "steps": K,
+            "warmup": W, "ms_per_step": ms_cl_nofb / K, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 fields, bf16 network (fp32 accumulation), fp64 spot check",
+            "data": "synthetic (seeded deck and seeded drives)",
+            "config": {"workload": "cfg4: 3D 384^3 dr 1 nm, 4x4 Au nanorod dimers, 1e6 three-level emitters under "
+                                   "the closure (GRU 128 + MLP 3 x 256, window 32), 1 % spot check",
+                       "cells": cells, "emitters": ne,
+                       "training": {"trajectories": args.trajectories, "steps_per_trajectory": L,
+                                    "batch": B, "bptt_steps": T, "adam_steps": args.train_steps,
+                                    "scaled_down_from": "2e6 trajectories x 2048 steps"}},
+            "emitter_steps_per_s": {"closure": dist.world * ne * K / (ms_cl_nofb / 1e3),
+                                    "plain_fp64": dist.world * ne * K / (ms_plain / 1e3)},
+            "plain_fp64_propagator": {"value": dist.world * cells * K / (ms_plain / 1e3) / 1e9,
+                                      "ms_per_step": ms_plain / K},
+            "closure_error": {"spot_check_last": status_nofb["last_error"], "held_out_windows": held,
+                              "tolerance": 1e-3, "fallback_at_1e-3": status["fallback"],
+                              "fallback_step": status["fallback_step"], "ms_per_step_at_1e-3": ms_cl / K},
+            "training": {"samples_per_s": samples / t_train,
+                         "tflops": CL_FLOPS_TRAIN * samples / t_train / 1e12,
+                         "loss_first": losses[0], "loss_last": losses[-1],
+                         "data_generation_s": t_gen,
+                         "timing": "wall clock, host batch assembly and transfers included"},
+            "roofline": {"bound": "tensor", "kernel": "k_gemm_tc (closure inference GEMMs)",
+                         "achieved": CL_FLOPS_INFER * ne * K / (ms_cl_nofb / 1e3) / 1e12, "peak": None,
+                         "unit": "TFLOP/s", "frac": None, "traffic": None,
+                         "note": "closure flops over the whole step time (field kernels included)"},
+            "cpu_baseline": None, "e2e": None, "gpu_launches": launches, "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     dist = Dist()
@@ -576,6 +683,8 @@ def main():
             reference_arm(args, dist)
         elif args.config == "cfg5":
             gpu_arm_cfg5(args, dist)
+        elif args.config == "cfg4":
+            gpu_arm_cfg4(args, dist)
         else:
             gpu_arm(args, dist)
     finally:

@@ -338,6 +338,28 @@ int omx_closure_gradient(omx_closure *cl, const float *e, const float *target, i
 /* one Adam step (beta 0.9 / 0.999) on that loss; *loss is the loss before the step */
 int omx_closure_train_step(omx_closure *cl, const float *e, const float *target, int B, int T, int skip,
                            float lr, double *loss);
+/* Training data from the plain propagator (the q-groups' FP64 RK4 emitter model): n emitters
+ * (params[n][7 or 9] as in omx_qgroup_create) start in the ground state and are driven by
+ * E(t_s) = amp * sum_k c_k cos(w_k t_s + phi_k), t_s = s * dt, with drive[n][1 + 3K] =
+ * (amp, c_1, w_1, phi_1, ...); outputs e[n][T] = E(t_s) / e_scale and d[n][T] = the dipole
+ * along the emitter axis after step s, / d_scale. */
+int omx_closure_trajectories(int model, int n, int T, int K, double dt, const double *params,
+                             const double *drive, double e_scale, double d_scale, float *e, float *d);
+/* Deploy a trained closure on q-group `group` (before the first step; the closure must outlive
+ * the context).  Each quantum step, the network maps every emitter's last 32 field samples on its
+ * dipole axis and its GRU state to its dipole (dP/dt and the current scatter as for the plain
+ * model).  A spot-check subset (check_fraction of the group, spread evenly) is propagated by the
+ * plain FP64 model with the same fields; every check_every steps the error max|network - plain|
+ * / max|plain| over the subset and those steps is compared with tol.  Above tol the plain
+ * propagator takes over for the rest of the run: the subset keeps its exact state, every other
+ * emitter restarts from the ground state replayed through its stored 32-sample window (earlier
+ * history is lost).  All decisions are taken on the device, inside captured graphs too. */
+int omx_qgroup_attach_closure(omx_ctx *ctx, int group, omx_closure *cl, double check_fraction, double tol,
+                              int check_every);
+/* last completed check's error, whether the plain propagator took over and at which closure step
+ * (-1 if not), and the number of checks so far */
+int omx_qgroup_closure_status(omx_ctx *ctx, int group, double *last_error, int *fallback,
+                              int *fallback_step, int *checks);
 
 #ifdef __cplusplus
 }

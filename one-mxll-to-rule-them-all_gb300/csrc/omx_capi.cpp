@@ -22,6 +22,9 @@
 
 namespace omx {
 void set_global_error(const std::string &msg);
+bool closure_infer(omx_closure *c, const ClDeploy &D, const EmitArgs &A, cudaStream_t s, std::string &err);
+double closure_e_scale(const omx_closure *c);
+double closure_d_scale(const omx_closure *c);
 }
 
 using namespace omx;
@@ -103,6 +106,14 @@ struct GroupRec {
     DevBuf<double> wk;
     std::vector<std::pair<long long, double>> pts;   // (cell key, wk) in write order
     std::vector<int> pts_owner;                       // emitter index per point
+    // learned closure deployed on this group (omx_qgroup_attach_closure)
+    omx_closure *cl = nullptr;
+    omx::ClDeploy dep{};
+    DevBuf<float> cwin, hst, cG, cY;
+    DevBuf<uint16_t> xh, chb, ca1, ca2, ca3;
+    DevBuf<int> sub, sub_of;
+    DevBuf<double> sub_rho;
+    DevBuf<unsigned char> cl_state;
 };
 
 struct omx_ctx {
@@ -953,6 +964,17 @@ template <class R> void do_group(omx_ctx *c, GroupRec &g, StepParam move)
     A.dt = g.d.dt;
     A.h2 = 0.5 * g.d.dt;
     A.h6 = g.d.dt / 6.0;
+    A.only_if = nullptr;
+    if (g.cl) {
+        // network step, spot-check subset, check / fallback; the plain propagator below runs only
+        // once the fallback flag is set
+        launch_cl_gather<R>(field_ptrs<R>(c), c->L, A, g.dep, move, c->stream);
+        std::string err;
+        if (!closure_infer(g.cl, g.dep, A, c->stream, err)) throw Fail{OMX_ERR_CUDA, err};
+        launch_cl_subset_check_reseed(A, g.dep, c->stream);
+        c->launches += 1 + 9 + (g.dep.n_sub > 0 ? 1 : 0) + 2;
+        A.only_if = &g.dep.st->plain_now;    // not on the step the fallback happens
+    }
     launch_emit<R>(field_ptrs<R>(c), c->L, A, move, c->stream);
     ScatArgs S;
     S.np = (int)c->jkeys.size();
@@ -1808,6 +1830,78 @@ int omx_qgroup_step(omx_ctx *c, int gid, int tq_step)
     if (c->fp32) do_group<float>(c, *c->groups[gid], imm(1.0));
     else do_group<double>(c, *c->groups[gid], imm(1.0));
     ck(cudaPeekAtLastError(), "emitter launch");
+    OMX_API_END(c)
+}
+
+int omx_qgroup_attach_closure(omx_ctx *c, int gid, omx_closure *cl, double check_fraction, double tol,
+                              int check_every)
+{
+    OMX_API_BEGIN
+    req(c && cl, "null argument");
+    c->epoch++;
+    req(gid >= 0 && gid < (int)c->groups.size(), "unknown q-group");
+    req(!c->started, "attach the closure before the first step", OMX_ERR_STATE);
+    req(check_fraction > 0.0 && check_fraction <= 1.0 && tol > 0.0 && check_every >= 1, "bad spot-check settings");
+    GroupRec &g = *c->groups[gid];
+    req(!g.cl, "the q-group already has a closure");
+    const int n = g.d.n_systems;
+    const int ns = std::max(1, (int)std::floor(check_fraction * n));
+    std::vector<int> sub(ns), sub_of(n, -1);
+    for (int s = 0; s < ns; ++s) {
+        sub[s] = (int)(((long long)s * n) / ns);    // spread evenly over the group
+        sub_of[sub[s]] = s;
+    }
+    g.sub.upload(sub);
+    g.sub_of.upload(sub_of);
+    g.sub_rho.alloc((size_t)ns * g.nst);             // ground state, as the group's own state
+    g.cwin.alloc((size_t)n * omx::CL_WIN);
+    g.hst.alloc((size_t)n * 128);
+    g.xh.alloc((size_t)n * 160, false);
+    g.cG.alloc((size_t)n * 512, false);
+    g.cY.alloc((size_t)n * 16, false);
+    g.chb.alloc((size_t)n * 128, false);
+    g.ca1.alloc((size_t)n * 256, false);
+    g.ca2.alloc((size_t)n * 256, false);
+    g.ca3.alloc((size_t)n * 256, false);
+    g.cl_state.alloc(sizeof(omx::ClDevState));
+    omx::ClDeploy &D = g.dep;
+    D.n = n;
+    D.n_sub = ns;
+    D.check_every = check_every;
+    D.e_scale = omx::closure_e_scale(cl);
+    D.d_scale = omx::closure_d_scale(cl);
+    D.tol = tol;
+    D.win = g.cwin.p;
+    D.hst = g.hst.p;
+    D.xh = g.xh.p;
+    D.G = g.cG.p;
+    D.Y = g.cY.p;
+    D.hb = g.chb.p;
+    D.a1 = g.ca1.p;
+    D.a2 = g.ca2.p;
+    D.a3 = g.ca3.p;
+    D.sub = g.sub.p;
+    D.sub_of = g.sub_of.p;
+    D.sub_rho = g.sub_rho.p;
+    D.st = reinterpret_cast<omx::ClDevState *>(g.cl_state.p);
+    D.err = c->d_err.p;
+    g.cl = cl;
+    OMX_API_END(c)
+}
+
+int omx_qgroup_closure_status(omx_ctx *c, int gid, double *last_error, int *fallback, int *fallback_step,
+                              int *checks)
+{
+    OMX_API_BEGIN
+    req(c, "null context");
+    req(gid >= 0 && gid < (int)c->groups.size() && c->groups[gid]->cl, "q-group without a closure");
+    sync_checked(c, "closure status");
+    omx::ClDevState st;
+    ck(cudaMemcpy(&st, c->groups[gid]->dep.st, sizeof(st), cudaMemcpyDeviceToHost), "closure status");
+    if (last_error) *last_error = st.last_err;
+    if (fallback) *fallback = st.use_plain;
+    if (fallback_step) *fallback_step = st.use_plain ? st.fallback_step : -1;
+    if (checks) *checks = st.checks;
     OMX_API_END(c)
 }
 

@@ -10,6 +10,7 @@
 
 #include "../../include/omx_gpu.h"
 #include "omx_gemm_tc.cuh"
+#include "omx_internal.h"
 
 namespace omx {
 void set_global_error(const std::string &msg);
@@ -242,11 +243,11 @@ __global__ void k_cl_build_xh(const float *__restrict__ e, long long lde, int t,
 
 // GRU cell: gates G [B x 512] (pre-activations, biases included) -> h_t (FP32 and BF16); the
 // activations r, z, n and the nh pre-activation are kept for the backward pass when cache != null
-__global__ void k_cl_gru_fwd(const float *__restrict__ G, const float *__restrict__ hprev, float *__restrict__ h,
-                             uint16_t *__restrict__ hb, float *__restrict__ cache, int B)
+__global__ void k_cl_gru_fwd(const float *__restrict__ G, const float *hprev, float *h, uint16_t *__restrict__ hb,
+                             float *__restrict__ cache, int B, const int *skip)
 {
     const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (q >= (long long)B * CL_H) return;
+    if (q >= (long long)B * CL_H || (skip && *skip)) return;
     const int b = (int)(q / CL_H), j = (int)(q % CL_H);
     const float *g = G + (long long)b * CL_G;
     const float r = cl_sigmoid(g[j]), z = cl_sigmoid(g[CL_H + j]);
@@ -482,7 +483,7 @@ static bool cl_forward(omx_closure *c, int B, int T, bool keep, std::string &err
         if (!gemm_bf16(xh, CL_XH, c->wg.p, CL_XH, CL_XH, E, c->stream, err)) return false;
         k_cl_gru_fwd<<<cl_blocks((long long)B * CL_H), 256, 0, c->stream>>>(
             c->G.p, hprev, c->H.p + (long long)t * B * CL_H, c->Hb.p + (long long)t * B * CL_H,
-            c->cache.p + (keep ? (long long)t * B * 4 * CL_H : 0), B);
+            c->cache.p + (keep ? (long long)t * B * 4 * CL_H : 0), B, nullptr);
     }
     // MLP on all T*B rows at once
     struct Layer {
@@ -655,6 +656,93 @@ static bool cl_finish(omx_closure *c, std::string &err)
 
 }  // namespace omx
 
+namespace omx {
+
+// network input of a deployed group: the window (oldest sample first; the newest was written at
+// the ring head cl_step % W) and the GRU state
+__global__ void k_cl_dep_xh(ClDeploy D)
+{
+    const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (q >= (long long)D.n * CL_XH || D.st->skip_nn) return;
+    const int n = (int)(q / CL_XH), c = (int)(q % CL_XH);
+    const int head = D.st->cl_step % CL_WIN;
+    const float v = c < CL_W ? D.win[(long long)n * CL_WIN + (head + 1 + c) % CL_WIN] : D.hst[(long long)n * CL_H + c - CL_W];
+    D.xh[q] = f32_to_bf16_rn(v);
+}
+
+// dipole = y * d_scale along the emitter axis, dP/dt against the previous dipole; then the ring
+// advances (one thread, after every reader of this step's head)
+__global__ void k_cl_dep_dipole(const float *__restrict__ Y, EmitArgs A, ClDeploy D)
+{
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (D.st->skip_nn) return;
+    if (n < A.n) {
+        const double *u = A.par + (long long)n * A.npar + (A.npar - 3);
+        const double d = (double)Y[(long long)n * CL_OUT] * D.d_scale;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const double old = A.dipole[3 * n + a];
+            const double nw = d * u[a];
+            A.dipole[3 * n + a] = nw;
+            A.dPdt[3 * n + a] = (nw - old) / A.dt;
+        }
+    }
+}
+__global__ void k_cl_dep_advance(ClDeploy D)
+{
+    if (!D.st->skip_nn) D.st->cl_step += 1;
+}
+
+// One network step of a deployed group (after k_cl_gather, before the spot-check kernels).
+bool closure_infer(omx_closure *c, const ClDeploy &D, const EmitArgs &A, cudaStream_t s, std::string &err)
+{
+    // every buffer belongs to the deployment (allocated when it was attached): nothing is
+    // allocated here, so the step can be captured in a graph
+    const int n = D.n;
+    const int *skip = &D.st->skip_nn;
+    k_cl_dep_xh<<<cl_blocks((long long)n * CL_XH), 256, 0, s>>>(D);
+    GemmEpi E = cl_epi(c, n, CL_G);
+    E.d_f32 = D.G;
+    E.ld_f32 = CL_G;
+    E.bias = c->p.p + CL_OFF_BG;
+    E.skip = skip;
+    E.err = D.err;
+    if (!gemm_bf16(D.xh, CL_XH, c->wg.p, CL_XH, CL_XH, E, s, err)) return false;
+    k_cl_gru_fwd<<<cl_blocks((long long)n * CL_H), 256, 0, s>>>(D.G, D.hst, D.hst, D.hb, nullptr, n, skip);
+    const uint16_t *in[3] = {D.hb, D.a1, D.a2};
+    uint16_t *out[3] = {D.a1, D.a2, D.a3};
+    const uint16_t *w[3] = {c->w1.p, c->w2.p, c->w3.p};
+    const long long bo[3] = {CL_OFF_B1, CL_OFF_B2, CL_OFF_B3};
+    const int k[3] = {CL_H, CL_F, CL_F};
+    for (int l = 0; l < 3; ++l) {
+        GemmEpi El = cl_epi(c, n, CL_F);
+        El.d_bf16 = out[l];
+        El.ld_bf16 = CL_F;
+        El.bias = c->p.p + bo[l];
+        El.act = 1;
+        El.skip = skip;
+        El.err = D.err;
+        if (!gemm_bf16(in[l], k[l], w[l], k[l], k[l], El, s, err)) return false;
+    }
+    GemmEpi Eo = cl_epi(c, n, CL_OUT);
+    Eo.d_f32 = D.Y;
+    Eo.ld_f32 = CL_OUT;
+    Eo.bias = c->b4pad.p;
+    Eo.skip = skip;
+    Eo.err = D.err;
+    if (!gemm_bf16(D.a3, CL_F, c->w4.p, CL_F, CL_F, Eo, s, err)) return false;
+    k_cl_dep_dipole<<<(n + 127) / 128, 128, 0, s>>>(D.Y, A, D);
+    k_cl_dep_advance<<<1, 1, 0, s>>>(D);
+    CL_CK(cudaGetLastError());
+    return true;
+}
+
+double closure_e_scale(const omx_closure *c) { return c->e_scale; }
+double closure_d_scale(const omx_closure *c) { return c->d_scale; }
+int *closure_err_word(omx_closure *c) { return c->err.p; }
+
+}  // namespace omx
+
 // ---- C-ABI of the closure ----------------------------------------------------------------------
 namespace {
 int cl_fail(int code, const std::string &m)
@@ -793,6 +881,47 @@ int omx_closure_train_step(omx_closure *c, const float *e, const float *target, 
         !cl_finish(c, err))
         return cl_fail(OMX_ERR_CUDA, err.empty() ? "train step failed" : err);
     if (loss) *loss = l;
+    return OMX_OK;
+}
+
+int omx_closure_trajectories(int model, int n, int T, int K, double dt, const double *params, const double *drive,
+                             double e_scale, double d_scale, float *e, float *d)
+{
+    using namespace omx;
+    if ((model != OMX_EMITTER_TWO_LEVEL && model != OMX_EMITTER_THREE_LEVEL) || n <= 0 || T <= 0 || K <= 0 ||
+        !(dt > 0) || !params || !drive || !e || !d || !(e_scale > 0) || !(d_scale > 0))
+        return cl_fail(OMX_ERR_ARG, "bad argument");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return cl_fail(OMX_ERR_NODEV, "no CUDA device");
+    }
+    const int npar = model == OMX_EMITTER_TWO_LEVEL ? 7 : 9;
+    DBuf<double> dp, dd;
+    DBuf<float> de, ddip;
+    if (!dp.ensure((size_t)n * npar) || !dd.ensure((size_t)n * (1 + 3 * K)) || !de.ensure((size_t)n * T) ||
+        !ddip.ensure((size_t)n * T))
+        return cl_fail(OMX_ERR_NOMEM, "device allocation failed");
+    cudaMemcpy(dp.p, params, sizeof(double) * n * npar, cudaMemcpyHostToDevice);
+    cudaMemcpy(dd.p, drive, sizeof(double) * n * (1 + 3 * K), cudaMemcpyHostToDevice);
+    ClTrajArgs A{};
+    A.n = n;
+    A.T = T;
+    A.K = K;
+    A.model = model;
+    A.npar = npar;
+    A.dt = dt;
+    A.e_scale = e_scale;
+    A.d_scale = d_scale;
+    A.params = dp.p;
+    A.drive = dd.p;
+    A.e = de.p;
+    A.d = ddip.p;
+    launch_cl_trajectories(A, 0);
+    const cudaError_t err = cudaDeviceSynchronize();
+    if (err != cudaSuccess) return cl_fail(OMX_ERR_CUDA, std::string("trajectories: ") + cudaGetErrorString(err));
+    cudaMemcpy(e, de.p, sizeof(float) * n * (size_t)T, cudaMemcpyDeviceToHost);
+    cudaMemcpy(d, ddip.p, sizeof(float) * n * (size_t)T, cudaMemcpyDeviceToHost);
     return OMX_OK;
 }
 

@@ -31,6 +31,7 @@ struct GemmEpi {
     const float *dtanh;    // optional: multiply by (1 - a^2), a = dtanh[row * ld_dtanh + col]
     int ld_f32, ld_bf16, ld_dtanh;
     int kpz;               // K blocks (of 64) per split (gridDim.z splits)
+    const int *skip;       // optional: the whole launch does nothing while *skip != 0
     long long split_stride;
     int act;               // 0 none, 1 tanh, 2 sigmoid, 3 relu
     float alpha;
@@ -65,6 +66,7 @@ __global__ void __launch_bounds__(128, 1) k_gemm_tc(const __grid_constant__ CUte
                                                     const __grid_constant__ CUtensorMap tmB, int K, GemmEpi E)
 {
     using S = GemmSmem<BN, STAGES>;
+    if (E.skip && *E.skip) return;   // uniform for the launch; before any barrier or TMEM use
     extern __shared__ unsigned char gemm_smem_raw[];
     unsigned char *sm = reinterpret_cast<unsigned char *>(
         (reinterpret_cast<uintptr_t>(gemm_smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));

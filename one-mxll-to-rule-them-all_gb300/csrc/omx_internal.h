@@ -122,6 +122,7 @@ struct EmitArgs {
     const double *rates;      // (1/T1, 1/T2) per emitter, formed at group creation
     double *rho, *E, *dipole, *dPdt;
     double dt, h2, h6;        // dt, dt/2, dt/6
+    const int *only_if;       // optional: run only while *only_if != 0 (the closure's fallback flag)
 };
 
 struct ScatArgs {
@@ -170,6 +171,49 @@ struct Fused2Args {
 void launch_fused_tmz(const Fused2Args &A, const GridArgs<float> &G, int form, void *stream);
 void launch_ade_post(const FieldPtrs<float> &Fin, const FieldPtrs<float> &Fout, const GridArgs<float> &G, void *stream);
 void launch_flush(float *buf, long long n, void *stream);
+
+// ---- learned closure: plain-propagator work that must round like the q-group kernel ------------
+// training trajectories: per trajectory q, E(t_s) = amp * sum_k c_k cos(w_k t_s + phi_k) with
+// t_s = s * dt (drive[q] = amp, then K triples c, w, phi); the emitter (params[q], npar values)
+// starts in the ground state and is advanced by the q-group's RK4 with E held over each step.
+struct ClTrajArgs {
+    int n, T, K, model, npar;
+    double dt, e_scale, d_scale;
+    const double *params, *drive;
+    float *e, *d;            // [n][T]: E(t_s) / e_scale and the dipole after step s / d_scale
+};
+void launch_cl_trajectories(const ClTrajArgs &A, void *stream);
+
+// deployment of a trained closure in a q-group (device-side control, so that a captured graph
+// needs no host decision): the state block and the per-group arguments
+constexpr int CL_WIN = 32;
+struct ClDevState {
+    int cl_step;          // closure steps taken (the window ring's head is cl_step % CL_WIN)
+    int use_plain;        // 1 once the spot-check failed: the plain propagator runs from then on
+    int skip_nn;          // 1 when the network does not run this step (no q-step, or use_plain)
+    int reseed;           // 1 on the step the fallback happened (density matrices re-seeded)
+    int checks, fallback_step, steps_since_check;
+    int plain_now;        // use_plain as it was when this step began (the plain kernel's switch)
+    unsigned long long err_bits, scale_bits;   // running max |closure - plain|, max |plain| (>= 0)
+    double last_err;      // error of the last completed check window
+};
+struct ClDeploy {
+    int n, n_sub, check_every;
+    double e_scale, d_scale, tol;
+    float *win;           // [n][CL_WIN] scaled field history on the dipole axis
+    float *hst;           // [n][128] GRU state
+    uint16_t *xh;         // [n][160] network input (BF16)
+    float *G, *Y;         // [n][512] gate pre-activations, [n][16] read-out
+    uint16_t *hb, *a1, *a2, *a3;   // [n][128], [n][256] x 3 layer outputs (BF16)
+    const int *sub;       // [n_sub] emitters of the spot-check subset
+    const int *sub_of;    // [n] subset slot of each emitter, or -1
+    double *sub_rho;      // [n_sub][nst] their plain density matrices
+    ClDevState *st;
+    int *err;             // error word of the owning context (tensor-core pipeline waits)
+};
+template <class R> void launch_cl_gather(const FieldPtrs<R> &F, const Lay &L, const EmitArgs &A, const ClDeploy &D,
+                                         StepParam move, void *stream);
+void launch_cl_subset_check_reseed(const EmitArgs &A, const ClDeploy &D, void *stream);
 
 // ---- batched multi-grid launches (3D): one launch per pass over several grids ----------------
 template <class R> struct BatchGrid {

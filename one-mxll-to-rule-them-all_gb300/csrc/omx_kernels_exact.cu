@@ -78,6 +78,26 @@ void launch_step_advance(int *step, void *s)
 {
     k_step_advance<<<1, 32, 0, (cudaStream_t)s>>>(step);
 }
+void launch_cl_trajectories(const ClTrajArgs &A, void *s)
+{
+    if (A.n <= 0) return;
+    k_cl_trajectories<<<(A.n + 63) / 64, 64, 0, (cudaStream_t)s>>>(A);
+}
+template <class R>
+void launch_cl_gather(const FieldPtrs<R> &F, const Lay &L, const EmitArgs &A, const ClDeploy &D, StepParam move, void *s)
+{
+    k_cl_gather<R><<<(A.n + 127) / 128, 128, 0, (cudaStream_t)s>>>(F, L, A, D, move);
+}
+template void launch_cl_gather<float>(const FieldPtrs<float> &, const Lay &, const EmitArgs &, const ClDeploy &,
+                                      StepParam, void *);
+template void launch_cl_gather<double>(const FieldPtrs<double> &, const Lay &, const EmitArgs &, const ClDeploy &,
+                                       StepParam, void *);
+void launch_cl_subset_check_reseed(const EmitArgs &A, const ClDeploy &D, void *s)
+{
+    if (D.n_sub > 0) k_cl_subset<<<(D.n_sub + 31) / 32, 32, 0, (cudaStream_t)s>>>(A, D);
+    k_cl_check<<<1, 1, 0, (cudaStream_t)s>>>(D);
+    k_cl_reseed<<<(A.n + 31) / 32, 32, 0, (cudaStream_t)s>>>(A, D);
+}
 void launch_flush(float *buf, long long n, void *s)
 {
     k_flush<<<152 * 8, 256, 0, (cudaStream_t)s>>>(buf, n);

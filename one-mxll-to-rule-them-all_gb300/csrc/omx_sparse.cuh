@@ -98,6 +98,7 @@ __global__ void k_emit(FieldPtrs<R> F, Lay L, EmitArgs A, StepParam move_p)
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= A.n) return;
     if (sp_get(move_p) == 0.0) return;
+    if (A.only_if && *A.only_if == 0) return;
     const int i = A.ci[n], j = A.cj[n], k = A.ck[n];
     const long long c = L.off + i + (long long)L.px * j + L.pz * k;
     double E[3] = {0.0, 0.0, 0.0};
@@ -231,6 +232,150 @@ template <class R> __global__ void k_sample_batch(const BatchDet<R> *__restrict_
     if (q >= total) return;
     const int k = batch_entry(e, n, q);
     sample_point<R>(e[k].F, e[k].D, e[k].slot, e[k].time, (int)(q - e[k].p0));
+}
+
+// ---- closure training data: the plain propagator under band-limited drives -------------------
+__global__ void k_cl_trajectories(ClTrajArgs A)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= A.n) return;
+    const double *pr = A.params + (long long)q * A.npar;
+    const double *dv = A.drive + (long long)q * (1 + 3 * A.K);
+    const int m = A.model == 1 ? 2 : 4;
+    const double g1 = 1.0 / pr[m], g2 = 1.0 / pr[m + 1], h2 = 0.5 * A.dt, h6 = A.dt / 6.0;
+    double rho[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int s = 0; s < A.T; ++s) {
+        const double t = A.dt * s;
+        double E = 0.0;
+        for (int k = 0; k < A.K; ++k) E += dv[1 + 3 * k] * cos(dv[2 + 3 * k] * t + dv[3 + 3 * k]);
+        E = dv[0] * E;
+        double d;
+        if (A.model == 1) {
+            rk4r<3>(1, pr, rho, E, A.dt, h2, h6, g1, g2);
+            d = 2.0 * pr[1] * rho[1];
+        } else {
+            rk4r<8>(2, pr, rho, E, A.dt, h2, h6, g1, g2);
+            d = 2.0 * pr[2] * rho[2] + 2.0 * pr[3] * rho[4];
+        }
+        A.e[(long long)q * A.T + s] = (float)(E / A.e_scale);
+        A.d[(long long)q * A.T + s] = (float)(d / A.d_scale);
+    }
+}
+
+// ---- closure deployment: the plain-arithmetic parts ---------------------------------------------
+// E at the emitter cell (the k_emit stencils), kept in A.E; its component on the dipole axis
+// goes into the window ring while the network runs
+template <class R>
+__global__ void k_cl_gather(FieldPtrs<R> F, Lay L, EmitArgs A, ClDeploy D, StepParam move_p)
+{
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool move = sp_get(move_p) != 0.0;
+    const int use_plain = D.st->use_plain;
+    if (n == 0) {
+        D.st->skip_nn = (!move || use_plain) ? 1 : 0;
+        D.st->plain_now = use_plain;
+    }
+    if (n >= A.n || !move) return;
+    const int i = A.ci[n], j = A.cj[n], k = A.ck[n];
+    const long long c = L.off + i + (long long)L.px * j + L.pz * k;
+    double E[3] = {0.0, 0.0, 0.0};
+    if (A.dims == 3) {
+        E[0] = 0.5 * ((double)F.f[0][c - 1] + (double)F.f[0][c]);
+        E[1] = 0.5 * ((double)F.f[1][c - L.px] + (double)F.f[1][c]);
+        E[2] = 0.5 * ((double)F.f[2][c - L.pz] + (double)F.f[2][c]);
+    } else if (A.dims == 2) {
+        if (A.mode2d == 2) {
+            E[0] = 0.5 * ((double)F.f[0][c - 1] + (double)F.f[0][c]);
+            E[1] = 0.5 * ((double)F.f[1][c - L.px] + (double)F.f[1][c]);
+        } else {
+            E[2] = (double)F.f[2][c];
+        }
+    } else {
+        E[0] = (double)F.f[0][c];
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) A.E[3 * n + a] = E[a];
+    if (!use_plain) {
+        const double *u = A.par + (long long)n * A.npar + (A.npar - 3);
+        const double E_u = u[0] * E[0] + u[1] * E[1] + u[2] * E[2];
+        D.win[(long long)n * CL_WIN + (D.st->cl_step % CL_WIN)] = (float)(E_u / D.e_scale);
+    }
+}
+
+__device__ __forceinline__ double cl_axis_dipole(const EmitArgs &A, const double *rho, const double *pr)
+{
+    return A.model == 1 ? 2.0 * pr[1] * rho[1] : 2.0 * pr[2] * rho[2] + 2.0 * pr[3] * rho[4];
+}
+
+// spot-check subset: the plain propagator on the sampled emitters with the gathered field; the
+// difference to the network's dipole (already in A.dipole) feeds the running maxima
+__global__ void k_cl_subset(EmitArgs A, ClDeploy D)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= D.n_sub || D.st->skip_nn) return;
+    const int n = D.sub[s];
+    const double *pr = A.par + (long long)n * A.npar;
+    const double *u = pr + (A.npar - 3);
+    const double E_u = u[0] * A.E[3 * n] + u[1] * A.E[3 * n + 1] + u[2] * A.E[3 * n + 2];
+    double *rho = D.sub_rho + (long long)s * A.nst;
+    double r[8];
+    for (int q = 0; q < A.nst; ++q) r[q] = rho[q];
+    const double g1 = A.rates[2 * n], g2 = A.rates[2 * n + 1];
+    if (A.model == 1) rk4r<3>(1, pr, r, E_u, A.dt, A.h2, A.h6, g1, g2);
+    else rk4r<8>(2, pr, r, E_u, A.dt, A.h2, A.h6, g1, g2);
+    for (int q = 0; q < A.nst; ++q) rho[q] = r[q];
+    const double dp = cl_axis_dipole(A, r, pr);
+    const double dn = u[0] * A.dipole[3 * n] + u[1] * A.dipole[3 * n + 1] + u[2] * A.dipole[3 * n + 2];
+    atomicMax(&D.st->err_bits, (unsigned long long)__double_as_longlong(fabs(dn - dp)));
+    atomicMax(&D.st->scale_bits, (unsigned long long)__double_as_longlong(fabs(dp)));
+}
+
+// every check_every network steps: error = max |closure - plain| / max |plain| over the window;
+// above tol the plain propagator takes over (and the density matrices are re-seeded)
+__global__ void k_cl_check(ClDeploy D)
+{
+    ClDevState *st = D.st;
+    st->reseed = 0;
+    if (st->skip_nn) return;
+    if (++st->steps_since_check < D.check_every) return;
+    const double err = __longlong_as_double((long long)st->err_bits);
+    const double sc = __longlong_as_double((long long)st->scale_bits);
+    const double rel = sc > 0.0 ? err / sc : (err > 0.0 ? 1e300 : 0.0);
+    st->last_err = rel;
+    st->checks += 1;
+    st->steps_since_check = 0;
+    st->err_bits = 0ull;
+    st->scale_bits = 0ull;
+    if (rel > D.tol) {
+        st->use_plain = 1;
+        st->reseed = 1;
+        st->fallback_step = st->cl_step;
+    }
+}
+
+// on the fallback step: every emitter's density matrix restarts from the ground state and is
+// replayed through its stored field window with the plain propagator (the sampled emitters take
+// their exact plain state); the network's last dipole stays as the previous-step dipole
+__global__ void k_cl_reseed(EmitArgs A, ClDeploy D)
+{
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= A.n || !D.st->reseed) return;
+    double *rho = A.rho + (long long)n * A.nst;
+    const int s = D.sub_of[n];
+    if (s >= 0) {
+        for (int q = 0; q < A.nst; ++q) rho[q] = D.sub_rho[(long long)s * A.nst + q];
+        return;
+    }
+    const double *pr = A.par + (long long)n * A.npar;
+    const double g1 = A.rates[2 * n], g2 = A.rates[2 * n + 1];
+    double r[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    const int head = D.st->cl_step % CL_WIN;        // the newest sample sits at head - 1
+    for (int c = 0; c < CL_WIN; ++c) {
+        const double E_u = (double)D.win[(long long)n * CL_WIN + (head + c) % CL_WIN] * D.e_scale;
+        if (A.model == 1) rk4r<3>(1, pr, r, E_u, A.dt, A.h2, A.h6, g1, g2);
+        else rk4r<8>(2, pr, r, E_u, A.dt, A.h2, A.h6, g1, g2);
+    }
+    for (int q = 0; q < A.nst; ++q) rho[q] = r[q];
 }
 
 }  // namespace omx

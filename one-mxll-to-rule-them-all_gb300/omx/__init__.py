@@ -91,6 +91,20 @@ class QGroup:
                                       A.dptr(rho)), self.mxll._ctx)
         return {"dipole": dip, "dPt_dt": dpdt, "E": ef, "rho": rho}
 
+    def attach_closure(self, closure, check_fraction=0.01, tol=1e-3, check_every=16):
+        """Run this group's emitters through a trained closure, with a spot-check subset on the
+        plain propagator that takes over above `tol` (omx_qgroup_attach_closure)."""
+        A.check(lib().omx_qgroup_attach_closure(self.mxll._ctx, self.gid, closure._c, float(check_fraction),
+                                                float(tol), int(check_every)), self.mxll._ctx)
+        self._closure = closure                  # the closure must outlive the context
+
+    def closure_status(self):
+        err, fb, step, checks = C.c_double(), C.c_int(), C.c_int(), C.c_int()
+        A.check(lib().omx_qgroup_closure_status(self.mxll._ctx, self.gid, C.byref(err), C.byref(fb), C.byref(step),
+                                                C.byref(checks)), self.mxll._ctx)
+        return {"last_error": err.value, "fallback": bool(fb.value), "fallback_step": step.value,
+                "checks": checks.value}
+
 
 class TMxll:
     """GPU drop-in for TMxll_1D/2D/3D (init_{1,2,3}Dgrid ... td_propagate_E_field)."""
@@ -372,6 +386,19 @@ class Batch:
 
 def _fptr(a):
     return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def closure_trajectories(model, params, drive, T, dt, e_scale, d_scale):
+    """Plain-propagator training trajectories (omx_closure_trajectories): returns e, d [n][T]."""
+    params = np.ascontiguousarray(params, np.float64)
+    drive = np.ascontiguousarray(drive, np.float64)
+    n = params.shape[0]
+    K = (drive.shape[1] - 1) // 3
+    e = np.zeros((n, T), np.float32)
+    d = np.zeros((n, T), np.float32)
+    A.check(lib().omx_closure_trajectories(int(model), n, int(T), K, float(dt), A.dptr(params), A.dptr(drive),
+                                           float(e_scale), float(d_scale), _fptr(e), _fptr(d)))
+    return e, d
 
 
 class Closure:

@@ -119,6 +119,9 @@ SIGNATURES = {
     "omx_closure_forward": (_I, [_VP, _PF, _I, _I, _PF]),
     "omx_closure_gradient": (_I, [_VP, _PF, _PF, _I, _I, _I, _PF, _PD]),
     "omx_closure_train_step": (_I, [_VP, _PF, _PF, _I, _I, _I, C.c_float, _PD]),
+    "omx_closure_trajectories": (_I, [_I, _I, _I, _I, _D, _PD, _PD, _D, _D, _PF, _PF]),
+    "omx_qgroup_attach_closure": (_I, [_VP, _I, _VP, _D, _D, _I]),
+    "omx_qgroup_closure_status": (_I, [_VP, _I, _PD, _PI, _PI, _PI]),
     "omx_batch_destroy": (_I, [_VP]),
     "omx_field_bounds": (_I, [_VP, _I, _PI, _PI]),
     "omx_read_field": (_I, [_VP, _I, _PD]),

@@ -134,3 +134,78 @@ def test_closure_training_reduces_loss():
         last = cl.train_step(e, target, 2e-3, skip=0)
     assert last <= first / 10.0, (first, last)
     cl.kill()
+
+
+# ---- deployment in a q-group: spot check, fallback, graphs --------------------------------------
+from omx import decks  # noqa: E402
+from gpu_harness import tmz_variant_deck  # noqa: E402
+
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle"))
+import oracle as orc_mod  # noqa: E402
+
+E_SCALE, D_SCALE = 1e-4, 1e-3
+
+
+def _deployed(tol, check_every, frac=0.1, seed=4):
+    deck = tmz_variant_deck(128, 96, 2, 3, src="plane")
+    g = omx.TMxll(2, deck["grid_Ndims"], deck["npml"], deck["boundaries"], deck["dt"], deck["dr"], mode=omx.TMZ,
+                  precision="fp32")
+    groups = decks.apply_deck(g, deck, omx, decks.media_map(deck, omx.media_map_from_voxels))
+    params = co.init_params(seed).astype(np.float32)
+    params[-1] = 0.5               # read-out bias: a visibly wrong network (the plain dipole starts at 0)
+    cl = omx.Closure(params, E_SCALE, D_SCALE)
+    groups[0].attach_closure(cl, check_fraction=frac, tol=tol, check_every=check_every)
+    return deck, g, groups[0], cl
+
+
+def test_closure_fallback_reseeds_from_the_window():
+    """An untrained network fails the first check (after 4 steps); every emitter outside the
+    subset restarts from the ground state replayed through its window (here: 28 empty slots and
+    the 4 samples seen), the subset keeps its exact plain state, and the plain propagator runs
+    from then on.  All compared bit for bit with the oracle's emitter step."""
+    deck, g, grp, cl = _deployed(tol=1e-6, check_every=4)
+    gd = deck["groups"][0]
+    par = np.asarray(gd["params"])
+    u = par[:, -3:]
+    Eu = []
+    for tt in range(1, 7):
+        g.run(tt, 1, deck["n_skip"], 0, use_graph=True)
+        E = grp.read()["E"]
+        Eu.append(u[:, 0] * E[:, 0] + u[:, 1] * E[:, 1] + u[:, 2] * E[:, 2])
+        st = grp.closure_status()
+        if tt < 4:
+            assert not st["fallback"]
+        if tt == 4:
+            assert st["fallback"] and st["fallback_step"] == 4 and st["checks"] == 1
+            rho4 = grp.read()["rho"]
+    rho6 = grp.read()["rho"]
+    n = par.shape[0]
+    for e in range(n):
+        r = np.zeros(3)
+        window = [0.0] * 28 + [float(np.float32(Eu[s][e] / E_SCALE)) * E_SCALE for s in range(4)]
+        if e % 10 == 0:                      # the subset (10 % of 30, spread evenly): exact plain state
+            window = [Eu[s][e] for s in range(4)]
+        for x in window:
+            r = orc_mod.emitter_step(1, par[e], r, x, gd["dt"])
+        assert np.array_equal(r, rho4[e]), e
+        for s in (4, 5):                     # plain propagator after the fallback
+            r = orc_mod.emitter_step(1, par[e], r, Eu[s][e], gd["dt"])
+        assert np.array_equal(r, rho6[e]), e
+    g.kill()
+    cl.kill()
+
+
+def test_closure_graph_equals_calls_and_check_cadence():
+    out = []
+    for graph in (True, False):
+        deck, g, grp, cl = _deployed(tol=1e30, check_every=5)
+        g.run(1, 23, deck["n_skip"], 0, use_graph=graph)
+        st = grp.closure_status()
+        assert not st["fallback"] and st["checks"] == 4
+        r = grp.read()
+        out.append((r["dipole"], r["dPt_dt"], g.read_field(3)))
+        g.kill()
+        cl.kill()
+    for a, b in zip(out[0], out[1]):
+        assert np.array_equal(a, b)
+    assert np.max(np.abs(out[0][0])) > 0
