@@ -10,7 +10,7 @@
 namespace omx {
 
 template <class R, bool EXACT, int PASS>
-__global__ void __launch_bounds__(128) k_batch3(const BatchGrid<R> *__restrict__ grids, int n, long long total, int kch)
+__global__ void __launch_bounds__(128, 5) k_batch3(const BatchGrid<R> *__restrict__ grids, int n, long long total, int kch)
 {
     __shared__ __align__(16) unsigned char raw[sizeof(BatchGrid<R>)];
     const BatchGrid<R> &sg = *reinterpret_cast<const BatchGrid<R> *>(raw);

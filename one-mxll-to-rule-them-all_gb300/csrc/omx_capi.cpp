@@ -1857,7 +1857,6 @@ int omx_qgroup_attach_closure(omx_ctx *c, int gid, omx_closure *cl, double check
     g.cwin.alloc((size_t)n * omx::CL_WIN);
     g.hst.alloc((size_t)n * 128);
     g.xh.alloc((size_t)n * 160, false);
-    g.cG.alloc((size_t)n * 512, false);
     g.cY.alloc((size_t)n * 16, false);
     g.chb.alloc((size_t)n * 128, false);
     g.ca1.alloc((size_t)n * 256, false);
@@ -1874,7 +1873,7 @@ int omx_qgroup_attach_closure(omx_ctx *c, int gid, omx_closure *cl, double check
     D.win = g.cwin.p;
     D.hst = g.hst.p;
     D.xh = g.xh.p;
-    D.G = g.cG.p;
+    D.G = nullptr;          // the gate pre-activations stay in tensor memory (fused GRU epilogue)
     D.Y = g.cY.p;
     D.hb = g.chb.p;
     D.a1 = g.ca1.p;

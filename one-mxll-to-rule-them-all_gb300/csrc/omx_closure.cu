@@ -46,28 +46,35 @@ static bool tmap_bf16(CUtensorMap *m, const void *base, unsigned long long rows,
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-constexpr int GEMM_STAGES = 4;
 constexpr int GEMM_MAX_DEV = 64;
 
-template <int BN> static cudaError_t gemm_launch(const CUtensorMap &ta, const CUtensorMap &tb, int K, const GemmEpi &E,
-                                                 cudaStream_t s)
+// Ring depth: 4 slots for long K; 2 for short K (the closure's K = 128..256), which leaves room
+// for three CTAs per SM so that one CTA's epilogue overlaps the others' loads and MMAs.
+template <int BN, int STAGES>
+static cudaError_t gemm_launch_s(const CUtensorMap &ta, const CUtensorMap &tb, int K, const GemmEpi &E, cudaStream_t s)
 {
-    using S = GemmSmem<BN, GEMM_STAGES>;
+    using S = GemmSmem<BN, STAGES>;
     static bool attr[GEMM_MAX_DEV] = {};
     int dev = 0;
     cudaGetDevice(&dev);
     bool &a = attr[dev < GEMM_MAX_DEV ? dev : 0];
     if (!a) {
         const cudaError_t e =
-            cudaFuncSetAttribute(k_gemm_tc<BN, GEMM_STAGES>, cudaFuncAttributeMaxDynamicSharedMemorySize, S::BYTES);
+            cudaFuncSetAttribute(k_gemm_tc<BN, STAGES>, cudaFuncAttributeMaxDynamicSharedMemorySize, S::BYTES);
         if (e != cudaSuccess) return e;
         a = true;
     }
     const int nk = (K + 63) / 64;
     const int splits = E.kpz > 0 ? (nk + E.kpz - 1) / E.kpz : 1;
     const dim3 grid((E.M + 127) / 128, (E.N + BN - 1) / BN, splits);
-    k_gemm_tc<BN, GEMM_STAGES><<<grid, 128, S::BYTES, s>>>(ta, tb, K, E);
+    k_gemm_tc<BN, STAGES><<<grid, 128, S::BYTES, s>>>(ta, tb, K, E);
     return cudaGetLastError();
+}
+template <int BN>
+static cudaError_t gemm_launch(const CUtensorMap &ta, const CUtensorMap &tb, int K, const GemmEpi &E, cudaStream_t s)
+{
+    const int nk = (E.kpz > 0 ? E.kpz : (K + 63) / 64);
+    return nk <= 4 ? gemm_launch_s<BN, 2>(ta, tb, K, E, s) : gemm_launch_s<BN, 4>(ta, tb, K, E, s);
 }
 
 // D = act(alpha * A * B^T + bias) on device buffers; A [M x K] (lda), B [N x K] (ldb) in BF16.
@@ -196,9 +203,17 @@ __device__ __forceinline__ bool cl_wg_masked(int row, int col)
 __device__ __forceinline__ float cl_sigmoid(float x) { return 1.0f / (1.0f + expf(-x)); }
 
 // FP32 master -> BF16 weights (row-major and transposed), masked Wg, padded read-out row
+// row of the gate weights in the deployment order: tile b of 128 rows holds hidden units
+// 32b .. 32b+31, four consecutive rows per unit in gate order r, z, nx, nh (the fused GRU epilogue)
+__device__ __forceinline__ int cl_gate_perm(int r)
+{
+    const int gate = r / CL_H, j = r % CL_H;
+    return 128 * (j / 32) + 4 * (j % 32) + gate;
+}
+
 __global__ void k_cl_refresh(const float *__restrict__ p, uint16_t *wg, uint16_t *wgT, uint16_t *w1, uint16_t *w1T,
                              uint16_t *w2, uint16_t *w2T, uint16_t *w3, uint16_t *w3T, uint16_t *w4, uint16_t *w4T,
-                             float *b4pad)
+                             float *b4pad, uint16_t *wgp, float *bgp)
 {
     const long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (n < (long long)CL_G * CL_XH) {
@@ -206,7 +221,9 @@ __global__ void k_cl_refresh(const float *__restrict__ p, uint16_t *wg, uint16_t
         const uint16_t v = cl_wg_masked(r, c) ? (uint16_t)0 : f32_to_bf16_rn(p[CL_OFF_WG + n]);
         wg[n] = v;
         wgT[(long long)c * CL_G + r] = v;
+        wgp[(long long)cl_gate_perm(r) * CL_XH + c] = v;
     }
+    if (n < CL_G) bgp[cl_gate_perm((int)n)] = p[CL_OFF_BG + n];
     if (n < (long long)CL_F * CL_H) {
         const int r = (int)(n / CL_H), c = (int)(n % CL_H);
         const uint16_t v = f32_to_bf16_rn(p[CL_OFF_W1 + n]);
@@ -407,8 +424,8 @@ struct omx_closure {
     cudaStream_t stream = nullptr;
     long long adam_step = 0;
     double e_scale = 1.0, d_scale = 1.0;   // field and dipole scales of the training data
-    omx::DBuf<float> p, g, m, v, b4pad;
-    omx::DBuf<uint16_t> wg, wgT, w1, w1T, w2, w2T, w3, w3T, w4, w4T;
+    omx::DBuf<float> p, g, m, v, b4pad, bgp;
+    omx::DBuf<uint16_t> wg, wgT, w1, w1T, w2, w2T, w3, w3T, w4, w4T, wgp;   // wgp, bgp: deployment gate order
     // training / batch work buffers (grown on demand)
     omx::DBuf<float> e, tgt, G, H, cache, A1, A2, A3, Y, dHm, dXH, dh, dhd, part;
     omx::DBuf<uint16_t> XH, Hb, A1b, A2b, A3b, dY, dZ1, dZ2, dZ3, dG, T1, T2;
@@ -439,7 +456,7 @@ static bool cl_refresh(omx_closure *c, std::string &err)
     k_cl_refresh<<<cl_blocks((long long)CL_F * CL_F > (long long)CL_G * CL_XH ? (long long)CL_F * CL_F
                                                                             : (long long)CL_G * CL_XH),
                    256, 0, c->stream>>>(c->p.p, c->wg.p, c->wgT.p, c->w1.p, c->w1T.p, c->w2.p, c->w2T.p, c->w3.p,
-                                        c->w3T.p, c->w4.p, c->w4T.p, c->b4pad.p);
+                                        c->w3T.p, c->w4.p, c->w4T.p, c->b4pad.p, c->wgp.p, c->bgp.p);
     CL_CK(cudaGetLastError());
     return true;
 }
@@ -701,14 +718,14 @@ bool closure_infer(omx_closure *c, const ClDeploy &D, const EmitArgs &A, cudaStr
     const int n = D.n;
     const int *skip = &D.st->skip_nn;
     k_cl_dep_xh<<<cl_blocks((long long)n * CL_XH), 256, 0, s>>>(D);
+    // gates and GRU cell in one launch: the epilogue turns the permuted gate columns into h
     GemmEpi E = cl_epi(c, n, CL_G);
-    E.d_f32 = D.G;
-    E.ld_f32 = CL_G;
-    E.bias = c->p.p + CL_OFF_BG;
+    E.bias = c->bgp.p;
+    E.gru_h = D.hst;
+    E.gru_hb = D.hb;
     E.skip = skip;
     E.err = D.err;
-    if (!gemm_bf16(D.xh, CL_XH, c->wg.p, CL_XH, CL_XH, E, s, err)) return false;
-    k_cl_gru_fwd<<<cl_blocks((long long)n * CL_H), 256, 0, s>>>(D.G, D.hst, D.hst, D.hb, nullptr, n, skip);
+    if (!gemm_bf16(D.xh, CL_XH, c->wgp.p, CL_XH, CL_XH, E, s, err)) return false;
     const uint16_t *in[3] = {D.hb, D.a1, D.a2};
     uint16_t *out[3] = {D.a1, D.a2, D.a3};
     const uint16_t *w[3] = {c->w1.p, c->w2.p, c->w3.p};
@@ -772,7 +789,8 @@ int omx_closure_create(omx_closure **out)
               c->w1.ensure((size_t)CL_F * CL_H) && c->w1T.ensure((size_t)CL_F * CL_H) &&
               c->w2.ensure((size_t)CL_F * CL_F) && c->w2T.ensure((size_t)CL_F * CL_F) &&
               c->w3.ensure((size_t)CL_F * CL_F) && c->w3T.ensure((size_t)CL_F * CL_F) &&
-              c->w4.ensure((size_t)CL_OUT * CL_F) && c->w4T.ensure((size_t)CL_OUT * CL_F) && c->loss.ensure(1) &&
+              c->w4.ensure((size_t)CL_OUT * CL_F) && c->w4T.ensure((size_t)CL_OUT * CL_F) &&
+              c->wgp.ensure((size_t)CL_G * CL_XH) && c->bgp.ensure(CL_G) && c->loss.ensure(1) &&
               c->err.ensure(1);
     if (ok) ok = cudaMemset(c->p.p, 0, sizeof(float) * CL_NPARAM) == cudaSuccess &&
                  cudaMemset(c->m.p, 0, sizeof(float) * CL_NPARAM) == cudaSuccess &&

@@ -32,6 +32,11 @@ struct GemmEpi {
     int ld_f32, ld_bf16, ld_dtanh;
     int kpz;               // K blocks (of 64) per split (gridDim.z splits)
     const int *skip;       // optional: the whole launch does nothing while *skip != 0
+    // GRU epilogue (gate rows permuted so that the 16 columns of a chunk hold r, z, nx, nh of
+    // four hidden units: column 4u + gate of chunk c in column tile b is unit 32b + 4c + u):
+    // h = (1 - z) tanh(nx + r nh) + z h, written in place to gru_h (row stride 128) and as BF16
+    float *gru_h;
+    uint16_t *gru_hb;
     long long split_stride;
     int act;               // 0 none, 1 tanh, 2 sigmoid, 3 relu
     float alpha;
@@ -138,10 +143,65 @@ __global__ void __launch_bounds__(128, 1) k_gemm_tc(const __grid_constant__ CUte
     if (write) {
         const int row = m0 + warp * 32 + lane;
         float *const dout = E.d_f32 ? E.d_f32 + (long long)blockIdx.z * E.split_stride : nullptr;
+        if (E.gru_h) {
+#pragma unroll 1
+            for (int c0 = 0; c0 < BN; c0 += 16) {
+                float v[16];
+                __syncwarp();              // tcgen05.ld is warp-collective: reconverge first
+                tmem_ld16(taddr + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+                if (row < E.M) {
+                    const long long h0 = (long long)row * 128 + (n0 >> 2) + (c0 >> 2);   // 4 units, 16-byte aligned
+                    const float4 hp = *reinterpret_cast<const float4 *>(E.gru_h + h0);
+                    const float hpv[4] = {hp.x, hp.y, hp.z, hp.w};
+                    float hn[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const int col = n0 + c0 + 4 * u;
+                        const float gr = v[4 * u] + E.bias[col], gz = v[4 * u + 1] + E.bias[col + 1];
+                        const float gx = v[4 * u + 2] + E.bias[col + 2], gh = v[4 * u + 3] + E.bias[col + 3];
+                        const float r = 1.0f / (1.0f + expf(-gr)), z = 1.0f / (1.0f + expf(-gz));
+                        const float nn = tanhf(gx + r * gh);
+                        hn[u] = (1.0f - z) * nn + z * hpv[u];
+                    }
+                    *reinterpret_cast<float4 *>(E.gru_h + h0) = make_float4(hn[0], hn[1], hn[2], hn[3]);
+                    const uint32_t lo = (uint32_t)f32_to_bf16_rn(hn[0]) | ((uint32_t)f32_to_bf16_rn(hn[1]) << 16);
+                    const uint32_t hi = (uint32_t)f32_to_bf16_rn(hn[2]) | ((uint32_t)f32_to_bf16_rn(hn[3]) << 16);
+                    *reinterpret_cast<uint2 *>(E.gru_hb + h0) = make_uint2(lo, hi);
+                }
+            }
+        } else {
 #pragma unroll 1
         for (int c0 = 0; c0 < BN; c0 += 16) {
             float v[16];
+            __syncwarp();                  // tcgen05.ld is warp-collective: reconverge first
             tmem_ld16(taddr + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+            const int cb = n0 + c0;
+            // whole chunk inside the matrix with 16-byte aligned rows: vector stores
+            const bool vec = row < E.M && cb + 16 <= E.N && !E.dtanh && (!dout || (E.ld_f32 % 4) == 0) &&
+                             (!E.d_bf16 || (E.ld_bf16 % 8) == 0);
+            if (vec) {
+#pragma unroll
+                for (int q = 0; q < 16; ++q) {
+                    float x = E.alpha * v[q];
+                    if (E.bias) x += E.bias[cb + q];
+                    v[q] = epi_act(x, E.act);
+                }
+                if (dout) {
+                    float4 *o = reinterpret_cast<float4 *>(dout + (long long)row * E.ld_f32 + cb);
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) o[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+                }
+                if (E.d_bf16) {
+                    uint32_t w[8];
+#pragma unroll
+                    for (int q = 0; q < 8; ++q)
+                        w[q] = (uint32_t)f32_to_bf16_rn(v[2 * q]) | ((uint32_t)f32_to_bf16_rn(v[2 * q + 1]) << 16);
+                    uint4 *o = reinterpret_cast<uint4 *>(E.d_bf16 + (long long)row * E.ld_bf16 + cb);
+                    o[0] = make_uint4(w[0], w[1], w[2], w[3]);
+                    o[1] = make_uint4(w[4], w[5], w[6], w[7]);
+                }
+                continue;
+            }
             if (row < E.M) {
 #pragma unroll
                 for (int q = 0; q < 16; ++q) {
@@ -158,6 +218,7 @@ __global__ void __launch_bounds__(128, 1) k_gemm_tc(const __grid_constant__ CUte
                     if (E.d_bf16) E.d_bf16[(long long)row * E.ld_bf16 + col] = f32_to_bf16_rn(x);
                 }
             }
+        }
         }
     } else if (threadIdx.x == 0) {
         atomicOr(E.err, 2);

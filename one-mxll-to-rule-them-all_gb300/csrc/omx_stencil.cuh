@@ -147,6 +147,7 @@ __device__ __forceinline__ void h3_tile(const FieldPtrs<R> &F, const GridArgs<R>
     const R dt_mu0 = G.dt_mu0, dr = G.dr;
     long long idx = L.off + i + (long long)L.px * j + L.pz * k0;
     R ex_c = Ex[idx], ey_c = Ey[idx];
+#pragma unroll 2   // two planes of loads in flight (the E pass is faster without)
     for (int k = k0; k <= k1; ++k, idx += L.pz) {
         const long long sz = (k == L.nz && G.per[2]) ? (long long)(1 - L.nz) * L.pz : L.pz;
         const R ez_c = Ez[idx], ez_jp = Ez[idx + sy], ez_ip = Ez[idx + sx];

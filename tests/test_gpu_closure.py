@@ -209,3 +209,27 @@ def test_closure_graph_equals_calls_and_check_cadence():
     for a, b in zip(out[0], out[1]):
         assert np.array_equal(a, b)
     assert np.max(np.abs(out[0][0])) > 0
+
+
+def test_closure_deployment_matches_forward():
+    """The deployed network (window ring, GRU state carried across steps, gates and GRU cell in
+    one tensor-core launch) gives the dipoles of omx_closure_forward on the same field history."""
+    deck, g, grp, cl = _deployed(tol=1e30, check_every=1000, frac=0.1, seed=6)
+    par = np.asarray(deck["groups"][0]["params"])
+    u = par[:, -3:]
+    n, T = par.shape[0], 12
+    eu, dip = [], []
+    for tt in range(1, T + 1):
+        g.run(tt, 1, deck["n_skip"], 0, use_graph=True)
+        r = grp.read()
+        eu.append(np.float32((u * r["E"]).sum(1) / E_SCALE))
+        dip.append((u * r["dipole"]).sum(1))
+    B = (n + 7) // 8 * 8
+    e_in = np.zeros((B, T + 31), np.float32)
+    e_in[:n, 31:] = np.stack(eu, axis=1)
+    y = cl.forward(e_in, T)[:, :n] * D_SCALE
+    ref = np.stack(dip, axis=0)
+    assert np.max(np.abs(ref)) > 0
+    assert np.max(np.abs(y - ref)) <= 1e-5 * np.max(np.abs(ref))
+    g.kill()
+    cl.kill()
