@@ -45,6 +45,8 @@ def parse():
     p.add_argument("--impl", default="omx", choices=["omx", "reference"])
     p.add_argument("--config", default="cfg2", choices=["cfg1", "cfg2", "cfg3", "cfg4", "cfg5"])
     p.add_argument("--instances", type=int, default=64, help="cfg5: number of grids in the batched sweep")
+    p.add_argument("--side-min", type=int, default=64, help="cfg5: smallest grid side")
+    p.add_argument("--side-max", type=int, default=256, help="cfg5: largest grid side")
     p.add_argument("--train-steps", type=int, default=300, help="cfg4: Adam steps of the closure training")
     p.add_argument("--trajectories", type=int, default=16384, help="cfg4: training trajectories (plain propagator)")
     p.add_argument("--cpu-seconds", type=float, default=12.0)
@@ -285,7 +287,7 @@ def reference_arm(args, dist):
         return
     if args.config == "cfg5":
         # the sweep's grids are independent: the sample is its smallest grid
-        dks, sides = cfg5_decks(args.instances)
+        dks, sides = cfg5_decks(args.instances, args.side_min, args.side_max)
         k = min(range(len(dks)), key=lambda q: sides[q])
         deck, desc = dks[k], "cfg5 sample: the sweep's smallest grid (side %d) of %d" % (sides[k], len(dks))
     else:
@@ -464,16 +466,16 @@ def gpu_arm(args, dist):
 CFG5_SEED = 20261208
 
 
-def cfg5_decks(count):
+def cfg5_decks(count, side_min=64, side_max=256):
     """The batched inverse-design sweep: `count` cubic 3D grids whose side is drawn per grid,
-    uniformly in [64, 256] (the side, not the volume, is uniform), each with its own seeded
-    binary permittivity map, dipole source and Ez detector."""
+    uniformly in [side_min, side_max] (the side, not the volume, is uniform), each with its own
+    seeded binary permittivity map, dipole source and Ez detector."""
     import numpy as np
 
     from omx import decks
 
     rng = np.random.default_rng(CFG5_SEED)
-    sides = [int(x) for x in rng.integers(64, 257, count)]
+    sides = [int(x) for x in rng.integers(side_min, side_max + 1, count)]
     return [decks.deck_cfg5_instance(n, seed=CFG5_SEED + 1 + k) for k, n in enumerate(sides)], sides
 
 
@@ -484,7 +486,7 @@ def gpu_arm_cfg5(args, dist):
 
     if dist.world > 1:
         omx.select_device(dist.local_rank % max(1, omx.device_count()))
-    dks, sides = cfg5_decks(args.instances)
+    dks, sides = cfg5_decks(args.instances, args.side_min, args.side_max)
     cells = sum(cells_of(d) for d in dks)
     K, W = args.steps, max(3, args.warmup)
     tdp = 1
@@ -544,9 +546,10 @@ def gpu_arm_cfg5(args, dist):
             "metric": METRIC, "value": value, "unit": "Gcell-updates/s", "n_gpus": dist.world, "steps": K,
             "warmup": W, "ms_per_step": t_batch / K * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded decks of the configuration's shape)",
-            "config": {"workload": "cfg5: %d 3D grids, cubic, side uniform in [64, 256] per grid (seed %d), "
+            "config": {"workload": "cfg5: %d 3D grids, cubic, side uniform in [%d, %d] per grid (seed %d), "
                                    "8-cell CPML, binary eps 1 / 12.1 map (fill 0.4) in the central 50%%, "
-                                   "1.55 um dipole source, one Ez detector each" % (len(dks), CFG5_SEED),
+                                   "1.55 um dipole source, one Ez detector each" % (len(dks), args.side_min,
+                                                                                    args.side_max, CFG5_SEED),
                        "cells": cells, "sides": sides, "precision": "fp32",
                        "parallelism": f"replicas x{dist.world}" if dist.world > 1 else "single GPU",
                        "l2": "working set %.1f GB > 126 MB L2, no flush" % (cells * 6 * 4 / 1e9),

@@ -243,6 +243,26 @@ int omx_detectors_record(omx_ctx *ctx, double time);
 int omx_detectors_drain(omx_ctx *ctx, double *times, double *values, int max_records,
                         int *n_records);
 
+/* Batched output (the reference opens, appends and closes every file at every print step,
+ * write_fields_subs_mod.f90:751-1509): drains every record and writes them in the reference's
+ * layout under dir: output_detector_NNNNNNN/point.dat ("time value" lines, appended) and one
+ * F_line_/F_plane_/F_volume_PPPPPPPPP.dat per record with a "# Time" header and one line of
+ * cell coordinates (nm, the reference's i*dr - int(N/2)*dr) and value per point.  *n_records
+ * (may be NULL) receives the number of records written. */
+int omx_detectors_write_text(omx_ctx *ctx, const char *dir, int *n_records);
+/* Running Fourier transforms of every detector sample, accumulated on the device in FP64 at
+ * each record: re/im[k][p] += weight * v_p(t) * (cos, -sin)(omega_k t) (weight: the record
+ * interval for a time integral).  Set up after the detectors are added; read resets nothing. */
+int omx_detectors_dft_setup(omx_ctx *ctx, int n_freq, const double *omega, double weight);
+int omx_detectors_dft_read(omx_ctx *ctx, double *re, double *im);
+/* Electromagnetic energy of the grid, FP64 on the device: 0.5 * dr^dims * sum over the interior
+ * of eps0 |E|^2 + mu0 |H|^2 (vacuum constants; each component on its own staggered cells). */
+int omx_field_energy(omx_ctx *ctx, double *energy);
+/* energy_and_dipole.dat of q-group `group` (output_mod.f90:279-331 layout) under
+ * dir/output_q_group_NNNN/: a "# Time" header and one line per emitter with its energy
+ * Tr(rho H0) in eV and its dipole; append != 0 appends to the file. */
+int omx_qgroup_write_text(omx_ctx *ctx, int group, const char *dir, double time, int append);
+
 /* ---- whole driver loop on the device (mxim_mxll.f90:92-132) --------------------------------- */
 /* Runs steps tt = tt0 .. tt0+nsteps-1 with the reference's ordering: H, sources, E, q-groups
  * on q-steps, detector records every t_det_print steps (0 disables).  n_skip_steps as in

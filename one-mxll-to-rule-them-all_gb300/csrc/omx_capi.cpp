@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <filesystem>
 #include <map>
 #include <memory>
 #include <string>
@@ -168,8 +169,18 @@ struct omx_ctx {
     int inj_n = 0;
     bool j_dirty = false;
     // detectors
-    struct Det { int type, field, nd; };
+    struct Det {
+        int type, field, nd;
+        int first;              // first tap (sample point) of this detector
+        std::vector<int> idx;   // indx_list, nd x dims (column-major, as passed)
+    };
     std::vector<Det> dets;
+    int print_det_step = 0;     // records written by omx_detectors_write_text (file numbering)
+    // running Fourier transforms of the detector samples
+    int n_freq = 0;
+    double dft_w = 0.0;
+    DevBuf<double> d_omega, dft_re, dft_im;
+    DevBuf<double> energy_buf;
     std::vector<int> tap_field, tap_nt;
     std::vector<double> tap_w;
     std::vector<long long> tap[4];
@@ -818,6 +829,11 @@ DetArgs det_args(omx_ctx *c)
     D.t3 = c->d_tap[3].p;
     D.rec = c->rec.p;
     D.times = c->rec_times.p;
+    D.n_freq = c->n_freq;
+    D.omega = c->d_omega.p;
+    D.dft_re = c->dft_re.p;
+    D.dft_im = c->dft_im.p;
+    D.dft_w = c->dft_w;
     return D;
 }
 
@@ -1924,6 +1940,7 @@ int omx_detector_add(omx_ctx *c, int type, int field, int nd, const int32_t *idx
     req(c && idx && nd >= 1, "bad argument");
     c->epoch++;
     req(type >= OMX_POINT_DETECTOR && type <= OMX_VOLUME_DETECTOR, "detector type");
+    req(c->n_freq == 0, "add detectors before omx_detectors_dft_setup");
     req(field >= OMX_EX_FIELD && field <= OMX_HZ_FIELD, "field");
     req(c->field_used[field - 1], "detector field not present in this grid/mode");
     const int dims = c->dims;
@@ -1966,7 +1983,15 @@ int omx_detector_add(omx_ctx *c, int type, int field, int nd, const int32_t *idx
         c->tap_w.push_back(w);
         for (int q = 0; q < 4; ++q) c->tap[q].push_back(t[q]);
     }
-    c->dets.push_back({type, field, nd});
+    {
+        omx_ctx::Det dd;
+        dd.type = type;
+        dd.field = field;
+        dd.nd = nd;
+        dd.first = (int)c->tap_field.size() - nd;
+        dd.idx.assign(idx, idx + (size_t)nd * dims);
+        c->dets.push_back(std::move(dd));
+    }
     c->det_dirty = true;
     if (did) *did = (int)c->dets.size() - 1;
     OMX_API_END(c)
@@ -2020,6 +2045,157 @@ int omx_detectors_drain(omx_ctx *c, double *times, double *values, int max_recor
     }
     c->rec_count -= n;
     *n_records = n;
+    OMX_API_END(c)
+}
+
+int omx_detectors_dft_setup(omx_ctx *c, int n_freq, const double *omega, double weight)
+{
+    OMX_API_BEGIN
+    req(c && n_freq >= 1 && omega, "bad argument");
+    req(!c->tap_field.empty(), "no detectors");
+    c->epoch++;
+    const size_t n = (size_t)n_freq * c->tap_field.size();
+    c->d_omega.upload(std::vector<double>(omega, omega + n_freq));
+    c->dft_re.alloc(n);
+    c->dft_im.alloc(n);
+    c->n_freq = n_freq;
+    c->dft_w = weight;
+    OMX_API_END(c)
+}
+
+int omx_detectors_dft_read(omx_ctx *c, double *re, double *im)
+{
+    OMX_API_BEGIN
+    req(c && re && im, "null argument");
+    req(c->n_freq > 0, "no Fourier transforms set up");
+    sync_checked(c, "dft read");
+    const size_t n = (size_t)c->n_freq * c->tap_field.size();
+    ck(cudaMemcpy(re, c->dft_re.p, n * sizeof(double), cudaMemcpyDeviceToHost), "dft read");
+    ck(cudaMemcpy(im, c->dft_im.p, n * sizeof(double), cudaMemcpyDeviceToHost), "dft read");
+    OMX_API_END(c)
+}
+
+int omx_field_energy(omx_ctx *c, double *energy)
+{
+    OMX_API_BEGIN
+    req(c && energy, "null argument");
+    if (!c->energy_buf.p) c->energy_buf.alloc(305);
+    int used[6];
+    for (int q = 0; q < 6; ++q) used[q] = c->field_used[q] ? 1 : 0;
+    const omx::Consts &K = omx::consts();
+    const double dV = std::pow(c->desc.dr, (double)c->dims);
+    if (c->fp32) launch_field_energy<float>(field_ptrs<float>(c), c->L, used, K.eps0, K.mu0, dV, c->energy_buf.p, c->stream);
+    else launch_field_energy<double>(field_ptrs<double>(c), c->L, used, K.eps0, K.mu0, dV, c->energy_buf.p, c->stream);
+    ck(cudaPeekAtLastError(), "energy");
+    sync_checked(c, "energy");
+    ck(cudaMemcpy(energy, c->energy_buf.p + 304, sizeof(double), cudaMemcpyDeviceToHost), "energy");
+    OMX_API_END(c)
+}
+
+namespace {
+const char *field_name(int f)
+{
+    static const char *n[6] = {"Ex", "Ey", "Ez", "Hx", "Hy", "Hz"};
+    return n[f - 1];
+}
+// cell index -> position in nm, as the reference's writers place a detector cell
+// (write_fields_subs_mod.f90:672-690: i*dr - int(N/2)*dr)
+double cell_nm(const omx_ctx *c, int axis, int i)
+{
+    return ((double)i * c->desc.dr - (double)(c->n[axis] / 2) * c->desc.dr) * omx::consts().au_to_nm;
+}
+}  // namespace
+
+int omx_detectors_write_text(omx_ctx *c, const char *dir, int *n_records)
+{
+    OMX_API_BEGIN
+    req(c && dir, "null argument");
+    sync_checked(c, "write detectors");
+    const int npts = (int)c->tap_field.size();
+    const int n = c->rec_count;
+    std::vector<double> times((size_t)n), vals((size_t)n * std::max(npts, 1));
+    if (n > 0) {
+        ck(cudaMemcpy(times.data(), c->rec_times.p, sizeof(double) * n, cudaMemcpyDeviceToHost), "write detectors");
+        ck(cudaMemcpy(vals.data(), c->rec.p, sizeof(double) * vals.size(), cudaMemcpyDeviceToHost), "write detectors");
+    }
+    namespace fs = std::filesystem;
+    const int dims = c->dims;
+    for (size_t d = 0; d < c->dets.size(); ++d) {
+        const omx_ctx::Det &D = c->dets[d];
+        char sub[64];
+        std::snprintf(sub, sizeof sub, "output_detector_%07d", (int)d + 1);
+        const fs::path dp = fs::path(dir) / sub;
+        std::error_code ec;
+        fs::create_directories(dp, ec);
+        req(!ec, "cannot create " + dp.string());
+        auto idx = [&](int s, int a) { return a < dims ? D.idx[(size_t)a * D.nd + s] : 0; };
+        if (D.type == OMX_POINT_DETECTOR) {
+            // one file, one "time value" line per record (appended)
+            const fs::path fp = dp / "point.dat";
+            FILE *f = std::fopen(fp.string().c_str(), c->print_det_step == 0 ? "w" : "a");
+            req(f != nullptr, "cannot open " + fp.string());
+            for (int r = 0; r < n; ++r)
+                std::fprintf(f, " %24.16E %24.16E\n", times[r], vals[(size_t)r * npts + D.first]);
+            std::fclose(f);
+            continue;
+        }
+        // lines, planes, volumes: one file per record with the reference's header lines
+        const char *kind = D.type <= OMX_LINE_Z_DETECTOR ? "line" : (D.type <= OMX_PLANE_ZX_DETECTOR ? "plane" : "volume");
+        for (int r = 0; r < n; ++r) {
+            char name[64];
+            std::snprintf(name, sizeof name, "%s_%s_%09d.dat", field_name(D.field), kind, c->print_det_step + r);
+            const fs::path fp = dp / name;
+            FILE *f = std::fopen(fp.string().c_str(), "w");
+            req(f != nullptr, "cannot open " + fp.string());
+            std::fprintf(f, "# Time = %18.8E (a.u.)\n", times[r]);
+            for (int s = 0; s < D.nd; ++s) {
+                for (int a = 0; a < dims; ++a) std::fprintf(f, " %24.16E", cell_nm(c, a, idx(s, a)));
+                std::fprintf(f, " %24.16E\n", vals[(size_t)r * npts + D.first + s]);
+            }
+            std::fclose(f);
+        }
+    }
+    c->print_det_step += n;
+    c->rec_count = 0;
+    if (n_records) *n_records = n;
+    OMX_API_END(c)
+}
+
+int omx_qgroup_write_text(omx_ctx *c, int gid, const char *dir, double time, int append)
+{
+    OMX_API_BEGIN
+    req(c && dir, "null argument");
+    req(gid >= 0 && gid < (int)c->groups.size(), "unknown q-group");
+    GroupRec &g = *c->groups[gid];
+    sync_checked(c, "write q-group");
+    const int n = g.d.n_systems;
+    std::vector<double> rho((size_t)n * g.nst), dip((size_t)n * 3), par((size_t)n * g.npar);
+    ck(cudaMemcpy(rho.data(), g.rho.p, rho.size() * sizeof(double), cudaMemcpyDeviceToHost), "write q-group");
+    ck(cudaMemcpy(dip.data(), g.dipole.p, dip.size() * sizeof(double), cudaMemcpyDeviceToHost), "write q-group");
+    ck(cudaMemcpy(par.data(), g.par.p, par.size() * sizeof(double), cudaMemcpyDeviceToHost), "write q-group");
+    namespace fs = std::filesystem;
+    char sub[64];
+    std::snprintf(sub, sizeof sub, "output_q_group_%04d", gid + 1);
+    const fs::path dp = fs::path(dir) / sub;
+    std::error_code ec;
+    fs::create_directories(dp, ec);
+    req(!ec, "cannot create " + dp.string());
+    const fs::path fp = dp / "energy_and_dipole.dat";
+    FILE *f = std::fopen(fp.string().c_str(), append ? "a" : "w");
+    req(f != nullptr, "cannot open " + fp.string());
+    // the reference's block (output_mod.f90:324-331): time header, column header, one line per
+    // emitter; the energy of a few-level emitter is Tr(rho H0) = sum over excited levels
+    std::fprintf(f, "# Time = %18.8E (a.u.)\n", time);
+    std::fprintf(f, "# N_mol        Energy (eV)                   Dipole_x (a.u.)             "
+                    "Dipole_y (a.u.)             Dipole_z (a.u.)\n");
+    const double au_to_ev = (double)27.2114f;
+    for (int e = 0; e < n; ++e) {
+        const double *p = &par[(size_t)e * g.npar], *r = &rho[(size_t)e * g.nst];
+        const double en = g.d.model == OMX_EMITTER_TWO_LEVEL ? p[0] * r[0] : p[0] * r[0] + p[1] * r[1];
+        std::fprintf(f, "%8d %24.16E %24.16E %24.16E %24.16E\n", e + 1, en * au_to_ev, dip[3 * e], dip[3 * e + 1],
+                     dip[3 * e + 2]);
+    }
+    std::fclose(f);
     OMX_API_END(c)
 }
 

@@ -141,6 +141,11 @@ struct DetArgs {
     const long long *t0, *t1, *t2, *t3;
     double *rec;           // [capacity][n]
     double *times;
+    // running Fourier transforms of every sample (FP64): re/im[k][s] += w * v * (cos, -sin)(omega_k t)
+    int n_freq;
+    const double *omega;
+    double *dft_re, *dft_im;
+    double dft_w;
 };
 
 // ---- launchers (instantiated in omx_kernels_fast.cu / omx_kernels_exact.cu) ------------------
@@ -171,6 +176,10 @@ struct Fused2Args {
 void launch_fused_tmz(const Fused2Args &A, const GridArgs<float> &G, int form, void *stream);
 void launch_ade_post(const FieldPtrs<float> &Fin, const FieldPtrs<float> &Fout, const GridArgs<float> &G, void *stream);
 void launch_flush(float *buf, long long n, void *stream);
+// FP64 electromagnetic energy of the interior: 0.5 * dV * sum(eps0 E^2 + mu0 H^2) over the fields
+// present (vacuum constants; each component over its own interior index range)
+template <class R> void launch_field_energy(const FieldPtrs<R> &F, const Lay &L, const int *used, double eps0,
+                                            double mu0, double dV, double *out, void *stream);
 
 // ---- learned closure: plain-propagator work that must round like the q-group kernel ------------
 // training trajectories: per trajectory q, E(t_s) = amp * sum_k c_k cos(w_k t_s + phi_k) with

@@ -98,6 +98,21 @@ void launch_cl_subset_check_reseed(const EmitArgs &A, const ClDeploy &D, void *s
     k_cl_check<<<1, 1, 0, (cudaStream_t)s>>>(D);
     k_cl_reseed<<<(A.n + 31) / 32, 32, 0, (cudaStream_t)s>>>(A, D);
 }
+template <class R>
+void launch_field_energy(const FieldPtrs<R> &F, const Lay &L, const int *used, double eps0, double mu0, double dV,
+                         double *out, void *s)
+{
+    // out[0..303] holds the per-block partials (zeroed here), out[304] the sum
+    constexpr int NB = 304;
+    cudaMemsetAsync(out, 0, sizeof(double) * NB, (cudaStream_t)s);
+    for (int c = 0; c < 6; ++c)
+        if (used[c]) k_field_energy<R><<<NB, 256, 0, (cudaStream_t)s>>>(F, L, c, 0.5 * dV * (c < 3 ? eps0 : mu0), out);
+    k_sum_parts<<<1, 32, 0, (cudaStream_t)s>>>(out, NB, out + NB);
+}
+template void launch_field_energy<float>(const FieldPtrs<float> &, const Lay &, const int *, double, double, double,
+                                         double *, void *);
+template void launch_field_energy<double>(const FieldPtrs<double> &, const Lay &, const int *, double, double, double,
+                                          double *, void *);
 void launch_flush(float *buf, long long n, void *s)
 {
     k_flush<<<152 * 8, 256, 0, (cudaStream_t)s>>>(buf, n);

@@ -187,6 +187,15 @@ __device__ __forceinline__ void sample_point(const FieldPtrs<R> &F, const DetArg
         v = D.w[s] * v;
     }
     D.rec[(long long)slot * D.n + s] = v;
+    if (D.n_freq > 0) {
+        const double t = sp_get(time_p);
+        for (int k = 0; k < D.n_freq; ++k) {
+            double sn, cs;
+            sincos(D.omega[k] * t, &sn, &cs);
+            D.dft_re[(long long)k * D.n + s] += D.dft_w * v * cs;
+            D.dft_im[(long long)k * D.n + s] -= D.dft_w * v * sn;
+        }
+    }
 }
 template <class R>
 __global__ void k_sample(FieldPtrs<R> F, DetArgs D, StepParam slot_p, StepParam time_p)
@@ -376,6 +385,38 @@ __global__ void k_cl_reseed(EmitArgs A, ClDeploy D)
         else rk4r<8>(2, pr, r, E_u, A.dt, A.h2, A.h6, g1, g2);
     }
     for (int q = 0; q < A.nst; ++q) rho[q] = r[q];
+}
+
+// ---- field energy (FP64 reduction, one partial per block, summed in a fixed order) ----------------
+template <class R>
+__global__ void k_field_energy(FieldPtrs<R> F, Lay L, int c, double coef, double *part)
+{
+    __shared__ double sh[256];
+    const long long nx = L.nx, ny = L.dims >= 2 ? L.ny : 1, nz = L.dims == 3 ? L.nz : 1;
+    const long long total = nx * ny * nz;
+    double acc = 0.0;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total;
+         q += (long long)gridDim.x * blockDim.x) {
+        const long long i = 1 + q % nx, j = (L.dims >= 2 ? 1 + (q / nx) % ny : 0), k = (L.dims == 3 ? 1 + q / (nx * ny) : 0);
+        const double v = (double)F.f[c][L.off + i + (long long)L.px * j + L.pz * k];
+        acc += v * v;
+    }
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] += coef * sh[0];
+}
+
+__global__ void k_sum_parts(const double *part, int n, double *out)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        double s = 0.0;
+        for (int q = 0; q < n; ++q) s += part[q];
+        *out = s;
+    }
 }
 
 }  // namespace omx

@@ -98,6 +98,11 @@ class QGroup:
                                                 float(tol), int(check_every)), self.mxll._ctx)
         self._closure = closure                  # the closure must outlive the context
 
+    def write_text(self, directory, time, append=False):
+        """energy_and_dipole.dat of this group in the reference's layout."""
+        A.check(lib().omx_qgroup_write_text(self.mxll._ctx, self.gid, str(directory).encode(), float(time),
+                                            1 if append else 0), self.mxll._ctx)
+
     def closure_status(self):
         err, fb, step, checks = C.c_double(), C.c_int(), C.c_int(), C.c_int()
         A.check(lib().omx_qgroup_closure_status(self.mxll._ctx, self.gid, C.byref(err), C.byref(fb), C.byref(step),
@@ -265,6 +270,29 @@ class TMxll:
         """The reference's time loop (mxim_mxll.f90:92-132) on the device."""
         self._chk(lib().omx_run(self._ctx, int(tt0), int(nsteps), int(n_skip_steps), int(t_det_print),
                                 1 if use_graph else 0))
+
+    def write_detectors_text(self, directory):
+        """Drain the records into the reference's detector file layout; returns the count."""
+        n = C.c_int()
+        self._chk(lib().omx_detectors_write_text(self._ctx, str(directory).encode(), C.byref(n)))
+        return n.value
+
+    def dft_setup(self, omega, weight):
+        om = np.ascontiguousarray(omega, np.float64)
+        self._dft_n = om.size
+        self._chk(lib().omx_detectors_dft_setup(self._ctx, om.size, A.dptr(om), float(weight)))
+
+    def dft_read(self):
+        npts = lib().omx_detectors_total_points(self._ctx)
+        re = np.zeros((self._dft_n, npts))
+        im = np.zeros((self._dft_n, npts))
+        self._chk(lib().omx_detectors_dft_read(self._ctx, A.dptr(re), A.dptr(im)))
+        return re + 1j * im
+
+    def field_energy(self):
+        e = C.c_double()
+        self._chk(lib().omx_field_energy(self._ctx, C.byref(e)))
+        return e.value
 
     def autotune(self, reps=20):
         """Pick this grid's kernel launch shape by timing the candidates on the initial zero

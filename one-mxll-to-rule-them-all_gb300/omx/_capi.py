@@ -104,6 +104,11 @@ SIGNATURES = {
     "omx_detectors_record": (_I, [_VP, _D]),
     "omx_detectors_drain": (_I, [_VP, _PD, _PD, _I, _PI]),
     "omx_run": (_I, [_VP, _I, _I, _I, _I, _I]),
+    "omx_detectors_write_text": (_I, [_VP, C.c_char_p, _PI]),
+    "omx_detectors_dft_setup": (_I, [_VP, _I, _PD, _D]),
+    "omx_detectors_dft_read": (_I, [_VP, _PD, _PD]),
+    "omx_field_energy": (_I, [_VP, _PD]),
+    "omx_qgroup_write_text": (_I, [_VP, _I, C.c_char_p, _D, _I]),
     "omx_autotune": (_I, [_VP, _I, _PI]),
     "omx_batch_create": (_I, [C.POINTER(_VP), _I, C.POINTER(_VP)]),
     "omx_batch_autotune": (_I, [_VP, _I, _PI]),
