@@ -95,6 +95,11 @@ def lib():
             "orc_emitter_step": (None, [C.c_int, _PD, _PD, C.c_double, C.c_double]),
             "orc_sample": (None, [_VP, C.c_int, C.c_int, C.c_int, _P32, _PD]),
             "orc_num_threads": (C.c_int, []),
+            "fd_create": (_VP, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _PI, C.c_double, C.c_double, _PD]),
+            "fd_destroy": (None, [_VP]),
+            "fd_vec_len": (C.c_longlong, [C.c_int, C.c_int, C.c_int, C.c_int]),
+            "fd_apply": (None, [_VP, _PD, _PD, C.c_int]),
+            "fd_bicgstab_l": (C.c_int, [_VP, _PD, _PD, C.c_int, C.c_double, C.c_int, C.c_int, _PI, _PD]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -289,3 +294,47 @@ class Grid:
         out = np.zeros(idx.shape[0])
         lib().orc_sample(self._g, detector_type, field, idx.shape[0], flat.ctypes.data_as(_P32), _d(out))
         return out
+
+
+class FDOperator:
+    """The frequency-domain operator and its BiCGStab(L) solver (fd_oracle.c).  Vectors are
+    complex arrays [6][nz + 2g][ny + 2g][nx + 2g] (components pl_x, pl_y, pl_z, mi_x, mi_y,
+    mi_z; g = n_der ghost cells on every side)."""
+
+    def __init__(self, n, n_pml, n_der, boundaries, dr, w0, eps):
+        self.n, self.g = tuple(n), n_der
+        eps = np.ascontiguousarray(np.asarray(eps, np.complex128).transpose(2, 1, 0))   # x fastest
+        b = np.asarray(boundaries, np.int32)
+        self._h = lib().fd_create(n[0], n[1], n[2], n_pml, n_der, b.ctypes.data_as(_PI), float(dr), float(w0),
+                                  eps.view(np.float64).ctypes.data_as(_PD))
+
+    def shape(self):
+        nx, ny, nz = self.n
+        g = self.g
+        return (6, nz + 2 * g, ny + 2 * g, nx + 2 * g)
+
+    def zeros(self):
+        return np.zeros(self.shape(), np.complex128)
+
+    def apply(self, f, transpose=False):
+        f = np.ascontiguousarray(f, np.complex128).copy()
+        out = self.zeros()
+        lib().fd_apply(self._h, f.view(np.float64).ctypes.data_as(_PD), out.view(np.float64).ctypes.data_as(_PD),
+                       1 if transpose else 0)
+        return out
+
+    def solve(self, j, f0, tol, n_max, L, transpose=False):
+        j = np.ascontiguousarray(j, np.complex128)
+        f = np.ascontiguousarray(f0, np.complex128).copy()
+        conv = C.c_int()
+        err = C.c_double()
+        it = lib().fd_bicgstab_l(self._h, j.view(np.float64).ctypes.data_as(_PD),
+                                 f.view(np.float64).ctypes.data_as(_PD), 1 if transpose else 0, float(tol), int(n_max),
+                                 int(L), C.byref(conv), C.byref(err))
+        return f, bool(conv.value), err.value, it
+
+    def __del__(self):
+        try:
+            lib().fd_destroy(self._h)
+        except Exception:
+            pass
