@@ -43,7 +43,7 @@ def parse():
     p.add_argument("--steps", type=int, default=2000)
     p.add_argument("--warmup", type=int, default=20)
     p.add_argument("--impl", default="omx", choices=["omx", "reference"])
-    p.add_argument("--config", default="cfg2", choices=["cfg1", "cfg2", "cfg3", "cfg4", "cfg5"])
+    p.add_argument("--config", default="cfg2", choices=["cfg1", "cfg2", "cfg3", "cfg4", "cfg5", "fdop"])
     p.add_argument("--instances", type=int, default=64, help="cfg5: number of grids in the batched sweep")
     p.add_argument("--side-min", type=int, default=64, help="cfg5: smallest grid side")
     p.add_argument("--side-max", type=int, default=256, help="cfg5: largest grid side")
@@ -678,6 +678,91 @@ def gpu_arm_cfg4(args, dist):
         print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------------- fdop
+def gpu_arm_fdop(args, dist):
+    """The inverse-design program's frequency-domain operator (FP64 complex stencil, order 4 in
+    each direction) on a 160^3 grid with 8-cell PML and a binary permittivity map, and a
+    BiCGStab(2) solve on a 32^3 grid (permittivity 1 / 2.25 + 0.05i), against the FP64 CPU oracle."""
+    import numpy as np
+
+    import omx
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import build_oracle
+
+    build_oracle.build()
+    import oracle as orc
+
+    if dist.world > 1:
+        omx.select_device(dist.local_rank % max(1, omx.device_count()))
+    rng = np.random.default_rng(CFG5_SEED + 7)
+    n, n_der = (160, 160, 160), 2
+    eps = 1.0 + 11.1 * (rng.random(n) < 0.4) + 0.0j
+    G = omx.FDOperator(n, 8, n_der, (3, 3, 3), 0.05, 2.0 * np.pi / 1.55, eps)
+    reps = max(5, min(args.steps, 200))
+    ms = dist.max(G.time_apply(reps))
+    cells = n[0] * n[1] * n[2]
+    # FP64 operations the kernel executes per cell (6 per complex product, 2 per complex add or
+    # real scaling): 12 (2n+1)-tap derivative sums (4 per tap), 12 stretch products, the three E
+    # sums (6), (eps - C4) C3 (8) and 6 outputs of one difference, three products and two sums (24)
+    taps = 2 * n_der + 1
+    flops = 12 * taps * 4 + 12 * 6 + 6 + 8 + 6 * 24
+    bytes_alg = 16 * (6 + 6 + 1)
+    # CPU oracle on the same operator (bounded sample)
+    O = orc.FDOperator(n, 8, n_der, (3, 3, 3), 0.05, 2.0 * np.pi / 1.55, eps)
+    f = O.zeros()
+    g = n_der
+    f[:, g:-g, g:-g, g:-g] = 1.0 + 0.5j
+    t0 = time.perf_counter()
+    k = 0
+    while True:
+        O.apply(f)
+        k += 1
+        if time.perf_counter() - t0 >= args.cpu_seconds / 2 or k >= 50:
+            break
+    cpu_ms = (time.perf_counter() - t0) / k * 1e3
+    # a solve on a smaller grid, GPU against the oracle
+    ns = (32, 32, 32)
+    eps_s = 1.0 + 1.25 * (rng.random(ns) < 0.4) + 0.05j
+    Gs = omx.FDOperator(ns, 6, n_der, (3, 3, 3), 0.05, 2.0 * np.pi / 1.55, eps_s)
+    Os = orc.FDOperator(ns, 6, n_der, (3, 3, 3), 0.05, 2.0 * np.pi / 1.55, eps_s)
+    j = Gs.zeros()
+    j[:, g:-g, g:-g, g:-g] = rng.normal(size=j[:, g:-g, g:-g, g:-g].shape)
+    t0 = time.perf_counter()
+    fg, cg, eg, ig = Gs.solve(j, Gs.zeros(), 1e-8, 2000, 2)
+    t_gpu = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    fo, co, eo, io = Os.solve(j, Os.zeros(), 1e-8, 2000, 2)
+    t_cpu = time.perf_counter() - t0
+    diff = float(np.linalg.norm(fg - fo) / max(np.linalg.norm(fo), 1e-300))
+    G.kill()
+    Gs.kill()
+    if dist.rank == 0:
+        value = dist.world * cells / (ms / 1e3) / 1e9
+        line = {
+            "metric": "frequency-domain operator applications, Gcell/s (and BiCGStab(2) solve time)",
+            "value": value, "unit": "Gcell-applications/s", "n_gpus": dist.world, "steps": reps, "warmup": 2,
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+            "data": "synthetic (seeded binary permittivity map)",
+            "config": {"workload": "apply_operator_3D on 160^3, n_der 2 (4th order), 8-cell PML, eps 1 / 12.1 "
+                                   "(fill 0.4); BiCGStab(2) to 1e-8 on 32^3, eps 1 / 2.25 + 0.05i", "cells": cells},
+            "roofline": {"bound": "fp64", "kernel": "k_fd_apply", "achieved": flops * cells / (ms / 1e3) / 1e12,
+                         "peak": 1.25, "unit": "TFLOP/s", "frac": flops * cells / (ms / 1e3) / 1e12 / 1.25,
+                         "peak_source": "nominal GB300 FP64 (1.25 TFLOP/s dense, FMA counted as 2)",
+                         "note": "compiled without FMA contraction for bit parity: one flop per FP64 "
+                                 "instruction, so the issue ceiling is half the nominal peak",
+                         "frac_of_no_fma_ceiling": flops * cells / (ms / 1e3) / 1e12 / 0.625, "traffic": None,
+                         "hbm_gbs_algorithmic": bytes_alg * cells / (ms / 1e3) / 1e9},
+            "solve": {"gpu_s": t_gpu, "cpu_oracle_s": t_cpu, "iterations_gpu": ig, "iterations_cpu": io,
+                      "converged": [cg, co], "relative_difference": diff},
+            "cpu_baseline": {"value": cells / (cpu_ms / 1e3) / 1e9, "unit": "Gcell-applications/s",
+                             "cores": 1, "kind": "port",
+                             "sample": f"{k} applications of the C oracle (single-threaded loops)"},
+            "e2e": None, "gpu_launches": reps + 2,
+        }
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     dist = Dist()
@@ -688,6 +773,8 @@ def main():
             gpu_arm_cfg5(args, dist)
         elif args.config == "cfg4":
             gpu_arm_cfg4(args, dist)
+        elif args.config == "fdop":
+            gpu_arm_fdop(args, dist)
         else:
             gpu_arm(args, dist)
     finally:

@@ -381,6 +381,31 @@ int omx_qgroup_attach_closure(omx_ctx *ctx, int group, omx_closure *cl, double c
 int omx_qgroup_closure_status(omx_ctx *ctx, int group, double *last_error, int *fallback,
                               int *fallback_step, int *checks);
 
+/* ---- frequency-domain operator of the inverse-design program ---------------------------------
+ * src/freq_domain_inverse_design/operator_mod.f90: init_operator (:41-232) and
+ * apply_operator_3D (:518-710); bicgstab_mod.f90:76-243: BICGStab_L.  3D, FP64, the program's
+ * units (c0 = eps0 = mu0 = 1).  Vectors are 6 complex components (pl_x, pl_y, pl_z, mi_x, mi_y,
+ * mi_z) over [1-g, n+g] per axis with g = n_der ghost cells, x fastest, as interleaved (re, im)
+ * doubles: omx_fd_vector_length complex values.  eps_r: nx*ny*nz complex values, x fastest.
+ * boundaries: 1 close, 2 periodic (the reference's ghost copies, including its y-axis copies of
+ * mi_x into the low ghosts only and mi_y into the high ghosts only), 3 PML (n_pml cells). */
+typedef struct omx_fdop omx_fdop;
+int omx_fd_create(const int grid_Ndims[3], int n_pml, int n_der, const int boundaries[3], double dr, double w0,
+                  const double *eps_r, omx_fdop **out);
+int omx_fd_destroy(omx_fdop *op);
+/* replace eps_r (the design's permittivity after an optimisation step; the reference passes its
+ * TMedium_eps_r to every apply_operator / BICGStab_L call) */
+int omx_fd_set_eps(omx_fdop *op, const double *eps_r);
+long long omx_fd_vector_length(const omx_fdop *op);
+/* Af = A f (transpose != 0: the adjoint form, C1 negated); f's periodic ghosts are refreshed */
+int omx_fd_apply(omx_fdop *op, const double *f, double *Af, int transpose);
+/* BiCGStab(L) for A f = j from the guess in f (solution returned in f); converged, the final
+ * relative residual |r| / |j| and the outer iteration count are returned */
+int omx_fd_solve(omx_fdop *op, const double *j, double *f, int transpose, double tol, int n_max, int L,
+                 int *converged, double *abs_err, int *iterations);
+/* measurement: mean time of reps applications on device-resident vectors (CUDA events) */
+int omx_fd_time_apply(omx_fdop *op, int reps, double *ms_per_apply);
+
 #ifdef __cplusplus
 }
 #endif

@@ -42,6 +42,8 @@ def _jobs():
                                                            "-o", os.path.join(BUILD, "noalloc.o")],
         [nvcc] + ARCH + common + inc + ["-c", os.path.join(CSRC, "omx_closure.cu"),
                                         "-o", os.path.join(BUILD, "closure.o")],
+        [nvcc] + ARCH + common + ["-fmad=false"] + inc + ["-c", os.path.join(CSRC, "omx_fd.cu"),
+                                                           "-o", os.path.join(BUILD, "fd.o")],
     ]
     for name in ("omx_capi", "omx_host"):
         jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-I", _cuda_include(), "-I", CSRC,
@@ -76,7 +78,7 @@ def build(force=False, verbose=False):
         for log in logs:
             if log.strip():
                 print(log)
-    objs = [os.path.join(BUILD, n) for n in ("exact.o", "fast.o", "noalloc.o", "closure.o", "omx_capi.o",
+    objs = [os.path.join(BUILD, n) for n in ("exact.o", "fast.o", "noalloc.o", "closure.o", "fd.o", "omx_capi.o",
                                               "omx_host.o")]
     tmp = OUT + ".tmp"
     run([_nvcc()] + ARCH + ["-shared", "-Xcompiler", "-fPIC", "-o", tmp] + objs)

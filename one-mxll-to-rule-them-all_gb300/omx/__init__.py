@@ -485,3 +485,62 @@ class Closure:
             self.kill()
         except Exception:
             pass
+
+
+class FDOperator:
+    """The frequency-domain operator of the inverse-design program and its BiCGStab(L) solver
+    (omx_fd_*).  Vectors: complex arrays [6][nz + 2g][ny + 2g][nx + 2g], g = n_der."""
+
+    def __init__(self, n, n_pml, n_der, boundaries, dr, w0, eps):
+        self.n, self.g = tuple(int(v) for v in n), int(n_der)
+        e = np.ascontiguousarray(np.asarray(eps, np.complex128).transpose(2, 1, 0))
+        nn = (C.c_int * 3)(*self.n)
+        bb = (C.c_int * 3)(*[int(b) for b in boundaries])
+        self._op = C.c_void_p()
+        A.check(lib().omx_fd_create(nn, int(n_pml), int(n_der), bb, float(dr), float(w0),
+                                    e.view(np.float64).ctypes.data_as(A._PD), C.byref(self._op)))
+
+    def shape(self):
+        nx, ny, nz = self.n
+        g = self.g
+        return (6, nz + 2 * g, ny + 2 * g, nx + 2 * g)
+
+    def zeros(self):
+        return np.zeros(self.shape(), np.complex128)
+
+    def apply(self, f, transpose=False):
+        f = np.ascontiguousarray(f, np.complex128)
+        out = self.zeros()
+        A.check(lib().omx_fd_apply(self._op, f.view(np.float64).ctypes.data_as(A._PD),
+                                   out.view(np.float64).ctypes.data_as(A._PD), 1 if transpose else 0))
+        return out
+
+    def solve(self, j, f0, tol, n_max, L, transpose=False):
+        j = np.ascontiguousarray(j, np.complex128)
+        f = np.ascontiguousarray(f0, np.complex128).copy()
+        conv, err, it = C.c_int(), C.c_double(), C.c_int()
+        A.check(lib().omx_fd_solve(self._op, j.view(np.float64).ctypes.data_as(A._PD),
+                                   f.view(np.float64).ctypes.data_as(A._PD), 1 if transpose else 0, float(tol),
+                                   int(n_max), int(L), C.byref(conv), C.byref(err), C.byref(it)))
+        return f, bool(conv.value), err.value, it.value
+
+    def set_eps(self, eps):
+        e = np.ascontiguousarray(np.asarray(eps, np.complex128).transpose(2, 1, 0))
+        assert e.shape == self.n[::-1]
+        A.check(lib().omx_fd_set_eps(self._op, e.view(np.float64).ctypes.data_as(A._PD)))
+
+    def time_apply(self, reps=20):
+        ms = C.c_double()
+        A.check(lib().omx_fd_time_apply(self._op, int(reps), C.byref(ms)))
+        return ms.value
+
+    def kill(self):
+        if self._op:
+            lib().omx_fd_destroy(self._op)
+            self._op = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.kill()
+        except Exception:
+            pass
