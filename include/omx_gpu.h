@@ -242,6 +242,16 @@ int omx_detectors_record(omx_ctx *ctx, double time);
 /* copy out and clear the recorded samples: times[n_rec], values[n_rec x total_points] */
 int omx_detectors_drain(omx_ctx *ctx, double *times, double *values, int max_records,
                         int *n_records);
+/* Asynchronous drain (the device ring buffer feeding the host writers without a stall): enqueue
+ * the copy of every recorded sample into one of OMX_DRAIN_SLOTS pinned slots owned by the
+ * library, clear the device records and return at once with a ticket; later steps may be
+ * launched right away.  omx_detectors_collect waits for that ticket's copy and hands its records
+ * to the caller (times[n_rec], values[n_rec x total_points]; max_records must cover them) and
+ * frees the slot.  OMX_ERR_STATE when every slot holds an uncollected ticket. */
+#define OMX_DRAIN_SLOTS 4
+int omx_detectors_drain_async(omx_ctx *ctx, long long *ticket);
+int omx_detectors_collect(omx_ctx *ctx, long long ticket, double *times, double *values, int max_records,
+                          int *n_records);
 
 /* Batched output (the reference opens, appends and closes every file at every print step,
  * write_fields_subs_mod.f90:751-1509): drains every record and writes them in the reference's

@@ -208,6 +208,21 @@ struct omx_ctx {
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     DevBuf<int> d_step2;
+    // a one-step omx_run leaves its side-stream work running (ev_join marks its end) so that the
+    // next call's fused pass overlaps it; every other entry point first orders the main stream
+    // after it (join_side)
+    bool side_pending = false;
+    // asynchronous detector drains: a ring of pinned slots, each filled by copies on the stream
+    // and marked by an event; omx_detectors_collect hands a slot's records to the caller
+    struct DrainSlot {
+        double *h = nullptr;   // times then values
+        size_t cap = 0;        // doubles
+        int *err = nullptr;    // copy of the kernel error word taken with the records
+        int n = 0;
+        long long ticket = -1;  // -1: free
+        cudaEvent_t ev = nullptr;
+    } drain_slots[OMX_DRAIN_SLOTS];
+    long long next_ticket = 0;
     DevBuf<float> rowc;    // packed per-row y coefficients of the fused FP32 TMz kernel
     DevBuf<int> d_err;     // kernel error word (bit 0: a bulk-copy wait of the fused kernel ran out)
     int *h_err = nullptr;  // pinned host copy of it, read at every synchronisation
@@ -249,6 +264,8 @@ struct omx_ctx {
 };
 
 namespace {
+
+void join_side(omx_ctx *c);
 
 int set_err(omx_ctx *ctx, const Fail &f)
 {
@@ -797,6 +814,7 @@ void ensure_rec_capacity(omx_ctx *c, int need)
 {
     const int npts = (int)c->tap_field.size();
     if (need <= c->rec_capacity) return;
+    join_side(c);   // records of a pending side sequence are copied below
     c->epoch++;
     int cap = std::max(need, c->rec_capacity * 2);
     DevBuf<double> nrec, ntim;
@@ -1044,9 +1062,19 @@ template <> void fused_step<float>(omx_ctx *c)
     c->cur = out;
 }
 
+// Order the main stream after the side-stream work a one-step omx_run left running.
+void join_side(omx_ctx *c)
+{
+    if (c && c->side_pending) {
+        ck(cudaStreamWaitEvent(c->stream, c->ev_join, 0), "join");
+        c->side_pending = false;
+    }
+}
+
 // Synchronise the stream and report a failure that a kernel recorded in the error word.
 void sync_checked(omx_ctx *c, const char *what)
 {
+    join_side(c);
     ck(cudaMemcpyAsync(c->h_err, c->d_err.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream), what);
     ck(cudaStreamSynchronize(c->stream), what);
     if (*c->h_err) {
@@ -1083,8 +1111,28 @@ struct RunPlan {
     int W = 0;
     bool has_det = false;
     int nrec = 0;
+    size_t need = 0;
+    omx_ctx::HostStage *stage = nullptr;
 };
-RunPlan stage_run(omx_ctx *c, int tt0, int nsteps, int n_skip, int t_det_print)
+// The device side of the staging: the table copy and the step counters.  first_counted: the
+// step's first kernel already ran without a counter, so the main counter starts at step 0.
+void stage_upload(omx_ctx *c, const RunPlan &plan, bool first_counted)
+{
+    if (plan.need > c->tab.n) {
+        c->tab.alloc(std::max(plan.need, 2 * c->tab.n), false);
+        c->epoch++;
+    }
+    ck(cudaMemcpyAsync(c->tab.p, plan.stage->p, plan.need * sizeof(double), cudaMemcpyHostToDevice, c->stream),
+       "tab");
+    ck(cudaEventRecord(plan.stage->ev, c->stream), "staging");
+    if (!c->d_step.p) c->d_step.alloc(1);
+    // the first kernel of every step advances the counter, so it starts one below step 0
+    ck(cudaMemsetAsync(c->d_step.p, first_counted ? 0x00 : 0xff, sizeof(int), c->stream), "step");
+    if (!c->d_step2.p) c->d_step2.alloc(1);
+    ck(cudaMemsetAsync(c->d_step2.p, 0xff, sizeof(int), c->stream), "step");
+    c->run_step = c->d_step.p;
+}
+RunPlan stage_run(omx_ctx *c, int tt0, int nsteps, int n_skip, int t_det_print, bool upload = true)
 {
     prepare(c);
     const int nsrc = (int)c->sources.size();
@@ -1126,22 +1174,13 @@ RunPlan stage_run(omx_ctx *c, int tt0, int nsteps, int n_skip, int t_det_print)
         for (int q = 0; q < nsrc; ++q) row[4 + q] = source_amp(*c->sources[q], time);
     }
     if (has_det) ensure_rec_capacity(c, c->rec_count + nrec);
-    if (need > c->tab.n) {
-        c->tab.alloc(std::max(need, 2 * c->tab.n), false);
-        c->epoch++;
-    }
-    ck(cudaMemcpyAsync(c->tab.p, tab, need * sizeof(double), cudaMemcpyHostToDevice, c->stream), "tab");
-    ck(cudaEventRecord(hs.ev, c->stream), "staging");
-    if (!c->d_step.p) c->d_step.alloc(1);
-    // the first kernel of every step advances the counter, so it starts one below step 0
-    ck(cudaMemsetAsync(c->d_step.p, 0xff, sizeof(int), c->stream), "step");
-    if (!c->d_step2.p) c->d_step2.alloc(1);
-    ck(cudaMemsetAsync(c->d_step2.p, 0xff, sizeof(int), c->stream), "step");
-    c->run_step = c->d_step.p;
     RunPlan plan;
     plan.W = W;
     plan.has_det = has_det;
     plan.nrec = nrec;
+    plan.need = need;
+    plan.stage = &hs;
+    if (upload) stage_upload(c, plan, false);
     return plan;
 }
 
@@ -1149,7 +1188,11 @@ StepParam plan_param(omx_ctx *c, const RunPlan &plan, int row) { return StepPara
 
 template <class R> void run_impl(omx_ctx *c, int tt0, int nsteps, int n_skip, int t_det_print, int use_graph)
 {
-    const RunPlan plan = stage_run(c, tt0, nsteps, n_skip, t_det_print);
+    // a configuration change, or anything but a one-step graph call, first waits for the side
+    // sequence a previous one-step call left running
+    if (c->j_dirty || c->det_dirty || c->fused_dirty || !c->started || nsteps != 1 || !use_graph || c->prof)
+        join_side(c);
+    const RunPlan plan = stage_run(c, tt0, nsteps, n_skip, t_det_print, false);
     struct Reset {
         omx_ctx *c;
         ~Reset() { c->run_step = nullptr; }
@@ -1159,9 +1202,39 @@ template <class R> void run_impl(omx_ctx *c, int tt0, int nsteps, int n_skip, in
     const int nrec = plan.nrec;
     const int nsrc = (int)c->sources.size();
     auto P = [&](int row) { return StepParam{0.0, c->tab.p + row, c->d_step.p, W}; };
+    auto P2 = [&](int row) { return StepParam{0.0, c->tab.p + row, c->d_step2.p, W}; };
+    const bool fused = std::is_same<R, float>::value && c->fused_ok;
+    // One step per call on the fused path (a host that drives the loop step by step): the step's
+    // scalars go to the kernels as arguments (no table upload), the fused pass reads only the
+    // field buffers, so it is launched before the wait on the previous call's side sequence and
+    // overlaps it; the sources, the emitter current and this step's own side sequence follow,
+    // and the side sequence is left running for the next call (every other entry point joins it
+    // first; an asynchronous drain queues its copies behind it).  Same operations on the same
+    // values as the graph schedule.
+    if (fused && nsteps == 1 && use_graph && !c->prof && (has_det || !c->groups.empty())) {
+        const double *row = plan.stage->p;    // this step's table row, on the host
+        fused_step<R>(c);
+        join_side(c);
+        std::vector<StepParam> amps;
+        for (int q = 0; q < nsrc; ++q) amps.push_back(imm(row[4 + q]));
+        do_sources<R>(c, amps);
+        do_inject<R>(c, imm(row[0]), imm(row[1]));
+        ck(cudaEventRecord(c->ev_fork, c->stream), "fork");
+        ck(cudaStreamWaitEvent(c->side, c->ev_fork, 0), "fork");
+        std::swap(c->stream, c->side);
+        if (has_det) do_sample<R>(c, imm(row[3]), imm(row[0]));
+        for (auto &g : c->groups) do_group<R>(c, *g, imm(row[2]));
+        std::swap(c->stream, c->side);
+        ck(cudaEventRecord(c->ev_join, c->side), "join");
+        c->side_pending = true;
+        ck(cudaPeekAtLastError(), "launch");
+        c->rec_count += nrec;
+        return;
+    }
+    join_side(c);
+    stage_upload(c, plan, false);
     std::vector<StepParam> amps;
     for (int q = 0; q < nsrc; ++q) amps.push_back(P(4 + q));
-    const bool fused = std::is_same<R, float>::value && c->fused_ok;
     auto tail = [&]() {
         for (auto &g : c->groups) do_group<R>(c, *g, P(2));
         if (has_det) do_sample<R>(c, P(3), P(0));
@@ -1184,7 +1257,6 @@ template <class R> void run_impl(omx_ctx *c, int tt0, int nsteps, int n_skip, in
     // of step s+1 waits for step s's scatter.  Sampling goes first on the side stream, so that
     // the wait on the scatter also orders it before the pass that overwrites its buffer set.
     // Same operations on the same values as one_step: results are identical.
-    auto P2 = [&](int row) { return StepParam{0.0, c->tab.p + row, c->d_step2.p, W}; };
     auto overlapped_step = [&](bool wait_prev) {
         fused_step<R>(c);
         do_sources<R>(c, amps);
@@ -1490,6 +1562,7 @@ int omx_create(const omx_grid_desc *d, omx_ctx **out)
 int omx_destroy(omx_ctx *c)
 {
     if (!c) return OMX_OK;
+    if (c->side) cudaStreamSynchronize(c->side);
     if (c->stream) cudaStreamSynchronize(c->stream);
     for (auto &e : c->evs) {
         cudaEventDestroy(e.a);
@@ -1509,6 +1582,11 @@ int omx_destroy(omx_ctx *c)
     }
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     if (c->ev_join) cudaEventDestroy(c->ev_join);
+    for (auto &d : c->drain_slots) {
+        if (d.h) cudaFreeHost(d.h);
+        if (d.err) cudaFreeHost(d.err);
+        if (d.ev) cudaEventDestroy(d.ev);
+    }
     cudaStream_t s = c->stream;
     delete c;
     if (s) cudaStreamDestroy(s);
@@ -1518,6 +1596,7 @@ int omx_destroy(omx_ctx *c)
 int omx_synchronize(omx_ctx *c)
 {
     OMX_API_BEGIN
+    join_side(c);
     req(c, "null context");
     sync_checked(c, "synchronize");
     OMX_API_END(c)
@@ -1567,6 +1646,7 @@ int omx_set_cpml_tables(omx_ctx *c, const double *be, const double *ce, const do
                         const double *dhy, const double *dhz)
 {
     OMX_API_BEGIN
+    join_side(c);
     req(c, "null context");
     c->epoch++;
     req(!c->started, "tables must be set before the first step", OMX_ERR_STATE);
@@ -1592,6 +1672,7 @@ int omx_set_media(omx_ctx *c, int n_media, const omx_medium *media, const int32_
                   const double *ey, const double *ez)
 {
     OMX_API_BEGIN
+    join_side(c);
     req(c, "null context");
     c->epoch++;
     req(!c->started, "media must be set before the first step", OMX_ERR_STATE);
@@ -1658,6 +1739,7 @@ int omx_media_map_from_voxels(int dims, const int grid_Ndims[3], double dr, int 
 int omx_step_H(omx_ctx *c)
 {
     OMX_API_BEGIN
+    join_side(c);
     req(c, "null context");
     prepare(c);
     if (c->fp32) do_H<float>(c);
@@ -1669,6 +1751,7 @@ int omx_step_H(omx_ctx *c)
 int omx_step_E(omx_ctx *c, double time, double t_skip)
 {
     OMX_API_BEGIN
+    join_side(c);
     req(c, "null context");
     prepare(c);
     if (c->fp32) do_E<float>(c, imm(time), imm(t_skip));
@@ -1680,6 +1763,7 @@ int omx_step_E(omx_ctx *c, double time, double t_skip)
 int omx_source_add(omx_ctx *c, const omx_source_desc *d, int *id)
 {
     OMX_API_BEGIN
+    join_side(c);
     req(c && d, "null argument");
     c->epoch++;
     req(d->dir == 'x' || d->dir == 'y' || d->dir == 'z', "source direction must be x, y or z");
@@ -1735,6 +1819,7 @@ int omx_source_add(omx_ctx *c, const omx_source_desc *d, int *id)
 int omx_plane_source_add(omx_ctx *c, const omx_plane_source_desc *d, int *id)
 {
     OMX_API_BEGIN
+    join_side(c);
     req(c && d, "null argument");
     c->epoch++;
     req(d->comp >= 1 && d->comp <= 3 && d->plane_axis >= 1 && d->plane_axis <= c->dims, "plane source axis/comp");
@@ -1756,6 +1841,7 @@ int omx_plane_source_add(omx_ctx *c, const omx_plane_source_desc *d, int *id)
 int omx_source_interactions(omx_ctx *c, double time)
 {
     OMX_API_BEGIN
+    join_side(c);
     req(c, "null context");
     prepare(c);
     std::vector<StepParam> amps;
@@ -1771,6 +1857,7 @@ int omx_qgroup_state_size(int model) { return model == OMX_EMITTER_TWO_LEVEL ? 3
 int omx_qgroup_create(omx_ctx *c, const omx_qgroup_desc *d, const int32_t *cell, const double *params, int *gid)
 {
     OMX_API_BEGIN
+    join_side(c);
     req(c && d && cell && params, "null argument");
     c->epoch++;
     req(!c->started, "q-groups must be created before the first step", OMX_ERR_STATE);
@@ -1840,6 +1927,7 @@ int omx_qgroup_create(omx_ctx *c, const omx_qgroup_desc *d, const int32_t *cell,
 int omx_qgroup_step(omx_ctx *c, int gid, int tq_step)
 {
     OMX_API_BEGIN
+    join_side(c);
     (void)tq_step;
     req(c && gid >= 0 && gid < (int)c->groups.size(), "bad group id");
     prepare(c);
@@ -1853,6 +1941,7 @@ int omx_qgroup_attach_closure(omx_ctx *c, int gid, omx_closure *cl, double check
                               int check_every)
 {
     OMX_API_BEGIN
+    join_side(c);
     req(c && cl, "null argument");
     c->epoch++;
     req(gid >= 0 && gid < (int)c->groups.size(), "unknown q-group");
@@ -1908,6 +1997,7 @@ int omx_qgroup_closure_status(omx_ctx *c, int gid, double *last_error, int *fall
                               int *checks)
 {
     OMX_API_BEGIN
+    join_side(c);
     req(c, "null context");
     req(gid >= 0 && gid < (int)c->groups.size() && c->groups[gid]->cl, "q-group without a closure");
     sync_checked(c, "closure status");
@@ -1923,6 +2013,7 @@ int omx_qgroup_closure_status(omx_ctx *c, int gid, double *last_error, int *fall
 int omx_qgroup_read(omx_ctx *c, int gid, double *dipole, double *dPdt, double *efield, double *rho)
 {
     OMX_API_BEGIN
+    join_side(c);
     req(c && gid >= 0 && gid < (int)c->groups.size(), "bad group id");
     GroupRec &g = *c->groups[gid];
     ck(cudaStreamSynchronize(c->stream), "sync");
@@ -1937,6 +2028,7 @@ int omx_qgroup_read(omx_ctx *c, int gid, double *dipole, double *dPdt, double *e
 int omx_detector_add(omx_ctx *c, int type, int field, int nd, const int32_t *idx, int *did)
 {
     OMX_API_BEGIN
+    join_side(c);
     req(c && idx && nd >= 1, "bad argument");
     c->epoch++;
     req(type >= OMX_POINT_DETECTOR && type <= OMX_VOLUME_DETECTOR, "detector type");
@@ -2002,6 +2094,7 @@ int omx_detectors_total_points(const omx_ctx *c) { return c ? (int)c->tap_field.
 int omx_detectors_set_capacity(omx_ctx *c, int records)
 {
     OMX_API_BEGIN
+    join_side(c);
     req(c && records >= 1, "bad argument");
     c->epoch++;
     prepare(c);
@@ -2012,6 +2105,7 @@ int omx_detectors_set_capacity(omx_ctx *c, int records)
 int omx_detectors_record(omx_ctx *c, double time)
 {
     OMX_API_BEGIN
+    join_side(c);
     req(c, "null context");
     req(!c->tap_field.empty(), "no detectors");
     prepare(c);
@@ -2026,6 +2120,7 @@ int omx_detectors_record(omx_ctx *c, double time)
 int omx_detectors_drain(omx_ctx *c, double *times, double *values, int max_records, int *n_records)
 {
     OMX_API_BEGIN
+    join_side(c);
     req(c && n_records, "null argument");
     sync_checked(c, "sync");
     const int npts = (int)c->tap_field.size();
@@ -2048,9 +2143,82 @@ int omx_detectors_drain(omx_ctx *c, double *times, double *values, int max_recor
     OMX_API_END(c)
 }
 
+int omx_detectors_drain_async(omx_ctx *c, long long *ticket)
+{
+    OMX_API_BEGIN
+    req(c && ticket, "null argument");
+    // behind a pending side sequence (which wrote the records) the copies go on the side stream,
+    // so the main stream's next step does not wait for them
+    const cudaStream_t st = c->side_pending ? c->side : c->stream;
+    omx_ctx::DrainSlot *d = nullptr;
+    for (auto &q : c->drain_slots)
+        if (q.ticket < 0) {
+            d = &q;
+            break;
+        }
+    if (!d) throw Fail{OMX_ERR_STATE, "every drain slot holds an uncollected ticket"};
+    const int npts = (int)c->tap_field.size();
+    const int n = c->rec_count;
+    const size_t need = (size_t)n * (1 + npts);
+    if (!d->ev) ck(cudaEventCreateWithFlags(&d->ev, cudaEventDisableTiming), "event");
+    if (!d->err) ck(cudaMallocHost(&d->err, sizeof(int)), "pinned drain");
+    if (d->cap < need) {
+        if (d->h) cudaFreeHost(d->h);
+        d->h = nullptr;
+        d->cap = 0;
+        ck(cudaMallocHost(&d->h, std::max<size_t>(need, 64) * sizeof(double)), "pinned drain");
+        d->cap = std::max<size_t>(need, 64);
+    }
+    if (n > 0) {
+        ck(cudaMemcpyAsync(d->h, c->rec_times.p, sizeof(double) * n, cudaMemcpyDeviceToHost, st), "drain");
+        ck(cudaMemcpyAsync(d->h + n, c->rec.p, sizeof(double) * (size_t)n * npts, cudaMemcpyDeviceToHost, st),
+           "drain");
+    }
+    ck(cudaMemcpyAsync(d->err, c->d_err.p, sizeof(int), cudaMemcpyDeviceToHost, st), "drain");
+    ck(cudaEventRecord(d->ev, st), "drain");
+    if (c->side_pending) ck(cudaEventRecord(c->ev_join, c->side), "join");   // the side sequence now ends here
+    // the records are taken: later steps write from slot 0 again (stream order keeps the copy first)
+    c->rec_count = 0;
+    d->n = n;
+    d->ticket = c->next_ticket++;
+    *ticket = d->ticket;
+    OMX_API_END(c)
+}
+
+int omx_detectors_collect(omx_ctx *c, long long ticket, double *times, double *values, int max_records,
+                          int *n_records)
+{
+    OMX_API_BEGIN
+    // waits on the ticket's own event only: no join, so a pending side sequence keeps running
+    // next to the main stream's next step
+    req(c && n_records, "null argument");
+    omx_ctx::DrainSlot *d = nullptr;
+    for (auto &q : c->drain_slots)
+        if (q.ticket == ticket && ticket >= 0) d = &q;
+    req(d != nullptr, "unknown or already collected ticket");
+    ck(cudaEventSynchronize(d->ev), "collect");
+    const int n = d->n;
+    const int err = *d->err;
+    d->ticket = -1;
+    if (err) {
+        join_side(c);
+        ck(cudaMemsetAsync(c->d_err.p, 0, sizeof(int), c->stream), "collect");
+        throw Fail{OMX_ERR_CUDA, "fused TMz kernel: a bulk-copy wait ran out; the fields of that step are invalid"};
+    }
+    req(max_records >= n, "max_records is smaller than the ticket's record count");
+    const int npts = (int)c->tap_field.size();
+    if (n > 0) {
+        if (times) std::memcpy(times, d->h, sizeof(double) * n);
+        if (values) std::memcpy(values, d->h + n, sizeof(double) * (size_t)n * npts);
+    }
+    *n_records = n;
+    OMX_API_END(c)
+}
+
 int omx_detectors_dft_setup(omx_ctx *c, int n_freq, const double *omega, double weight)
 {
     OMX_API_BEGIN
+    join_side(c);
     req(c && n_freq >= 1 && omega, "bad argument");
     req(!c->tap_field.empty(), "no detectors");
     c->epoch++;
@@ -2066,6 +2234,7 @@ int omx_detectors_dft_setup(omx_ctx *c, int n_freq, const double *omega, double 
 int omx_detectors_dft_read(omx_ctx *c, double *re, double *im)
 {
     OMX_API_BEGIN
+    join_side(c);
     req(c && re && im, "null argument");
     req(c->n_freq > 0, "no Fourier transforms set up");
     sync_checked(c, "dft read");
@@ -2078,6 +2247,7 @@ int omx_detectors_dft_read(omx_ctx *c, double *re, double *im)
 int omx_field_energy(omx_ctx *c, double *energy)
 {
     OMX_API_BEGIN
+    join_side(c);
     req(c && energy, "null argument");
     if (!c->energy_buf.p) c->energy_buf.alloc(305);
     int used[6];
@@ -2109,6 +2279,7 @@ double cell_nm(const omx_ctx *c, int axis, int i)
 int omx_detectors_write_text(omx_ctx *c, const char *dir, int *n_records)
 {
     OMX_API_BEGIN
+    join_side(c);
     req(c && dir, "null argument");
     sync_checked(c, "write detectors");
     const int npts = (int)c->tap_field.size();
@@ -2164,6 +2335,7 @@ int omx_detectors_write_text(omx_ctx *c, const char *dir, int *n_records)
 int omx_qgroup_write_text(omx_ctx *c, int gid, const char *dir, double time, int append)
 {
     OMX_API_BEGIN
+    join_side(c);
     req(c && dir, "null argument");
     req(gid >= 0 && gid < (int)c->groups.size(), "unknown q-group");
     GroupRec &g = *c->groups[gid];
@@ -2212,6 +2384,7 @@ int omx_run(omx_ctx *c, int tt0, int nsteps, int n_skip_steps, int t_det_print, 
 int omx_autotune(omx_ctx *c, int reps, int *choice)
 {
     OMX_API_BEGIN
+    join_side(c);
     req(c && reps >= 1, "bad argument");
     req(!c->started && !c->fields_written,
         "omx_autotune times kernels on the initial zero fields: call it after the grid is configured and "
@@ -2367,6 +2540,7 @@ struct BatchStreams {
     std::vector<cudaStream_t> saved;
     explicit BatchStreams(omx_batch *bb) : b(bb)
     {
+        for (auto *c : b->ctx) join_side(c);
         for (auto *c : b->ctx) ck(cudaStreamSynchronize(c->stream), "sync");
         for (auto *c : b->ctx) {
             saved.push_back(c->stream);
@@ -2587,6 +2761,7 @@ int omx_field_bounds(const omx_ctx *c, int field, int lo[3], int hi[3])
 int omx_read_field(omx_ctx *c, int field, double *host)
 {
     OMX_API_BEGIN
+    join_side(c);
     req(c && host, "null argument");
     if (c->fp32) read_field_impl<float>(c, field, host);
     else read_field_impl<double>(c, field, host);
@@ -2596,6 +2771,7 @@ int omx_read_field(omx_ctx *c, int field, double *host)
 int omx_write_field(omx_ctx *c, int field, const double *host)
 {
     OMX_API_BEGIN
+    join_side(c);
     req(c && host, "null argument");
     c->fields_written = true;
     if (c->fp32) write_field_impl<float>(c, field, host);
@@ -2606,6 +2782,7 @@ int omx_write_field(omx_ctx *c, int field, const double *host)
 int omx_profile_enable(omx_ctx *c, int on)
 {
     OMX_API_BEGIN
+    join_side(c);
     req(c, "null context");
     c->epoch++;
     prof_collect(c);
@@ -2620,6 +2797,7 @@ int omx_profile_enable(omx_ctx *c, int on)
 int omx_profile_query(omx_ctx *c, int kc, double *total_ms, long long *launches)
 {
     OMX_API_BEGIN
+    join_side(c);
     req(c && kc >= 0 && kc < KC_N, "bad argument");
     prof_collect(c);
     if (total_ms) *total_ms = c->prof_ms[kc];
@@ -2683,6 +2861,7 @@ long long omx_launch_count(const omx_ctx *c) { return c ? c->launches : 0; }
 int omx_timer_start(omx_ctx *c)
 {
     OMX_API_BEGIN
+    join_side(c);
     req(c, "null context");
     ck(cudaEventRecord(c->t0, c->stream), "event");
     OMX_API_END(c)
@@ -2691,6 +2870,7 @@ int omx_timer_start(omx_ctx *c)
 int omx_timer_stop(omx_ctx *c, float *ms)
 {
     OMX_API_BEGIN
+    join_side(c);
     req(c && ms, "null argument");
     ck(cudaEventRecord(c->t1, c->stream), "event");
     ck(cudaEventSynchronize(c->t1), "event sync");
@@ -2701,6 +2881,7 @@ int omx_timer_stop(omx_ctx *c, float *ms)
 int omx_flush_l2(omx_ctx *c)
 {
     OMX_API_BEGIN
+    join_side(c);
     req(c, "null context");
     const long long n = 64LL << 20;   // 256 MB of floats, twice the L2
     if (!c->flushbuf.p) c->flushbuf.alloc((size_t)n);

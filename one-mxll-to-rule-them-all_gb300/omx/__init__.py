@@ -266,6 +266,23 @@ class TMxll:
         n = nrec.value
         return times[:n].copy(), vals[:n, :npts].copy()
 
+    def drain_async(self):
+        """Enqueue the copy of the recorded samples into a pinned slot; returns a ticket."""
+        t = C.c_longlong()
+        self._chk(lib().omx_detectors_drain_async(self._ctx, C.byref(t)))
+        return t.value
+
+    def collect(self, ticket, max_records=64):
+        """Wait for a ticket's copy; returns (times, values) like drain_detectors."""
+        npts = lib().omx_detectors_total_points(self._ctx)
+        nrec = C.c_int()
+        times = np.zeros(max_records)
+        vals = np.zeros((max_records, max(npts, 1)))
+        self._chk(lib().omx_detectors_collect(self._ctx, int(ticket), A.dptr(times), A.dptr(vals), int(max_records),
+                                              C.byref(nrec)))
+        n = nrec.value
+        return times[:n].copy(), vals[:n, :npts].copy()
+
     def run(self, tt0, nsteps, n_skip_steps=1, t_det_print=0, use_graph=True):
         """The reference's time loop (mxim_mxll.f90:92-132) on the device."""
         self._chk(lib().omx_run(self._ctx, int(tt0), int(nsteps), int(n_skip_steps), int(t_det_print),
@@ -389,6 +406,23 @@ class Batch:
         choice = C.c_int()
         A.check(lib().omx_batch_autotune(self._b, int(reps), C.byref(choice)))
         return choice.value
+
+    def drain_async(self):
+        """Enqueue the copy of the recorded samples into a pinned slot; returns a ticket."""
+        t = C.c_longlong()
+        self._chk(lib().omx_detectors_drain_async(self._ctx, C.byref(t)))
+        return t.value
+
+    def collect(self, ticket, max_records=64):
+        """Wait for a ticket's copy; returns (times, values) like drain_detectors."""
+        npts = lib().omx_detectors_total_points(self._ctx)
+        nrec = C.c_int()
+        times = np.zeros(max_records)
+        vals = np.zeros((max_records, max(npts, 1)))
+        self._chk(lib().omx_detectors_collect(self._ctx, int(ticket), A.dptr(times), A.dptr(vals), int(max_records),
+                                              C.byref(nrec)))
+        n = nrec.value
+        return times[:n].copy(), vals[:n, :npts].copy()
 
     def run(self, tt0, nsteps, n_skip_steps=1, t_det_print=0, use_graph=True):
         A.check(lib().omx_batch_run(self._b, int(tt0), int(nsteps), int(n_skip_steps), int(t_det_print),

@@ -258,6 +258,79 @@ def test_autotune_fused_tmz(orc_mod):
     assert trace_error(tg, tc) <= FP32_TOL
 
 
+def test_one_step_calls_with_async_drain_equal_one_run():
+    """A host that drives the fused path one omx_run call per step leaves each step's side-stream
+    work running into the next call, and drains every step asynchronously (tickets collected one
+    step late); fields, detector records and emitter state equal a single multi-step run bit for
+    bit, also with unrelated entry points (a field read) between the calls."""
+    deck = tmz_variant_deck(256, 64, 2, 3, src="plane")
+    n = 37
+    out = []
+    for mode in ("one_run", "per_step"):
+        g = omx.TMxll(2, deck["grid_Ndims"], deck["npml"], deck["boundaries"], deck["dt"], deck["dr"], mode=omx.TMZ,
+                      precision="fp32")
+        groups = decks.apply_deck(g, deck, omx, decks.media_map(deck, omx.media_map_from_voxels))
+        for det in deck["detectors"]:
+            g.add_detector(det["type"], det["field"], det["idx"])
+        if mode == "one_run":
+            g.run(1, n, deck["n_skip"], 1)
+            times, tr = g.drain_detectors()
+        else:
+            tl, vl = [], []
+            pending = None
+            for tt in range(1, n + 1):
+                g.run(tt, 1, deck["n_skip"], 1)
+                if tt == 17:
+                    g.read_field(3)
+                t = g.drain_async()
+                if pending is not None:
+                    a, b = g.collect(pending)
+                    tl.append(a)
+                    vl.append(b)
+                pending = t
+            a, b = g.collect(pending)
+            tl.append(a)
+            vl.append(b)
+            times, tr = np.concatenate(tl), np.concatenate(vl)
+        st = groups[0].read()
+        out.append((times, tr, [g.read_field(f) for f in (3, 4, 5)], st["rho"], st["dipole"]))
+        g.kill()
+    (s0, t0, f0, r0, d0), (s1, t1, f1, r1, d1) = out
+    assert len(s0) == n and np.max(np.abs(t0)) > 0 and np.max(np.abs(d0)) > 0
+    assert np.array_equal(s0, s1) and np.array_equal(t0, t1)
+    assert np.array_equal(r0, r1) and np.array_equal(d0, d1)
+    for a, b in zip(f0, f1):
+        assert np.array_equal(a, b)
+
+
+def test_async_drain_ring_limits():
+    deck = tmz_variant_deck(128, 48, 2, 2, src="plane")
+    g = omx.TMxll(2, deck["grid_Ndims"], deck["npml"], deck["boundaries"], deck["dt"], deck["dr"], mode=omx.TMZ,
+                  precision="fp32")
+    decks.apply_deck(g, deck, omx, decks.media_map(deck, omx.media_map_from_voxels))
+    for det in deck["detectors"]:
+        g.add_detector(det["type"], det["field"], det["idx"])
+    tickets = []
+    for tt in range(1, 5):
+        g.run(tt, 1, deck["n_skip"], 1)
+        tickets.append(g.drain_async())
+    with pytest.raises(omx.OMXError):
+        g.drain_async()                       # all four slots hold uncollected tickets
+    with pytest.raises(omx.OMXError):
+        g.collect(tickets[0] + 100)           # unknown ticket
+    times, _ = g.collect(tickets[0])
+    assert len(times) == 1
+    with pytest.raises(omx.OMXError):
+        g.collect(tickets[0])                 # already collected
+    g.run(5, 3, deck["n_skip"], 1)
+    t5 = g.drain_async()
+    with pytest.raises(omx.OMXError):
+        g.collect(t5, max_records=2)          # three records do not fit
+    for t in tickets[1:]:
+        assert len(g.collect(t)[0]) == 1
+    g.kill()
+
+
 @pytest.mark.parametrize("steps", [61, 80])
 def test_fused_graph_overlap_equals_sequential(steps):
     """In a graph the fused path runs step s's sampling and emitter work on a side stream next to
