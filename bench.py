@@ -469,7 +469,8 @@ def gpu_arm(args, dist):
                                           "how": "the reference's per-step call sequence through the C-ABI "
                                                  "(omx_step_H, omx_source_interactions, omx_step_E, "
                                                  "omx_qgroup_step, omx_detectors_record) + asynchronous drain "
-                                                 "every step"}},
+                                                 "every step; omx_step_H is deferred into the fused pass of "
+                                                 "omx_step_E"}},
             "gpu_launches": launches,
             "clocks": clk,
         }

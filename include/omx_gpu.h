@@ -283,7 +283,8 @@ int omx_run(omx_ctx *ctx, int tt0, int nsteps, int n_skip_steps, int t_det_print
 /* Launch-shape autotuner (no counterpart in the reference, whose loops have no launch shape).
  * Times each candidate shape of this grid's field kernels `reps` times and keeps the fastest:
  * the fused FP32 TMz kernel's form (0 register prefetch, 4/5/6/8 bulk-copy ring depth, 14/15/16
- * ring depth 4/5/6 filled by a dedicated copy warp) or the
+ * ring depth 4/5/6 filled by a dedicated copy warp, 24/25 the same with depth 4/5 and two 4-cell
+ * chunks per thread) or the
  * planes / rows each thread marches in the unfused kernels.  The candidates run on the initial
  * all-zero fields, which every kernel maps to zero, so the simulation state is unchanged: call it
  * after the grid is configured and before the first step or omx_write_field (OMX_ERR_STATE

@@ -212,6 +212,11 @@ struct omx_ctx {
     // next call's fused pass overlaps it; every other entry point first orders the main stream
     // after it (join_side)
     bool side_pending = false;
+    // the reference's per-call sequence on the fused FP32 TMz path: omx_step_H is deferred and
+    // fused with the next omx_step_E (sources requested in between are added after the fused
+    // pass, as omx_run does); any other entry point first runs the deferred work unfused
+    bool h_pending = false, src_pending = false;
+    double src_time = 0.0;
     // asynchronous detector drains: a ring of pinned slots, each filled by copies on the stream
     // and marked by an event; omx_detectors_collect hands a slot's records to the caller
     struct DrainSlot {
@@ -1063,11 +1068,32 @@ template <> void fused_step<float>(omx_ctx *c)
 }
 
 // Order the main stream after the side-stream work a one-step omx_run left running.
-void join_side(omx_ctx *c)
+void join_stream(omx_ctx *c)
 {
     if (c && c->side_pending) {
         ck(cudaStreamWaitEvent(c->stream, c->ev_join, 0), "join");
         c->side_pending = false;
+    }
+}
+
+double source_amp(const SourceRec &S, double time);
+
+// Bring the context to a settled state before an entry point touches it: the side-stream work
+// is joined and a deferred omx_step_H (with the sources requested after it) runs unfused.
+void join_side(omx_ctx *c)
+{
+    join_stream(c);
+    if (c && c->h_pending) {
+        c->h_pending = false;
+        if (c->fp32) do_H<float>(c);
+        else do_H<double>(c);
+        if (c->src_pending) {
+            c->src_pending = false;
+            std::vector<StepParam> amps;
+            for (auto &s : c->sources) amps.push_back(imm(source_amp(*s, c->src_time)));
+            if (c->fp32) do_sources<float>(c, amps);
+            else do_sources<double>(c, amps);
+        }
     }
 }
 
@@ -1188,6 +1214,7 @@ StepParam plan_param(omx_ctx *c, const RunPlan &plan, int row) { return StepPara
 
 template <class R> void run_impl(omx_ctx *c, int tt0, int nsteps, int n_skip, int t_det_print, int use_graph)
 {
+    if (c->h_pending) join_side(c);
     // a configuration change, or anything but a one-step graph call, first waits for the side
     // sequence a previous one-step call left running
     if (c->j_dirty || c->det_dirty || c->fused_dirty || !c->started || nsteps != 1 || !use_graph || c->prof)
@@ -1340,7 +1367,7 @@ template <class R> int autotune_impl(omx_ctx *c, int reps)
 {
     const bool fused = std::is_same<R, float>::value && c->fused_ok;
     std::vector<int> cand;
-    if (fused) cand = {0, 4, 5, 6, 8, 14, 15, 16};
+    if (fused) cand = {0, 4, 5, 6, 8, 14, 15, 16, 24, 25, 34, 36};
     else if (c->dims == 3) cand = {4, 8, 16, 32};
     else if (c->dims == 2) cand = {8, 16, 32, 64};
     else return 0;
@@ -1742,6 +1769,10 @@ int omx_step_H(omx_ctx *c)
     join_side(c);
     req(c, "null context");
     prepare(c);
+    if (c->fp32 && c->fused_ok && !c->prof) {
+        c->h_pending = true;                 // runs with the next omx_step_E as one fused pass
+        return OMX_OK;
+    }
     if (c->fp32) do_H<float>(c);
     else do_H<double>(c);
     ck(cudaPeekAtLastError(), "H launch");
@@ -1751,8 +1782,24 @@ int omx_step_H(omx_ctx *c)
 int omx_step_E(omx_ctx *c, double time, double t_skip)
 {
     OMX_API_BEGIN
-    join_side(c);
     req(c, "null context");
+    if (c->h_pending) {
+        // the deferred H half and this E half in one pass, then the sources requested between
+        // them and the emitter current: the order of omx_run's fused step
+        join_stream(c);
+        c->h_pending = false;
+        fused_step<float>(c);
+        if (c->src_pending) {
+            c->src_pending = false;
+            std::vector<StepParam> amps;
+            for (auto &s : c->sources) amps.push_back(imm(source_amp(*s, c->src_time)));
+            do_sources<float>(c, amps);
+        }
+        do_inject<float>(c, imm(time), imm(t_skip));
+        ck(cudaPeekAtLastError(), "E launch");
+        return OMX_OK;
+    }
+    join_side(c);
     prepare(c);
     if (c->fp32) do_E<float>(c, imm(time), imm(t_skip));
     else do_E<double>(c, imm(time), imm(t_skip));
@@ -1841,8 +1888,13 @@ int omx_plane_source_add(omx_ctx *c, const omx_plane_source_desc *d, int *id)
 int omx_source_interactions(omx_ctx *c, double time)
 {
     OMX_API_BEGIN
-    join_side(c);
     req(c, "null context");
+    if (c->h_pending && !c->src_pending && !c->j_dirty && !c->det_dirty && !c->fused_dirty) {
+        c->src_pending = true;               // added after the fused pass of the next omx_step_E
+        c->src_time = time;
+        return OMX_OK;
+    }
+    join_side(c);
     prepare(c);
     std::vector<StepParam> amps;
     for (auto &s : c->sources) amps.push_back(imm(source_amp(*s, time)));

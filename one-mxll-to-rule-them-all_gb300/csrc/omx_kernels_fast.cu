@@ -48,6 +48,10 @@ static int default_fused_form()
             else if (!strcmp(v, "ws4")) form = 14;
             else if (!strcmp(v, "ws5")) form = 15;
             else if (!strcmp(v, "ws6")) form = 16;
+            else if (!strcmp(v, "ws4x2")) form = 24;
+            else if (!strcmp(v, "ws5x2")) form = 25;
+            else if (!strcmp(v, "rt4")) form = 34;
+            else if (!strcmp(v, "rt6")) form = 36;
         }
     }
     return form;
@@ -70,19 +74,26 @@ template <bool X, int D> static void launch_tma(const Fused2Args &A, const GridA
     k_fused_tmz_tma<X, D><<<grid, 128, smem, s>>>(A, G, nstrip);
 }
 
-template <bool X, int D> static void launch_ws(const Fused2Args &A, const GridArgs<float> &G, int nstrip, cudaStream_t s)
+template <bool X, int D, int CH> static void launch_ws(const Fused2Args &A, const GridArgs<float> &G, cudaStream_t s)
 {
-    const size_t smem = D * sizeof(FzStage) + 2 * D * sizeof(uint64_t);
+    const size_t smem = D * sizeof(FzStageT<CH>) + 2 * D * sizeof(uint64_t);
+    const int nstrip = (G.L.nx / 4 + 128 * CH - 1) / (128 * CH);
     static int nb[FZ_MAX_DEV] = {};
     int dev = 0;
     cudaGetDevice(&dev);
     int &n = nb[dev < FZ_MAX_DEV ? dev : 0];
     if (n == 0) {
-        cudaFuncSetAttribute(k_fused_tmz_ws<X, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        n = persistent_blocks((const void *)k_fused_tmz_ws<X, D>, smem, 32 * (FZ_CONSUMERS + 1));
+        cudaFuncSetAttribute(k_fused_tmz_ws<X, D, CH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        n = persistent_blocks((const void *)k_fused_tmz_ws<X, D, CH>, smem, 32 * (FZ_CONSUMERS + 1));
     }
     const int grid = (int)std::min<long long>(n, (long long)nstrip * G.L.ny);
-    k_fused_tmz_ws<X, D><<<grid, 32 * (FZ_CONSUMERS + 1), smem, s>>>(A, G, nstrip);
+    k_fused_tmz_ws<X, D, CH><<<grid, 32 * (FZ_CONSUMERS + 1), smem, s>>>(A, G, nstrip);
+}
+
+template <bool X, int R> static void launch_rt(const Fused2Args &A, const GridArgs<float> &G, int nstrip, cudaStream_t s)
+{
+    const int ntile = (G.L.ny + R - 1) / R;
+    k_fused_tmz_rt<X, R><<<(unsigned)(nstrip * ntile), 128, 0, s>>>(A, G, ntile);
 }
 
 template <bool X> static void launch_regs(const Fused2Args &A, const GridArgs<float> &G, int nstrip, cudaStream_t s)
@@ -104,10 +115,14 @@ static void launch_form(const Fused2Args &A, const GridArgs<float> &G, int form,
     case 4: launch_tma<X, 4>(A, G, nstrip, s); break;
     case 6: launch_tma<X, 6>(A, G, nstrip, s); break;
     case 8: launch_tma<X, 8>(A, G, nstrip, s); break;
-    case 16: launch_ws<X, 6>(A, G, nstrip, s); break;
+    case 16: launch_ws<X, 6, 1>(A, G, s); break;
     case 5: launch_tma<X, 5>(A, G, nstrip, s); break;
-    case 15: launch_ws<X, 5>(A, G, nstrip, s); break;
-    default: launch_ws<X, 4>(A, G, nstrip, s); break;
+    case 15: launch_ws<X, 5, 1>(A, G, s); break;
+    case 24: launch_ws<X, 4, 2>(A, G, s); break;
+    case 34: launch_rt<X, 4>(A, G, nstrip, s); break;
+    case 36: launch_rt<X, 6>(A, G, nstrip, s); break;
+    case 25: launch_ws<X, 5, 2>(A, G, s); break;
+    default: launch_ws<X, 4, 1>(A, G, s); break;
     }
 }
 

@@ -208,7 +208,7 @@ def test_fp32_fused_tmz_variants(orc_mod, shape, bx, by, src, steps):
     assert trace_error(tg2, tc) <= FP32_TOL
 
 
-FORMS = ("regs", "tma4", "tma5", "tma6", "tma8", "ws4", "ws5", "ws6")
+FORMS = ("regs", "tma4", "tma5", "tma6", "tma8", "ws4", "ws5", "ws6", "ws4x2", "ws5x2", "rt4", "rt6")
 
 
 @pytest.mark.parametrize("shape,bx,by,src,steps", [
@@ -218,8 +218,8 @@ FORMS = ("regs", "tma4", "tma5", "tma6", "tma8", "ws4", "ws5", "ws6")
 ])
 def test_fused_forms_bit_identical(tmp_path, shape, bx, by, src, steps):
     """Every form of the fused TMz kernel (register prefetch, bulk copies into rings of 4-8
-    slots, with or without a dedicated copy warp) performs the same arithmetic on the same words: fields and detector traces agree
-    bit for bit.  Each form runs in its own process (the form is chosen once per process)."""
+    slots, with or without a dedicated copy warp, one or two 4-cell chunks per thread) performs
+    the same arithmetic on the same words: fields and detector traces agree bit for bit.  Each form runs in its own process (the form is chosen once per process)."""
     out = {}
     for form in FORMS:
         f = tmp_path / f"{form}.npz"
@@ -301,6 +301,53 @@ def test_one_step_calls_with_async_drain_equal_one_run():
     assert np.array_equal(r0, r1) and np.array_equal(d0, d1)
     for a, b in zip(f0, f1):
         assert np.array_equal(a, b)
+
+
+def _tmz_context(deck):
+    g = omx.TMxll(2, deck["grid_Ndims"], deck["npml"], deck["boundaries"], deck["dt"], deck["dr"], mode=omx.TMZ,
+                  precision="fp32")
+    groups = decks.apply_deck(g, deck, omx, decks.media_map(deck, omx.media_map_from_voxels))
+    for det in deck["detectors"]:
+        g.add_detector(det["type"], det["field"], det["idx"])
+    return g, groups
+
+
+def test_per_call_sequence_runs_the_fused_pass():
+    """The reference's per-step calls (omx_step_H, omx_source_interactions, omx_step_E,
+    omx_qgroup_step, omx_detectors_record) on the FP32 TMz path defer the H half into the fused
+    pass of omx_step_E: bit-identical to omx_run.  An entry point between the H and E calls (a
+    field read) runs the deferred H half unfused; that run agrees with the fused one to FP32
+    rounding."""
+    deck = tmz_variant_deck(256, 64, 2, 3, src="plane")
+    n = 41
+    out = []
+    for mode in ("run", "calls", "calls_flushed"):
+        g, groups = _tmz_context(deck)
+        if mode == "run":
+            g.run(1, n, deck["n_skip"], deck["t_det_print"])
+        else:
+            class Target:
+                def __getattr__(self, k):
+                    return getattr(g, k)
+
+                def td_propagate_H_field(self):
+                    g.td_propagate_H_field()
+                    if mode == "calls_flushed":
+                        g.read_field(4)
+
+            step_loop(Target(), deck, groups, 1, n, {"tq_old": 0, "t_skip": 0.0},
+                      sample=lambda t: g.write_detectors_outputs(t))
+        _, tr = g.drain_detectors()
+        st = groups[0].read()
+        out.append((tr, [g.read_field(f) for f in (3, 4, 5)], st["rho"], st["dipole"]))
+        g.kill()
+    (t0, f0, r0, d0), (t1, f1, r1, d1), (t2, f2, r2, d2) = out
+    assert np.max(np.abs(t0)) > 0 and np.max(np.abs(d0)) > 0
+    assert np.array_equal(t0, t1) and np.array_equal(r0, r1) and np.array_equal(d0, d1)
+    for a, b in zip(f0, f1):
+        assert np.array_equal(a, b)
+    assert not np.array_equal(t0, t2)          # the flushed run did take the unfused path
+    assert trace_error(t2, t0) <= FP32_TOL
 
 
 def test_async_drain_ring_limits():
