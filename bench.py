@@ -50,6 +50,8 @@ def parse():
     p.add_argument("--train-steps", type=int, default=300, help="cfg4: Adam steps of the closure training")
     p.add_argument("--trajectories", type=int, default=16384, help="cfg4: training trajectories (plain propagator)")
     p.add_argument("--cpu-seconds", type=float, default=12.0)
+    p.add_argument("--grid", type=int, default=None,
+                   help="cfg3: cube side instead of 512 (a smaller case of the same scene, e.g. for a profiler)")
     p.add_argument("--skip-plain", action="store_true")
     p.add_argument("--error-steps", type=int, default=None,
                    help="length of the FP32-vs-FP64 error run (default: the configuration's full run)")
@@ -143,15 +145,18 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------------- workload
-def make_deck(cfg):
+def make_deck(cfg, grid=None):
     from omx import decks
 
     if cfg == "cfg1":
         return decks.deck_cfg1(), "cfg1: 3D 128^3 dr 2 nm, 10-cell CPML, Drude-Lorentz Au sphere r 20 nm, " \
                                   "x-polarised 2.2 eV plane-wave soft source, 16 point detectors"
     if cfg == "cfg3":
-        return decks.deck_cfg3(), "cfg3: 3D 512^3 dr 1 nm, 10-cell CPML, 4x4 Au nanorod dimers, 1e5 three-level " \
-                                  "emitters in the gaps, chirped 1.8-2.6 eV drive, 16 point detectors"
+        n = grid or 512
+        ne = 100000 if n == 512 else max(1000, int(100000 * (n / 512) ** 3))
+        return decks.deck_cfg3(n=n, n_emitters=ne), \
+            f"cfg3: 3D {n}^3 dr 1 nm, 10-cell CPML, 4x4 Au nanorod dimers, {ne} three-level emitters in the gaps, " \
+            "chirped 1.8-2.6 eV drive, 16 point detectors"
     return decks.deck_cfg2(), "cfg2: 2D TMz 4096x4096 dr 2 nm, periodic x / CPML y, 40 nm Drude Ag film with " \
                               "150 nm holes at 400 nm pitch, 1e4 two-level emitters, 3.0 eV source, 16 point detectors"
 
@@ -291,7 +296,7 @@ def reference_arm(args, dist):
         k = min(range(len(dks)), key=lambda q: sides[q])
         deck, desc = dks[k], "cfg5 sample: the sweep's smallest grid (side %d) of %d" % (sides[k], len(dks))
     else:
-        deck, desc = make_deck(args.config)
+        deck, desc = make_deck(args.config, args.grid)
     cells = cells_of(deck)
     # W warm-up steps and K timed steps of the CPU restatement, each bounded: the whole run is
     # sized to finish within a few minutes (about 2 s per timed step at most).
@@ -316,7 +321,7 @@ def gpu_arm(args, dist):
 
     if dist.world > 1:
         omx.select_device(dist.local_rank % max(1, omx.device_count()))
-    deck, desc = make_deck(args.config)
+    deck, desc = make_deck(args.config, args.grid)
     cells = cells_of(deck)
     ne = n_emitters(deck)
     K, W = args.steps, max(3, args.warmup)
@@ -358,7 +363,8 @@ def gpu_arm(args, dist):
     if per["H"]["launches"] == 0:      # FP32 2D TMz: one fused pass per step
         per["fused_HE"] = per.pop("E")
         per.pop("H")
-        dom, kernel_name = "fused_HE", "k_fused_tmz_* (H+E step in one pass; form from OMX_FUSED_KERNEL, default ws4)"
+        dom, kernel_name = "fused_HE", ("k_fused3 (3D H+E step in one pass)" if deck["dimensions"] == 3 else
+                                        "k_fused_tmz_* (H+E step in one pass; form from OMX_FUSED_KERNEL, default ws4)")
     alg_bytes = gpu.algorithmic_bytes(kc_dom)
     traffic, traffic_src = (None, None)
     if dom == "fused_HE" and args.config == "cfg2" and os.environ.get("OMX_FUSED_KERNEL", "ws4") == "ws4":
@@ -527,10 +533,13 @@ def gpu_arm_cfg5(args, dist):
     batch.kill()
     for g in grids:
         g.kill()
-    # ---- the same grids one at a time (each its own omx_run, CUDA graph per grid)
+    # ---- the same grids one at a time (each its own omx_run, CUDA graph per grid), first with the
+    # batch's arithmetic (the two half-step passes; traces compared bit for bit), then with the
+    # single-pass FP32 step a solo grid takes by default
     t_solo, same = 0.0, True
     for d, tb in zip(dks, traces_b):
         g = build_gpu(d, "fp32")[0]
+        g.set_fused(False)
         g.run(1, W, 1, tdp, use_graph=True)
         g.synchronize()
         t0 = time.perf_counter()
@@ -541,8 +550,20 @@ def gpu_arm_cfg5(args, dist):
         same = same and ts.shape == tb.shape and bool(np.array_equal(ts, tb))
         g.kill()
     t_solo = dist.max(t_solo)
+    t_fused = 0.0
+    for d in dks:
+        g = build_gpu(d, "fp32")[0]
+        g.run(1, W, 1, tdp, use_graph=True)
+        g.synchronize()
+        t0 = time.perf_counter()
+        g.run(1 + W, K, 1, tdp, use_graph=True)
+        g.synchronize()
+        t_fused += time.perf_counter() - t0
+        g.kill()
+    t_fused = dist.max(t_fused)
     value = dist.world * cells * K / t_batch / 1e9
     solo_value = dist.world * cells * K / t_solo / 1e9
+    fused_value = dist.world * cells * K / t_fused / 1e9
     peak, peak_kind = peaks()
     achieved = alg * K / t_batch / 1e9
     cpu = None
@@ -574,7 +595,11 @@ def gpu_arm_cfg5(args, dist):
             "one_at_a_time": {"value": solo_value, "unit": "Gcell-updates/s",
                               "how": "the same grids, each its own omx_run (CUDA graph), run one after another",
                               "batch_speedup": value / solo_value,
-                              "detector_traces_bit_identical": same},
+                              "detector_traces_bit_identical": same,
+                              "arithmetic": "two half-step passes per grid, as the batch"},
+            "one_at_a_time_fused": {"value": fused_value, "unit": "Gcell-updates/s",
+                                    "how": "the same grids one after another, each with the single-pass "
+                                           "FP32 3D step (k_fused3), the default for a solo grid"},
             "roofline": {"bound": "hbm", "kernel": "k_batch3 (H and bulk E passes over all grids)",
                          "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": None, "peak_source": peak_kind,

@@ -280,6 +280,12 @@ int omx_qgroup_write_text(omx_ctx *ctx, int group, const char *dir, double time,
  * graph is kept and reused by later calls until a configuration call changes the context. */
 int omx_run(omx_ctx *ctx, int tt0, int nsteps, int n_skip_steps, int t_det_print, int use_graph);
 
+/* FP32 single-pass steps on (enable != 0) or off (the two half-step passes, the arithmetic of
+ * batched runs, which turn it off for their members).  Default: on for 2D TMz, off in 3D, where
+ * the single pass (k_fused3) measures slower than the two passes on GB300.  Either way the same
+ * FP32 bar holds; the switch may be flipped between steps. */
+int omx_set_fused(omx_ctx *ctx, int enable);
+
 /* Launch-shape autotuner (no counterpart in the reference, whose loops have no launch shape).
  * Times each candidate shape of this grid's field kernels `reps` times and keeps the fastest:
  * the fused FP32 TMz kernel's form (0 register prefetch, 4/5/6/8 bulk-copy ring depth, 14/15/16

@@ -264,6 +264,9 @@ struct omx_ctx {
     int cur = 0;
     bool fused_ok = false;
     bool fused_dirty = true;    // media or sources changed since the last eligibility check
+    // omx_set_fused: on by default for the 2D TMz pass, off in 3D (the single pass measures
+    // slower than the two unfused ones there); a batch turns it off for its members
+    bool fuse_enabled = true;
     int *run_step = nullptr;    // device step counter while omx_run issues a step sequence
     std::string err;
 };
@@ -862,26 +865,39 @@ DetArgs det_args(omx_ctx *c)
 
 // The FP32 fused TMz step applies dispersive cells and sources after the bulk pass; that
 // commutes with the reference's order only outside the CPML slabs and away from sources.
+// The FP32 fused passes (2D TMz: k_fused_tmz_*, 3D: k_fused3) apply dispersive cells, sources
+// and the emitter current after the bulk update, which needs no dispersive cell in a CPML slab
+// (its psi term would be lost) and no source point in a dispersive cell.
 bool fused_eligible(const omx_ctx *c)
 {
-    if (!c->fp32 || c->dims != 2 || c->desc.mode != OMX_TMZ_2D_MODE || c->n[0] % 4 != 0) return false;
+    if (!c->fp32 || !c->fuse_enabled) return false;
+    if (c->dims == 2) {
+        if (c->desc.mode != OMX_TMZ_2D_MODE || c->n[0] % 4 != 0) return false;
+    } else if (c->dims == 3) {
+        if (c->n[0] % 32 != 0 || c->n[1] % F3_BY != 0) return false;
+    } else {
+        return false;
+    }
     const int npml = c->desc.npml;
     for (const int4 &e : c->ade_host) {
-        for (int a = 0; a < 2; ++a) {
-            const int p = a == 0 ? e.x : e.y;
+        for (int a = 0; a < c->dims; ++a) {
+            const int p = a == 0 ? e.x : (a == 1 ? e.y : e.z);
             if (c->cpml_axis[a] && (p <= npml || p >= c->n[a] + 1 - npml)) return false;
         }
     }
     if (!c->ade_host.empty()) {
+        const bool d3 = c->dims == 3;
         std::unordered_map<long long, int> disp;
-        for (const int4 &e : c->ade_host) disp[cell_key(c, e.x, e.y, 0) * 4 + e.w] = 1;
+        for (const int4 &e : c->ade_host) disp[cell_key(c, e.x, e.y, d3 ? e.z : 0) * 4 + e.w] = 1;
         for (const auto &S : c->sources) {
             if (S->kind == 0) {
                 for (const int4 &p : S->cells)
-                    if (disp.count(cell_key(c, p.x, p.y, 0) * 4 + p.w)) return false;
+                    if (disp.count(cell_key(c, p.x, p.y, d3 ? p.z : 0) * 4 + p.w)) return false;
             } else {
-                for (const int4 &e : c->ade_host)
-                    if (e.w == S->pd.comp - 1 && (S->pd.plane_axis == 1 ? e.x : e.y) == S->pd.plane_index) return false;
+                for (const int4 &e : c->ade_host) {
+                    const int at = S->pd.plane_axis == 1 ? e.x : (S->pd.plane_axis == 2 ? e.y : e.z);
+                    if (e.w == S->pd.comp - 1 && at == S->pd.plane_index) return false;
+                }
             }
         }
     }
@@ -901,8 +917,9 @@ void prepare(omx_ctx *c)
     if (c->fused_ok && !c->ff2[2].p) {
         for (int q = 0; q < 6; ++q)
             if (c->field_used[q]) c->ff2[q].alloc(c->felems);
-        for (int a = 0; a < 2; ++a)
-            if (c->psif[a][1][0].p) c->psiH2[a][0].alloc(c->psif[a][1][0].n);
+        for (int a = 0; a < 3; ++a)
+            for (int q = 0; q < 2; ++q)
+                if (c->psif[a][1][q].p) c->psiH2[a][q].alloc(c->psif[a][1][q].n);
         c->epoch++;
     }
 }
@@ -1046,6 +1063,18 @@ template <> void fused_step<float>(omx_ctx *c)
     const int in = c->cur, out = 1 - c->cur;
     const FieldPtrs<float> Fin = field_ptrs<float>(c, in), Fout = field_ptrs<float>(c, out);
     const GridArgs<float> G = grid_args<float>(c);
+    if (c->dims == 3) {
+        Fused3Args A;
+        A.in = Fin;
+        A.out = Fout;
+        for (int a = 0; a < 3; ++a)
+            for (int q = 0; q < 2; ++q) A.psiH_out[a][q] = in == 0 ? c->psiH2[a][q].p : c->psif[a][1][q].p;
+        launch_fused3(A, G, c->march, c->stream);
+        launch_ade_post(Fin, Fout, G, c->stream);
+        c->launches += 1 + (c->ade_n > 0 ? 1 : 0);
+        c->cur = out;
+        return;
+    }
     Fused2Args A;
     A.ez_in = Fin.f[2];
     A.hx_in = Fin.f[3];
@@ -1367,14 +1396,15 @@ template <class R> int autotune_impl(omx_ctx *c, int reps)
 {
     const bool fused = std::is_same<R, float>::value && c->fused_ok;
     std::vector<int> cand;
-    if (fused) cand = {0, 4, 5, 6, 8, 14, 15, 16, 24, 25, 34, 36};
+    if (fused && c->dims == 3) cand = {8, 16, 32};
+    else if (fused) cand = {0, 4, 5, 6, 8, 14, 15, 16, 24, 25, 34, 36};
     else if (c->dims == 3) cand = {4, 8, 16, 32};
     else if (c->dims == 2) cand = {8, 16, 32, 64};
     else return 0;
     float best = 0.f;
     int pick = cand[0];
     for (size_t k = 0; k < cand.size(); ++k) {
-        if (fused) c->fused_form = cand[k];
+        if (fused && c->dims == 2) c->fused_form = cand[k];
         else c->march = cand[k];
         auto once = [&]() {
             if (fused) {
@@ -1396,7 +1426,7 @@ template <class R> int autotune_impl(omx_ctx *c, int reps)
             pick = cand[k];
         }
     }
-    if (fused) c->fused_form = pick;
+    if (fused && c->dims == 2) c->fused_form = pick;
     else c->march = pick;
     ck(cudaPeekAtLastError(), "autotune");
     return pick;
@@ -1521,6 +1551,7 @@ int omx_create(const omx_grid_desc *d, omx_ctx **out)
             for (int a = 0; a < naxes; ++a)
                 if (c->cpml_axis[a]) req(c->n[a] >= 2 * d->npml, "grid too small for two CPML slabs");
         }
+        c->fuse_enabled = c->dims != 3;
         ck(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream");
         ck(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking), "stream");
         ck(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming), "event");
@@ -2433,6 +2464,17 @@ int omx_run(omx_ctx *c, int tt0, int nsteps, int n_skip_steps, int t_det_print, 
     OMX_API_END(c)
 }
 
+int omx_set_fused(omx_ctx *c, int enable)
+{
+    OMX_API_BEGIN
+    join_side(c);
+    req(c, "null context");
+    c->fuse_enabled = enable != 0;
+    c->fused_dirty = true;
+    c->epoch++;
+    OMX_API_END(c)
+}
+
 int omx_autotune(omx_ctx *c, int reps, int *choice)
 {
     OMX_API_BEGIN
@@ -2745,6 +2787,14 @@ int omx_batch_create(omx_ctx *const *ctxs, int n, omx_batch **out)
         for (int k = 0; k < i; ++k) req(ctxs[k] != c, "a context appears twice in the batch");
         b->ctx.push_back(c);
     }
+    // the batched passes are the two unfused half steps of every grid; a member used on its own
+    // afterwards keeps that arithmetic
+    for (auto *c : b->ctx) {
+        join_side(c);
+        c->fuse_enabled = false;
+        c->fused_dirty = true;
+        c->fused_ok = false;
+    }
     b->fp32 = ctxs[0]->fp32;
     ck(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "stream");
     ck(cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming), "event");
@@ -2892,11 +2942,11 @@ int omx_algorithmic_bytes(const omx_ctx *c, int kc, double *bytes)
             }
         ade_bytes = (double)drude * 2.0 * w + (double)dl * (2.0 + 2.0 + 4.0 * c->P) * w;
     }
-    const bool fused = c->fused_ok;   // FP32 2D TMz: one pass per step (class KC_E)
+    const bool fused = c->fused_ok;   // FP32 fused (2D TMz, 3D): one pass per step (class KC_E)
     if (kc == KC_H) {
         b = fused ? 0.0 : cells * w * (ncomp_e + 2.0 * ncomp_h) + psi_cells_h * 2.0 * w;
     } else if (kc == KC_E) {
-        if (fused)   // each of Ez, Hx, Hy read once and written once
+        if (fused)   // each field word read once and written once
             b = cells * w * 2.0 * (ncomp_e + ncomp_h) + (psi_cells_h + psi_cells_e) * 2.0 * w +
                 (double)c->bbV * ncomp_e + ade_bytes;
         else

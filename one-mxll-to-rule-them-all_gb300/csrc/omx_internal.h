@@ -174,6 +174,14 @@ struct Fused2Args {
 // form: 0 register prefetch, 4/5/6/8 bulk-copy ring depth, 14/15/16 ring depth 4/5/6 with a
 // dedicated copy warp; < 0 the default
 void launch_fused_tmz(const Fused2Args &A, const GridArgs<float> &G, int form, void *stream);
+// FP32 fused 3D step (k_fused3): in / out buffer sets, the out set's H psi
+constexpr int F3_BY = 8;   // thread rows per block of the fused 3D pass (32 x 8 threads)
+struct Fused3Args {
+    FieldPtrs<float> in, out;
+    float *psiH_out[3][2];   // H psi of the out set (the in set's is GridArgs::psiH)
+};
+// kch: planes marched per thread (0 = default)
+void launch_fused3(const Fused3Args &A, const GridArgs<float> &G, int kch, void *stream);
 void launch_ade_post(const FieldPtrs<float> &Fin, const FieldPtrs<float> &Fout, const GridArgs<float> &G, void *stream);
 void launch_flush(float *buf, long long n, void *stream);
 // FP64 electromagnetic energy of the interior: 0.5 * dV * sum(eps0 E^2 + mu0 H^2) over the fields

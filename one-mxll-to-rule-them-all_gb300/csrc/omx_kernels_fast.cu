@@ -8,6 +8,7 @@
 #include <algorithm>
 #include "omx_batch.cuh"
 #include "omx_fused2d.cuh"
+#include "omx_fused3d.cuh"
 
 namespace omx {
 
@@ -131,6 +132,14 @@ void launch_fused_tmz(const Fused2Args &A, const GridArgs<float> &G, int form, v
     const int nstrip = (G.L.nx / 4 + 127) / 128;
     if (A.psi_ezx) launch_form<true>(A, G, form, nstrip, (cudaStream_t)s);
     else launch_form<false>(A, G, form, nstrip, (cudaStream_t)s);
+}
+
+void launch_fused3(const Fused3Args &A, const GridArgs<float> &G, int kch, void *s)
+{
+    const int m = kch > 0 ? kch : 16;
+    const dim3 b(32, F3_BY, 1), g((unsigned)((G.L.nx + 31) / 32), (unsigned)((G.L.ny + F3_BY - 1) / F3_BY),
+                                  (unsigned)((G.L.nz + m - 1) / m));
+    k_fused3<<<g, b, 0, (cudaStream_t)s>>>(A, G, m);
 }
 
 template <> void launch_batch3<float>(int pass, const BatchGrid<float> *g, int n, long long total, int kch,

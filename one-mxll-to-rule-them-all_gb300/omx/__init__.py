@@ -266,6 +266,10 @@ class TMxll:
         n = nrec.value
         return times[:n].copy(), vals[:n, :npts].copy()
 
+    def set_fused(self, enable):
+        """FP32 single-pass steps on (default) or off (the two half-step passes)."""
+        self._chk(lib().omx_set_fused(self._ctx, 1 if enable else 0))
+
     def drain_async(self):
         """Enqueue the copy of the recorded samples into a pinned slot; returns a ticket."""
         t = C.c_longlong()

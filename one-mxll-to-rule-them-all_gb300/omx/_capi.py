@@ -104,6 +104,7 @@ SIGNATURES = {
     "omx_detectors_record": (_I, [_VP, _D]),
     "omx_detectors_drain": (_I, [_VP, _PD, _PD, _I, _PI]),
     "omx_detectors_drain_async": (_I, [_VP, C.POINTER(C.c_longlong)]),
+    "omx_set_fused": (_I, [_VP, _I]),
     "omx_detectors_collect": (_I, [_VP, C.c_longlong, _PD, _PD, _I, _PI]),
     "omx_run": (_I, [_VP, _I, _I, _I, _I, _I]),
     "omx_detectors_write_text": (_I, [_VP, C.c_char_p, _PI]),

@@ -23,10 +23,12 @@ class OracleFactory:
         return self.orc.medium_dl_custom(*a)
 
 
-def make_pair(orc, deck, precision="fp64", autotune=False):
+def make_pair(orc, deck, precision="fp64", autotune=False, fused=None):
     d = deck
     gpu = omx.TMxll(d["dimensions"], d["grid_Ndims"], d["npml"], d["boundaries"], d["dt"], d["dr"],
                     mode=d["mode"], precision=precision)
+    if fused is not None:
+        gpu.set_fused(fused)
     cpu = orc.Grid(d["dimensions"], d["grid_Ndims"], d["npml"], d["boundaries"], d["dt"], d["dr"], mode=d["mode"])
     mm = decks.media_map(d, omx.media_map_from_voxels) if d["voxels"] else None
     gg = decks.apply_deck(gpu, d, omx, mm)
@@ -65,8 +67,8 @@ def oracle_detectors(cpu, deck):
     return np.concatenate([cpu.sample(det["type"], det["field"], det["idx"]) for det in deck["detectors"]])
 
 
-def run_both(orc, deck, nsteps, precision="fp64", gpu_mode="calls", use_graph=True, autotune=False):
-    gpu, cpu, gg, cg = make_pair(orc, deck, precision, autotune)
+def run_both(orc, deck, nsteps, precision="fp64", gpu_mode="calls", use_graph=True, autotune=False, fused=None):
+    gpu, cpu, gg, cg = make_pair(orc, deck, precision, autotune, fused)
     st_c = {"tq_old": 0, "t_skip": 0.0}
     trace_c = []
     step_loop(cpu, deck, cg, 1, nsteps, st_c, sample=lambda t: trace_c.append(oracle_detectors(cpu, deck)))

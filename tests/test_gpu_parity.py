@@ -90,18 +90,27 @@ def one_d_deck():
     return d
 
 
-def periodic_box_deck():
-    """3D periodic on all axes with a dielectric block and a radial y-source; line/plane detectors."""
-    d = decks._base(3, (24, 20, 16), 4, (2, 2, 2), 2.0)
-    I, J, K = np.meshgrid(np.arange(8, 14), np.arange(5, 12), np.arange(6, 10), indexing="ij")
+def periodic_box_deck(n=(24, 20, 16), boundaries=(2, 2, 2), npml=4, drude=False):
+    """3D box (periodic on all axes by default) with a dielectric block (and a Drude block) and a
+    radial y-source; line/plane detectors."""
+    nx, ny, nz = n
+    d = decks._base(3, n, npml, boundaries, 2.0)
+    I, J, K = np.meshgrid(np.arange(nx // 3, nx // 3 + 6), np.arange(5, 12), np.arange(nz // 2 - 2, nz // 2 + 2),
+                          indexing="ij")
     d["media"].append(dict(kind="dielectric", eps_r=4.0))
-    d["voxels"].append(np.stack([decks._cell_nm(I.ravel(), 24, 2.0), decks._cell_nm(J.ravel(), 20, 2.0),
-                                 decks._cell_nm(K.ravel(), 16, 2.0)], axis=1))
+    d["voxels"].append(np.stack([decks._cell_nm(I.ravel(), nx, 2.0), decks._cell_nm(J.ravel(), ny, 2.0),
+                                 decks._cell_nm(K.ravel(), nz, 2.0)], axis=1))
+    if drude:
+        I, J, K = np.meshgrid(np.arange(nx // 2 + 4, nx // 2 + 9), np.arange(ny // 2 - 3, ny // 2 + 3),
+                              np.arange(nz // 2 - 3, nz // 2 + 2), indexing="ij")
+        d["media"].append(dict(kind="drude", omegaD=7.0, GammaD=0.2, eps_r=1.5))
+        d["voxels"].append(np.stack([decks._cell_nm(I.ravel(), nx, 2.0), decks._cell_nm(J.ravel(), ny, 2.0),
+                                     decks._cell_nm(K.ravel(), nz, 2.0)], axis=1))
     ev, fs = omx.UNITS["ev_to_au"], omx.UNITS["fs_to_au"]
     d["sources"].append(dict(dir="y", j_amp=2.0, w0=2.0 * ev, t0=4 * fs, tau=1.5 * fs, r0=[10 * decks.NM, 0.0, 0.0],
                              radius=1.5 * d["dr"], t_init=0.0, t_final=1e30, phase=0.0, chirp=0.0))
-    line = np.array([[i, 3, 4] for i in range(1, 25)], np.int32)
-    plane = np.array([[i, j, 8] for j in range(1, 21) for i in range(1, 25)], np.int32)
+    line = np.array([[i, 3, 4] for i in range(1, nx + 1)], np.int32)
+    plane = np.array([[i, j, nz // 2] for j in range(1, ny + 1) for i in range(1, nx + 1)], np.int32)
     for f in range(1, 7):
         d["detectors"].append(dict(type=2, field=f, idx=line))
     d["detectors"].append(dict(type=5, field=3, idx=plane))
@@ -164,6 +173,24 @@ def test_fp32_within_tolerance(orc_mod, case):
         ga, cb = a.read(), cpu.q_group_read(b)
         ref = max(np.max(np.abs(cb["dipole"])), 1e-300)
         assert np.max(np.abs(ga["dipole"] - cb["dipole"])) / ref <= 1e-3
+
+
+@pytest.mark.parametrize("n,boundaries,drude,steps", [
+    ((32, 24, 16), (2, 2, 2), False, 90),    # periodic on every axis: every recompute wraps
+    ((64, 32, 24), (3, 2, 2), True, 90),     # CPML x, periodic y / z, a Drude block (k_ade_post)
+    ((32, 40, 36), (3, 3, 3), True, 100),    # CPML on every face, several blocks along y and z
+    ((64, 24, 20), (3, 2, 3), True, 100),    # two tiles along x (lane 0 recomputes inside the grid)
+])
+def test_fp32_fused3d(orc_mod, n, boundaries, drude, steps):
+    """The FP32 single-pass 3D step (opt-in, omx_set_fused): detector traces within the FP32 bar of
+    the FP64 oracle through the device loop and through the per-call sequence (omx_step_H
+    deferred into the fused pass)."""
+    deck = periodic_box_deck(n, boundaries, npml=6, drude=drude)
+    for mode in ("run", "calls"):
+        gpu, cpu, gg, cg, tc, tg = run_both(orc_mod, deck, steps, "fp32", mode, use_graph=True, fused=True)
+        assert np.max(np.abs(tc)) > 0
+        assert trace_error(tg, tc) <= FP32_TOL, (mode, trace_error(tg, tc))
+        assert compare_fields(gpu, cpu, deck) <= 10 * FP32_TOL
 
 
 def test_long_run_fp64_cfg1_shape(orc_mod):
