@@ -368,7 +368,7 @@ def gpu_arm(args, dist):
     alg_bytes = gpu.algorithmic_bytes(kc_dom)
     traffic, traffic_src = (None, None)
     if dom == "fused_HE" and args.config == "cfg2" and os.environ.get("OMX_FUSED_KERNEL", "ws4") == "ws4":
-        traffic, traffic_src = recorded_traffic("k_fused_tmz_ws<0, 4> tmz4096")
+        traffic, traffic_src = recorded_traffic("k_fused_tmz_ws<0, 4, 1> tmz4096")
     avg_s = per[dom]["ms_total"] / per[dom]["launches"] / 1e3
     peak, peak_kind = peaks()
     achieved = alg_bytes / avg_s / 1e9
