@@ -533,13 +533,12 @@ def gpu_arm_cfg5(args, dist):
     batch.kill()
     for g in grids:
         g.kill()
-    # ---- the same grids one at a time (each its own omx_run, CUDA graph per grid), first with the
-    # batch's arithmetic (the two half-step passes; traces compared bit for bit), then with the
-    # single-pass FP32 step a solo grid takes by default
+    # ---- the same grids one at a time (each its own omx_run, CUDA graph per grid) with the
+    # batch's arithmetic (traces compared bit for bit)
     t_solo, same = 0.0, True
     for d, tb in zip(dks, traces_b):
         g = build_gpu(d, "fp32")[0]
-        g.set_fused(False)
+        g.set_step_form(omx.STEP_TWO_PASS)
         g.run(1, W, 1, tdp, use_graph=True)
         g.synchronize()
         t0 = time.perf_counter()
@@ -550,20 +549,8 @@ def gpu_arm_cfg5(args, dist):
         same = same and ts.shape == tb.shape and bool(np.array_equal(ts, tb))
         g.kill()
     t_solo = dist.max(t_solo)
-    t_fused = 0.0
-    for d in dks:
-        g = build_gpu(d, "fp32")[0]
-        g.run(1, W, 1, tdp, use_graph=True)
-        g.synchronize()
-        t0 = time.perf_counter()
-        g.run(1 + W, K, 1, tdp, use_graph=True)
-        g.synchronize()
-        t_fused += time.perf_counter() - t0
-        g.kill()
-    t_fused = dist.max(t_fused)
     value = dist.world * cells * K / t_batch / 1e9
     solo_value = dist.world * cells * K / t_solo / 1e9
-    fused_value = dist.world * cells * K / t_fused / 1e9
     peak, peak_kind = peaks()
     achieved = alg * K / t_batch / 1e9
     cpu = None
@@ -597,9 +584,6 @@ def gpu_arm_cfg5(args, dist):
                               "batch_speedup": value / solo_value,
                               "detector_traces_bit_identical": same,
                               "arithmetic": "two half-step passes per grid, as the batch"},
-            "one_at_a_time_fused": {"value": fused_value, "unit": "Gcell-updates/s",
-                                    "how": "the same grids one after another, each with the single-pass "
-                                           "FP32 3D step (k_fused3), the default for a solo grid"},
             "roofline": {"bound": "hbm", "kernel": "k_batch3 (H and bulk E passes over all grids)",
                          "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": None, "peak_source": peak_kind,

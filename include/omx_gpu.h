@@ -280,11 +280,17 @@ int omx_qgroup_write_text(omx_ctx *ctx, int group, const char *dir, double time,
  * graph is kept and reused by later calls until a configuration call changes the context. */
 int omx_run(omx_ctx *ctx, int tt0, int nsteps, int n_skip_steps, int t_det_print, int use_graph);
 
-/* FP32 single-pass steps on (enable != 0) or off (the two half-step passes, the arithmetic of
- * batched runs, which turn it off for their members).  Default: on for 2D TMz, off in 3D, where
- * the single pass (k_fused3) measures slower than the two passes on GB300.  Either way the same
- * FP32 bar holds; the switch may be flipped between steps. */
-int omx_set_fused(omx_ctx *ctx, int enable);
+/* Kernel form of the FP32 time step (no counterpart in the reference).  Every form meets the same
+ * FP32 bar; they differ in rounding, and the form may be changed between steps.
+ *   OMX_STEP_DEFAULT      2D TMz: one fused pass per step; 3D: the two half-step passes
+ *   OMX_STEP_TWO_PASS     the two half-step passes everywhere: the arithmetic of batched runs
+ *                         (omx_batch_create sets it on its members)
+ *   OMX_STEP_SINGLE_PASS  one fused pass per step where eligible (3D: k_fused3, nx % 32 == 0,
+ *                         ny % 8 == 0; measured slower than the two passes on GB300) */
+#define OMX_STEP_DEFAULT 0
+#define OMX_STEP_TWO_PASS 1
+#define OMX_STEP_SINGLE_PASS 2
+int omx_set_step_form(omx_ctx *ctx, int form);
 
 /* Launch-shape autotuner (no counterpart in the reference, whose loops have no launch shape).
  * Times each candidate shape of this grid's field kernels `reps` times and keeps the fastest:

@@ -264,9 +264,7 @@ struct omx_ctx {
     int cur = 0;
     bool fused_ok = false;
     bool fused_dirty = true;    // media or sources changed since the last eligibility check
-    // omx_set_fused: on by default for the 2D TMz pass, off in 3D (the single pass measures
-    // slower than the two unfused ones there); a batch turns it off for its members
-    bool fuse_enabled = true;
+    int step_form = OMX_STEP_DEFAULT;   // omx_set_step_form; a batch sets TWO_PASS on its members
     int *run_step = nullptr;    // device step counter while omx_run issues a step sequence
     std::string err;
 };
@@ -870,7 +868,8 @@ DetArgs det_args(omx_ctx *c)
 // (its psi term would be lost) and no source point in a dispersive cell.
 bool fused_eligible(const omx_ctx *c)
 {
-    if (!c->fp32 || !c->fuse_enabled) return false;
+    if (!c->fp32 || c->step_form == OMX_STEP_TWO_PASS) return false;
+    if (c->dims == 3 && c->step_form != OMX_STEP_SINGLE_PASS) return false;
     if (c->dims == 2) {
         if (c->desc.mode != OMX_TMZ_2D_MODE || c->n[0] % 4 != 0) return false;
     } else if (c->dims == 3) {
@@ -1551,7 +1550,6 @@ int omx_create(const omx_grid_desc *d, omx_ctx **out)
             for (int a = 0; a < naxes; ++a)
                 if (c->cpml_axis[a]) req(c->n[a] >= 2 * d->npml, "grid too small for two CPML slabs");
         }
-        c->fuse_enabled = c->dims != 3;
         ck(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream");
         ck(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking), "stream");
         ck(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming), "event");
@@ -2464,12 +2462,13 @@ int omx_run(omx_ctx *c, int tt0, int nsteps, int n_skip_steps, int t_det_print, 
     OMX_API_END(c)
 }
 
-int omx_set_fused(omx_ctx *c, int enable)
+int omx_set_step_form(omx_ctx *c, int form)
 {
     OMX_API_BEGIN
     join_side(c);
     req(c, "null context");
-    c->fuse_enabled = enable != 0;
+    req(form == OMX_STEP_DEFAULT || form == OMX_STEP_TWO_PASS || form == OMX_STEP_SINGLE_PASS, "unknown step form");
+    c->step_form = form;
     c->fused_dirty = true;
     c->epoch++;
     OMX_API_END(c)
@@ -2791,7 +2790,7 @@ int omx_batch_create(omx_ctx *const *ctxs, int n, omx_batch **out)
     // afterwards keeps that arithmetic
     for (auto *c : b->ctx) {
         join_side(c);
-        c->fuse_enabled = false;
+        c->step_form = OMX_STEP_TWO_PASS;
         c->fused_dirty = true;
         c->fused_ok = false;
     }

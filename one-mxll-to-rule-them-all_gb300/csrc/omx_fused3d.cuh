@@ -12,7 +12,7 @@
 //   * k-1: the thread's own previous plane (registers); the first plane recomputes it.
 // E psi and the ADE state are touched by their owner only.  Dispersive cells are finished by
 // k_ade_post afterwards, sources and the emitter current by their own kernels (they commute with
-// the bulk update up to FP32 rounding).  The host offers this path (omx_set_fused) only when no
+// the bulk update up to FP32 rounding).  The host offers this path (omx_set_step_form) only when no
 // dispersive cell lies in a CPML slab and no source point lies in a dispersive cell, for
 // nx % 32 == 0 and ny % F3_BY == 0 (every thread owns a cell and reaches every barrier).
 //

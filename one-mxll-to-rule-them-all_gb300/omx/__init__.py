@@ -15,8 +15,8 @@ import numpy as np
 from . import _capi as A
 from ._capi import (CLOSE, CPML, DIELECTRIC, DL, DRUDE, EX, EY, EZ, FIELDS, HX, HY, HZ, KC_DET, KC_E,
                     KC_EMIT, KC_H, KC_SRC, LINE_X, LINE_Y, LINE_Z, NONE_MEDIUM, PERIODIC, PLANE_XY,
-                    PLANE_YZ, PLANE_ZX, POINT, PREC_FP32, PREC_FP64, Q_MATERIAL, Q_SINGLE, TEZ,
-                    THREE_LEVEL, TMZ, TWO_LEVEL, VOLUME, OMXError, lib)
+                    PLANE_YZ, PLANE_ZX, POINT, PREC_FP32, PREC_FP64, Q_MATERIAL, Q_SINGLE, STEP_DEFAULT,
+                    STEP_SINGLE_PASS, STEP_TWO_PASS, TEZ, THREE_LEVEL, TMZ, TWO_LEVEL, VOLUME, OMXError, lib)
 from .units import UNITS
 
 __all__ = ["TMxll", "Medium", "OMXError", "lib", "UNITS", "medium_dielectric", "medium_drude",
@@ -266,9 +266,10 @@ class TMxll:
         n = nrec.value
         return times[:n].copy(), vals[:n, :npts].copy()
 
-    def set_fused(self, enable):
-        """FP32 single-pass steps on (default) or off (the two half-step passes)."""
-        self._chk(lib().omx_set_fused(self._ctx, 1 if enable else 0))
+    def set_step_form(self, form):
+        """Kernel form of the FP32 step: STEP_DEFAULT, STEP_TWO_PASS (the batch arithmetic) or
+        STEP_SINGLE_PASS."""
+        self._chk(lib().omx_set_step_form(self._ctx, int(form)))
 
     def drain_async(self):
         """Enqueue the copy of the recorded samples into a pinned slot; returns a ticket."""

@@ -23,6 +23,7 @@ PREC_FP64, PREC_FP32 = 0, 1
 TWO_LEVEL, THREE_LEVEL = 1, 2
 MAX_POLES = 8
 KC_H, KC_E, KC_EMIT, KC_SRC, KC_DET = range(5)
+STEP_DEFAULT, STEP_TWO_PASS, STEP_SINGLE_PASS = 0, 1, 2
 
 
 class OMXError(RuntimeError):
@@ -104,7 +105,7 @@ SIGNATURES = {
     "omx_detectors_record": (_I, [_VP, _D]),
     "omx_detectors_drain": (_I, [_VP, _PD, _PD, _I, _PI]),
     "omx_detectors_drain_async": (_I, [_VP, C.POINTER(C.c_longlong)]),
-    "omx_set_fused": (_I, [_VP, _I]),
+    "omx_set_step_form": (_I, [_VP, _I]),
     "omx_detectors_collect": (_I, [_VP, C.c_longlong, _PD, _PD, _I, _PI]),
     "omx_run": (_I, [_VP, _I, _I, _I, _I, _I]),
     "omx_detectors_write_text": (_I, [_VP, C.c_char_p, _PI]),

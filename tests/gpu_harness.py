@@ -23,12 +23,12 @@ class OracleFactory:
         return self.orc.medium_dl_custom(*a)
 
 
-def make_pair(orc, deck, precision="fp64", autotune=False, fused=None):
+def make_pair(orc, deck, precision="fp64", autotune=False, form=None):
     d = deck
     gpu = omx.TMxll(d["dimensions"], d["grid_Ndims"], d["npml"], d["boundaries"], d["dt"], d["dr"],
                     mode=d["mode"], precision=precision)
-    if fused is not None:
-        gpu.set_fused(fused)
+    if form is not None:
+        gpu.set_step_form(form)
     cpu = orc.Grid(d["dimensions"], d["grid_Ndims"], d["npml"], d["boundaries"], d["dt"], d["dr"], mode=d["mode"])
     mm = decks.media_map(d, omx.media_map_from_voxels) if d["voxels"] else None
     gg = decks.apply_deck(gpu, d, omx, mm)
@@ -67,8 +67,8 @@ def oracle_detectors(cpu, deck):
     return np.concatenate([cpu.sample(det["type"], det["field"], det["idx"]) for det in deck["detectors"]])
 
 
-def run_both(orc, deck, nsteps, precision="fp64", gpu_mode="calls", use_graph=True, autotune=False, fused=None):
-    gpu, cpu, gg, cg = make_pair(orc, deck, precision, autotune, fused)
+def run_both(orc, deck, nsteps, precision="fp64", gpu_mode="calls", use_graph=True, autotune=False, form=None):
+    gpu, cpu, gg, cg = make_pair(orc, deck, precision, autotune, form)
     st_c = {"tq_old": 0, "t_skip": 0.0}
     trace_c = []
     step_loop(cpu, deck, cg, 1, nsteps, st_c, sample=lambda t: trace_c.append(oracle_detectors(cpu, deck)))

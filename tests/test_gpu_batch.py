@@ -33,7 +33,7 @@ def test_batch_equals_solo_runs(precision, use_graph, autotune):
     solo, batch = [], []
     for k, n in enumerate(SIZES):
         d, g = build(n, 100 + k, precision)
-        g.set_fused(False)    # the batch's arithmetic: the two half-step passes
+        g.set_step_form(omx.STEP_TWO_PASS)    # the batch's arithmetic
         g.run(1, steps, d["n_skip"], d["t_det_print"], use_graph=True)
         solo.append((fields(g), g.drain_detectors()[1]))
         g.kill()

@@ -182,12 +182,13 @@ def test_fp32_within_tolerance(orc_mod, case):
     ((64, 24, 20), (3, 2, 3), True, 100),    # two tiles along x (lane 0 recomputes inside the grid)
 ])
 def test_fp32_fused3d(orc_mod, n, boundaries, drude, steps):
-    """The FP32 single-pass 3D step (opt-in, omx_set_fused): detector traces within the FP32 bar of
+    """The FP32 single-pass 3D step (opt-in, omx_set_step_form): detector traces within the FP32 bar of
     the FP64 oracle through the device loop and through the per-call sequence (omx_step_H
     deferred into the fused pass)."""
     deck = periodic_box_deck(n, boundaries, npml=6, drude=drude)
     for mode in ("run", "calls"):
-        gpu, cpu, gg, cg, tc, tg = run_both(orc_mod, deck, steps, "fp32", mode, use_graph=True, fused=True)
+        gpu, cpu, gg, cg, tc, tg = run_both(orc_mod, deck, steps, "fp32", mode, use_graph=True,
+                                            form=omx.STEP_SINGLE_PASS)
         assert np.max(np.abs(tc)) > 0
         assert trace_error(tg, tc) <= FP32_TOL, (mode, trace_error(tg, tc))
         assert compare_fields(gpu, cpu, deck) <= 10 * FP32_TOL
