@@ -405,16 +405,18 @@ int omx_qgroup_closure_status(omx_ctx *ctx, int group, double *last_error, int *
                               int *fallback_step, int *checks);
 
 /* ---- frequency-domain operator of the inverse-design program ---------------------------------
- * src/freq_domain_inverse_design/operator_mod.f90: init_operator (:41-232) and
- * apply_operator_3D (:518-710); bicgstab_mod.f90:76-243: BICGStab_L.  3D, FP64, the program's
- * units (c0 = eps0 = mu0 = 1).  Vectors are 6 complex components (pl_x, pl_y, pl_z, mi_x, mi_y,
- * mi_z) over [1-g, n+g] per axis with g = n_der ghost cells, x fastest, as interleaved (re, im)
- * doubles: omx_fd_vector_length complex values.  eps_r: nx*ny*nz complex values, x fastest.
- * boundaries: 1 close, 2 periodic (the reference's ghost copies, including its y-axis copies of
- * mi_x into the low ghosts only and mi_y into the high ghosts only), 3 PML (n_pml cells). */
+ * src/freq_domain_inverse_design/operator_mod.f90: init_operator (:41-232), apply_operator_1D
+ * (:293-361), _2D (:364-514), _3D (:518-710); bicgstab_mod.f90:76-243: BICGStab_L.  FP64, the
+ * program's units (c0 = eps0 = mu0 = 1).  Vectors are complex components -- 3D and 2D: pl_x,
+ * pl_y, pl_z, mi_x, mi_y, mi_z; 1D: pl_x, pl_y, mi_x, mi_y -- each over [1-g, n+g] along every
+ * active axis (g = n_der ghost cells), x fastest, as interleaved (re, im) doubles:
+ * omx_fd_vector_length complex values.  eps_r: the grid's nx*ny*nz complex values, x fastest
+ * (ny = nz = 1 below 3D).  boundaries (per active axis): 1 close, 2 periodic (the reference's
+ * ghost copies, including the 3D y-axis copies of mi_x into the low ghosts only and mi_y into the
+ * high ghosts only), 3 PML (n_pml cells). */
 typedef struct omx_fdop omx_fdop;
-int omx_fd_create(const int grid_Ndims[3], int n_pml, int n_der, const int boundaries[3], double dr, double w0,
-                  const double *eps_r, omx_fdop **out);
+int omx_fd_create(int dimensions, const int grid_Ndims[3], int n_pml, int n_der, const int boundaries[3], double dr,
+                  double w0, const double *eps_r, omx_fdop **out);
 int omx_fd_destroy(omx_fdop *op);
 /* replace eps_r (the design's permittivity after an optimisation step; the reference passes its
  * TMedium_eps_r to every apply_operator / BICGStab_L call) */

@@ -1,9 +1,10 @@
 // omx_fd.cu -- the frequency-domain operator of the reference's inverse-design program on the GPU
-// (src/freq_domain_inverse_design/operator_mod.f90:518-710, apply_operator_3D) and its
-// BiCGStab(L) solver (bicgstab_mod.f90:76-243).
+// (src/freq_domain_inverse_design/operator_mod.f90: apply_operator_1D :293-361, _2D :364-514,
+// _3D :518-710) and its BiCGStab(L) solver (bicgstab_mod.f90:76-243).
 //
-// Vectors are 6 complex components (Riemann-Silberstein pl_x, pl_y, pl_z, mi_x, mi_y, mi_z), each
-// an array over [1-g, n+g] per axis (g = n_der ghost cells), x fastest, FP64 as in the reference.
+// Vectors are complex components (Riemann-Silberstein pl_x, pl_y, pl_z, mi_x, mi_y, mi_z; in 1D
+// pl_x, pl_y, mi_x, mi_y), each an array over [1-g, n+g] along every active axis (g = n_der
+// ghost cells), x fastest, FP64 as in the reference.
 // The operator kernel keeps the reference's operand order with FMA contraction off (this file is
 // compiled with -fmad=false), so A f equals the FP64 oracle bit for bit.  The solver's scalar
 // recursion runs on the host exactly as the oracle's; its dot products are reduced on the device
@@ -29,14 +30,20 @@ __host__ __device__ inline cplx cadd(cplx a, cplx b) { return {a.re + b.re, a.im
 __host__ __device__ inline cplx csub(cplx a, cplx b) { return {a.re - b.re, a.im - b.im}; }
 __host__ __device__ inline cplx cmul(cplx a, cplx b) { return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
 __host__ __device__ inline cplx cscale(cplx a, double s) { return {a.re * s, a.im * s}; }
+// complex division by Smith's method (R. L. Smith, CACM 5:435, 1962), the range-reduced form
+// gfortran uses for complex(dp) division under its default Fortran rules
 inline cplx cdiv(cplx a, cplx b)
 {
-    const double d = b.re * b.re + b.im * b.im;
-    return {(a.re * b.re + a.im * b.im) / d, (a.im * b.re - a.re * b.im) / d};
+    if (std::fabs(b.re) < std::fabs(b.im)) {
+        const double t = b.re / b.im, d = b.re * t + b.im;
+        return {(a.re * t + a.im) / d, (a.im * t - a.re) / d};
+    }
+    const double t = b.im / b.re, d = b.im * t + b.re;
+    return {(a.im * t + a.re) / d, (a.im - a.re * t) / d};
 }
 
 struct FdGeom {
-    int nx, ny, nz, g, n_der;
+    int dims, ncomp, nx, ny, nz, g, gy, gz, n_der;   // ny = nz = 1 in 1D, nz = 1 in 2D
     long long px, pxy, len;   // padded row and plane pitch, elements per component
     int per[3];
     double coef[9];
@@ -45,19 +52,19 @@ struct FdGeom {
 
 __device__ inline long long fd_at(const FdGeom &G, int i, int j, int k)   // 1-based interior indices
 {
-    return (long long)(i - 1 + G.g) + G.px * (j - 1 + G.g) + G.pxy * (k - 1 + G.g);
+    return (long long)(i - 1 + G.g) + G.px * (j - 1 + G.gy) + G.pxy * (k - 1 + G.gz);
 }
 
-// periodic ghost copies (operator_mod.f90:549-621): axis 0 over interior y, z; axis 1 over
-// interior x, z, with mi_x only into the low ghosts and mi_y only into the high ones; axis 2 over
-// interior x, y.  One thread per (component, ghost cell pair).
+// periodic ghost copies (1D operator_mod.f90:316-329, 2D :389-452, 3D :549-621): axis 0 over
+// interior y, z; axis 1 over interior x, z (in 3D with mi_x only into the low ghosts and mi_y only
+// into the high ones); axis 2 over interior x, y.  One thread per (component, ghost cell pair).
 __global__ void k_fd_ghosts(cplx *f, FdGeom G, int axis)
 {
     const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     const int na = axis == 0 ? G.nx : (axis == 1 ? G.ny : G.nz);
     const int n1 = axis == 0 ? G.ny : G.nx, n2 = axis == 2 ? G.ny : G.nz;
     const long long per_c = (long long)G.g * n1 * n2;
-    if (q >= 6 * per_c) return;
+    if (q >= G.ncomp * per_c) return;
     const int c = (int)(q / per_c);
     long long r = q % per_c;
     const int t = 1 + (int)(r % G.g);
@@ -69,7 +76,8 @@ __global__ void k_fd_ghosts(cplx *f, FdGeom G, int axis)
         if (axis == 1) return fd_at(G, a1, s, a2);
         return fd_at(G, a1, a2, s);
     };
-    const bool lo = !(axis == 1 && c == 4), hi = !(axis == 1 && c == 3);
+    const bool quirk = axis == 1 && G.dims == 3;
+    const bool lo = !(quirk && c == 4), hi = !(quirk && c == 3);
     if (lo) v[at(1 - t)] = v[at(na + 1 - t)];
     if (hi) v[at(na + t)] = v[at(t)];
 }
@@ -137,14 +145,92 @@ __global__ void __launch_bounds__(128) k_fd_apply(const cplx *__restrict__ f, cp
     Af[p + 5 * G.len] = cadd(cadd(cmul(mC1, csub(dmydx, dmxdy)), cmul(C2, miz[p])), cmul(m3, Ez));
 }
 
-// vector operations over the interior of all six components (rs_operations_subs_mod.f90)
+// apply_operator_1D: one thread per cell; the products keep the reference's order C1 * d * s_inv,
+// and the y components carry no medium term (as written in the reference)
+__global__ void __launch_bounds__(128) k_fd_apply1(const cplx *__restrict__ f, cplx *__restrict__ Af, FdGeom G,
+                                                   const cplx *__restrict__ sx, const cplx *__restrict__ eps)
+{
+    const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (i > G.nx) return;
+    const long long p = fd_at(G, i, 1, 1);
+    const cplx *plx = f, *ply = f + G.len, *mix = f + 2 * G.len, *miy = f + 3 * G.len;
+    const int n = G.n_der;
+    cplx dpxdz = {0, 0}, dpydz = {0, 0}, dmxdz = {0, 0}, dmydz = {0, 0};
+    for (int q = -n; q <= n; ++q) {
+        const double a = G.coef[n + q];
+        dpxdz = cadd(dpxdz, cscale(plx[p + q], a));
+        dpydz = cadd(dpydz, cscale(ply[p + q], a));
+        dmxdz = cadd(dmxdz, cscale(mix[p + q], a));
+        dmydz = cadd(dmydz, cscale(miy[p + q], a));
+    }
+    const cplx C1 = {0.0, G.sign}, mC1 = {-0.0, -G.sign}, C2 = {0.0, -G.w0}, C3 = {0.0, -G.w0 / 2.0}, C4 = {1.0, 0.0};
+    const cplx Ex = cadd(plx[p], mix[p]);
+    const cplx s = sx[i - 1], e = eps[i - 1];
+    const cplx m3 = cmul(C3, csub(e, C4));
+    Af[p] = cadd(cadd(cmul(cmul(mC1, dpydz), s), cmul(C2, plx[p])), cmul(m3, Ex));
+    Af[p + G.len] = cadd(cmul(cmul(C1, dpxdz), s), cmul(C2, ply[p]));
+    Af[p + 2 * G.len] = cadd(cadd(cmul(cmul(C1, dmydz), s), cmul(C2, mix[p])), cmul(m3, Ex));
+    Af[p + 3 * G.len] = cadd(cmul(cmul(mC1, dmxdz), s), cmul(C2, miy[p]));
+}
+
+// apply_operator_2D: one thread per cell; the curl terms carry the opposite sign of the 3D
+// operator's (as written in the reference)
+__global__ void __launch_bounds__(128) k_fd_apply2(const cplx *__restrict__ f, cplx *__restrict__ Af, FdGeom G,
+                                                   const cplx *__restrict__ sx, const cplx *__restrict__ sy,
+                                                   const cplx *__restrict__ eps)
+{
+    const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x, j = 1 + blockIdx.y;
+    if (i > G.nx) return;
+    const long long p = fd_at(G, i, j, 1);
+    const cplx *plx = f, *ply = f + G.len, *plz = f + 2 * G.len, *mix = f + 3 * G.len, *miy = f + 4 * G.len,
+               *miz = f + 5 * G.len;
+    const int n = G.n_der;
+    cplx dpxdy = {0, 0}, dpydx = {0, 0}, dpzdx = {0, 0}, dpzdy = {0, 0};
+    cplx dmxdy = {0, 0}, dmydx = {0, 0}, dmzdx = {0, 0}, dmzdy = {0, 0};
+    for (int q = -n; q <= n; ++q) {
+        const double a = G.coef[n + q];
+        dpydx = cadd(dpydx, cscale(ply[p + q], a));
+        dpzdx = cadd(dpzdx, cscale(plz[p + q], a));
+        dmydx = cadd(dmydx, cscale(miy[p + q], a));
+        dmzdx = cadd(dmzdx, cscale(miz[p + q], a));
+    }
+    for (int q = -n; q <= n; ++q) {
+        const double a = G.coef[n + q];
+        const long long o = p + q * G.px;
+        dpxdy = cadd(dpxdy, cscale(plx[o], a));
+        dpzdy = cadd(dpzdy, cscale(plz[o], a));
+        dmxdy = cadd(dmxdy, cscale(mix[o], a));
+        dmzdy = cadd(dmzdy, cscale(miz[o], a));
+    }
+    const cplx Ex = cadd(plx[p], mix[p]), Ey = cadd(ply[p], miy[p]), Ez = cadd(plz[p], miz[p]);
+    const cplx sxi = sx[i - 1], syj = sy[j - 1];
+    dpxdy = cmul(dpxdy, syj);
+    dpydx = cmul(dpydx, sxi);
+    dpzdx = cmul(dpzdx, sxi);
+    dpzdy = cmul(dpzdy, syj);
+    dmxdy = cmul(dmxdy, syj);
+    dmydx = cmul(dmydx, sxi);
+    dmzdx = cmul(dmzdx, sxi);
+    dmzdy = cmul(dmzdy, syj);
+    const cplx C1 = {0.0, G.sign}, mC1 = {-0.0, -G.sign}, C2 = {0.0, -G.w0}, C3 = {0.0, -G.w0 / 2.0}, C4 = {1.0, 0.0};
+    const cplx e = eps[(long long)(i - 1) + (long long)G.nx * (j - 1)];
+    const cplx m3 = cmul(C3, csub(e, C4));
+    Af[p] = cadd(cadd(cmul(mC1, dpzdy), cmul(C2, plx[p])), cmul(m3, Ex));
+    Af[p + G.len] = cadd(cadd(cmul(C1, dpzdx), cmul(C2, ply[p])), cmul(m3, Ey));
+    Af[p + 2 * G.len] = cadd(cadd(cmul(mC1, csub(dpydx, dpxdy)), cmul(C2, plz[p])), cmul(m3, Ez));
+    Af[p + 3 * G.len] = cadd(cadd(cmul(C1, dmzdy), cmul(C2, mix[p])), cmul(m3, Ex));
+    Af[p + 4 * G.len] = cadd(cadd(cmul(mC1, dmzdx), cmul(C2, miy[p])), cmul(m3, Ey));
+    Af[p + 5 * G.len] = cadd(cadd(cmul(C1, csub(dmydx, dmxdy)), cmul(C2, miz[p])), cmul(m3, Ez));
+}
+
+// vector operations over the interior of every component (rs_operations_subs_mod.f90)
 // mode 0: v1 = v1 + a v2;  mode 1: v1 = a v1 + v2;  mode 2: v1 = a v1
 __global__ void k_fd_lin(cplx *v1, const cplx *v2, cplx a, FdGeom G, int mode)
 {
     const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x, j = 1 + blockIdx.y, k = 1 + blockIdx.z;
     if (i > G.nx) return;
     const long long p = fd_at(G, i, j, k);
-    for (int c = 0; c < 6; ++c) {
+    for (int c = 0; c < G.ncomp; ++c) {
         const long long q = p + c * G.len;
         const cplx x = v1[q];
         if (mode == 0) v1[q] = cadd(x, cmul(a, v2[q]));
@@ -159,7 +245,7 @@ __global__ void k_fd_dot(const cplx *v1, const cplx *v2, FdGeom G, cplx *part)
     __shared__ cplx sh[128];
     const int j = 1 + blockIdx.x, k = 1 + blockIdx.y;
     cplx s = {0, 0};
-    for (int c = 0; c < 6; ++c)
+    for (int c = 0; c < G.ncomp; ++c)
         for (int i = 1 + threadIdx.x; i <= G.nx; i += blockDim.x) {
             const long long q = fd_at(G, i, j, k) + c * G.len;
             const cplx a = {v1[q].re, -v1[q].im};
@@ -217,13 +303,15 @@ dim3 cell_grid(const FdGeom &G) { return dim3((G.nx + 127) / 128, G.ny, G.nz); }
 void fd_apply_dev(omx_fdop *op, cplx *f, cplx *Af)
 {
     const FdGeom &G = op->G;
-    for (int a = 0; a < 3; ++a) {
+    for (int a = 0; a < G.dims; ++a) {
         if (!G.per[a]) continue;
         const int n1 = a == 0 ? G.ny : G.nx, n2 = a == 2 ? G.ny : G.nz;
-        const long long cnt = 6LL * G.g * n1 * n2;
+        const long long cnt = (long long)G.ncomp * G.g * n1 * n2;
         k_fd_ghosts<<<(unsigned)((cnt + 255) / 256), 256, 0, op->s>>>(f, G, a);
     }
-    k_fd_apply<<<cell_grid(G), 128, 0, op->s>>>(f, Af, G, op->sx, op->sy, op->sz, op->eps);
+    if (G.dims == 1) k_fd_apply1<<<cell_grid(G), 128, 0, op->s>>>(f, Af, G, op->sx, op->eps);
+    else if (G.dims == 2) k_fd_apply2<<<cell_grid(G), 128, 0, op->s>>>(f, Af, G, op->sx, op->sy, op->eps);
+    else k_fd_apply<<<cell_grid(G), 128, 0, op->s>>>(f, Af, G, op->sx, op->sy, op->sz, op->eps);
 }
 
 void fd_lin(omx_fdop *op, cplx *v1, const cplx *v2, cplx a, int mode)
@@ -247,12 +335,13 @@ cplx fd_dot(omx_fdop *op, const cplx *v1, const cplx *v2)
 
 extern "C" {
 
-int omx_fd_create(const int grid_Ndims[3], int n_pml, int n_der, const int boundaries[3], double dr, double w0,
-                  const double *eps_r, omx_fdop **out)
+int omx_fd_create(int dimensions, const int grid_Ndims[3], int n_pml, int n_der, const int boundaries[3], double dr,
+                  double w0, const double *eps_r, omx_fdop **out)
 {
-    if (!grid_Ndims || !boundaries || !eps_r || !out || n_der < 1 || n_der > 4 || !(dr > 0) || !(w0 > 0))
-        return fd_fail(OMX_ERR_ARG, "bad argument (n_der 1..4)");
-    for (int a = 0; a < 3; ++a) {
+    if (!grid_Ndims || !boundaries || !eps_r || !out || n_der < 1 || n_der > 4 || !(dr > 0) || !(w0 > 0) ||
+        dimensions < 1 || dimensions > 3)
+        return fd_fail(OMX_ERR_ARG, "bad argument (dimensions 1..3, n_der 1..4)");
+    for (int a = 0; a < dimensions; ++a) {
         if (grid_Ndims[a] < 1) return fd_fail(OMX_ERR_ARG, "grid sizes must be >= 1");
         if (boundaries[a] < 1 || boundaries[a] > 3) return fd_fail(OMX_ERR_ARG, "boundaries: 1 close, 2 periodic, 3 PML");
         if (boundaries[a] == 3 && grid_Ndims[a] < 2 * n_pml) return fd_fail(OMX_ERR_ARG, "PML slabs do not fit");
@@ -267,15 +356,19 @@ int omx_fd_create(const int grid_Ndims[3], int n_pml, int n_der, const int bound
     omx_fdop *op = new omx_fdop;
     try {
         FdGeom &G = op->G;
+        G.dims = dimensions;
+        G.ncomp = dimensions == 1 ? 4 : 6;
         G.nx = grid_Ndims[0];
-        G.ny = grid_Ndims[1];
-        G.nz = grid_Ndims[2];
+        G.ny = dimensions >= 2 ? grid_Ndims[1] : 1;
+        G.nz = dimensions == 3 ? grid_Ndims[2] : 1;
         G.g = n_der;
+        G.gy = dimensions >= 2 ? n_der : 0;
+        G.gz = dimensions == 3 ? n_der : 0;
         G.n_der = n_der;
         G.px = G.nx + 2 * G.g;
-        G.pxy = G.px * (G.ny + 2 * G.g);
-        G.len = G.pxy * (G.nz + 2 * G.g);
-        for (int a = 0; a < 3; ++a) G.per[a] = boundaries[a] == 2;
+        G.pxy = G.px * (G.ny + 2 * G.gy);
+        G.len = G.pxy * (G.nz + 2 * G.gz);
+        for (int a = 0; a < 3; ++a) G.per[a] = a < dimensions && boundaries[a] == 2;
         G.w0 = w0;
         // operator_mod.f90:97-140: central-difference coefficients of order 2 n_der, / dr
         static const double C[4][9] = {{-0.5, 0.0, 0.5},
@@ -290,7 +383,7 @@ int omx_fd_create(const int grid_Ndims[3], int n_pml, int n_der, const int bound
         const double m = 3.0, kmax = 5.0, sig_max = 0.8 * (m + 1.0) / (dr * std::sqrt(1.0 / 1.0));
         for (int a = 0; a < 3; ++a) {
             s[a].assign(n[a], cplx{1.0, 0.0});
-            if (boundaries[a] != 3) continue;
+            if (a >= dimensions || boundaries[a] != 3) continue;
             for (int i = 1; i <= n_pml; ++i) {
                 const double r = (double)(n_pml - i + 1) / (double)n_pml;
                 const double sig = sig_max * std::pow(r, m);
@@ -341,7 +434,7 @@ int omx_fd_destroy(omx_fdop *op)
     return OMX_OK;
 }
 
-long long omx_fd_vector_length(const omx_fdop *op) { return op ? 6 * op->G.len : 0; }
+long long omx_fd_vector_length(const omx_fdop *op) { return op ? (long long)op->G.ncomp * op->G.len : 0; }
 
 int omx_fd_apply(omx_fdop *op, const double *f, double *Af, int transpose)
 {
@@ -349,7 +442,7 @@ int omx_fd_apply(omx_fdop *op, const double *f, double *Af, int transpose)
     cplx *df = nullptr, *dAf = nullptr;
     try {
         op->G.sign = transpose ? -1.0 : 1.0;
-        const size_t bytes = sizeof(cplx) * 6 * op->G.len;
+        const size_t bytes = sizeof(cplx) * op->G.ncomp * op->G.len;
         fck(cudaMalloc(&df, bytes), "alloc");
         fck(cudaMalloc(&dAf, bytes), "alloc");
         fck(cudaMemcpy(df, f, bytes, cudaMemcpyHostToDevice), "upload");
@@ -376,7 +469,7 @@ int omx_fd_time_apply(omx_fdop *op, int reps, double *ms_per_apply)
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     try {
         op->G.sign = 1.0;
-        const size_t n = 6 * (size_t)op->G.len;
+        const size_t n = (size_t)op->G.ncomp * op->G.len;
         std::vector<cplx> h(n);
         unsigned long long x = 88172645463325252ull;
         for (auto &v : h) {
@@ -420,7 +513,7 @@ int omx_fd_solve(omx_fdop *op, const double *j_vec, double *f_io, int transpose,
     try {
         FdGeom &G = op->G;
         G.sign = transpose ? -1.0 : 1.0;
-        const size_t bytes = sizeof(cplx) * 6 * G.len;
+        const size_t bytes = sizeof(cplx) * G.ncomp * G.len;
         const size_t need = 5 + 2 * (size_t)(L + 1);
         while (op->vecs.size() < need) {
             cplx *v = nullptr;

@@ -528,21 +528,23 @@ class Closure:
 
 class FDOperator:
     """The frequency-domain operator of the inverse-design program and its BiCGStab(L) solver
-    (omx_fd_*).  Vectors: complex arrays [6][nz + 2g][ny + 2g][nx + 2g], g = n_der."""
+    (omx_fd_*) on a 1D, 2D or 3D grid n.  Vectors: complex arrays [6][nz+2g][ny+2g][nx+2g] (3D),
+    [6][ny+2g][nx+2g] (2D), [4][nx+2g] (1D), g = n_der; eps of shape n."""
 
     def __init__(self, n, n_pml, n_der, boundaries, dr, w0, eps):
         self.n, self.g = tuple(int(v) for v in n), int(n_der)
-        e = np.ascontiguousarray(np.asarray(eps, np.complex128).transpose(2, 1, 0))
-        nn = (C.c_int * 3)(*self.n)
-        bb = (C.c_int * 3)(*[int(b) for b in boundaries])
+        dims = len(self.n)
+        e = np.ascontiguousarray(np.asarray(eps, np.complex128).reshape(self.n).transpose())
+        nn = (C.c_int * 3)(*(list(self.n) + [1] * (3 - dims)))
+        bb = (C.c_int * 3)(*([int(b) for b in boundaries] + [1] * (3 - len(boundaries))))
         self._op = C.c_void_p()
-        A.check(lib().omx_fd_create(nn, int(n_pml), int(n_der), bb, float(dr), float(w0),
+        A.check(lib().omx_fd_create(dims, nn, int(n_pml), int(n_der), bb, float(dr), float(w0),
                                     e.view(np.float64).ctypes.data_as(A._PD), C.byref(self._op)))
 
     def shape(self):
-        nx, ny, nz = self.n
         g = self.g
-        return (6, nz + 2 * g, ny + 2 * g, nx + 2 * g)
+        pad = tuple(v + 2 * g for v in reversed(self.n))
+        return ((4,) if len(self.n) == 1 else (6,)) + pad
 
     def zeros(self):
         return np.zeros(self.shape(), np.complex128)
@@ -564,8 +566,7 @@ class FDOperator:
         return f, bool(conv.value), err.value, it.value
 
     def set_eps(self, eps):
-        e = np.ascontiguousarray(np.asarray(eps, np.complex128).transpose(2, 1, 0))
-        assert e.shape == self.n[::-1]
+        e = np.ascontiguousarray(np.asarray(eps, np.complex128).reshape(self.n).transpose())
         A.check(lib().omx_fd_set_eps(self._op, e.view(np.float64).ctypes.data_as(A._PD)))
 
     def time_apply(self, reps=20):

@@ -131,7 +131,7 @@ SIGNATURES = {
     "omx_closure_trajectories": (_I, [_I, _I, _I, _I, _D, _PD, _PD, _D, _D, _PF, _PF]),
     "omx_qgroup_attach_closure": (_I, [_VP, _I, _VP, _D, _D, _I]),
     "omx_qgroup_closure_status": (_I, [_VP, _I, _PD, _PI, _PI, _PI]),
-    "omx_fd_create": (_I, [_PI, _I, _I, _PI, _D, _D, _PD, C.POINTER(_VP)]),
+    "omx_fd_create": (_I, [_I, _PI, _I, _I, _PI, _D, _D, _PD, C.POINTER(_VP)]),
     "omx_fd_destroy": (_I, [_VP]),
     "omx_fd_vector_length": (C.c_longlong, [_VP]),
     "omx_fd_apply": (_I, [_VP, _PD, _PD, _I]),

@@ -4,6 +4,8 @@
  *
  * Follows src/freq_domain_inverse_design/ of the reference:
  *   operator_mod.f90:41-232   init_operator (derivative coefficients, PML stretch factors)
+ *   operator_mod.f90:293-361  apply_operator_1D (components pl_x, pl_y, mi_x, mi_y)
+ *   operator_mod.f90:364-514  apply_operator_2D
  *   operator_mod.f90:518-710  apply_operator_3D (periodic ghost copies, curl of the
  *                             Riemann-Silberstein vectors, medium term)
  *   bicgstab_mod.f90:76-243   BICGStab_L
@@ -26,16 +28,28 @@ static cplx cadd(cplx a, cplx b) { cplx r = {a.re + b.re, a.im + b.im}; return r
 static cplx csub(cplx a, cplx b) { cplx r = {a.re - b.re, a.im - b.im}; return r; }
 static cplx cmul(cplx a, cplx b) { cplx r = {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; return r; }
 static cplx cscale(cplx a, double s) { cplx r = {a.re * s, a.im * s}; return r; }
+/* complex division by Smith's method (R. L. Smith, CACM 5:435, 1962), the range-reduced form
+ * gfortran uses for complex(dp) division under its default Fortran rules */
 static cplx cdiv(cplx a, cplx b)
 {
-    const double d = b.re * b.re + b.im * b.im;
-    cplx r = {(a.re * b.re + a.im * b.im) / d, (a.im * b.re - a.re * b.im) / d};
+    cplx r;
+    if (fabs(b.re) < fabs(b.im)) {
+        const double t = b.re / b.im, d = b.re * t + b.im;
+        r.re = (a.re * t + a.im) / d;
+        r.im = (a.im * t - a.re) / d;
+    } else {
+        const double t = b.im / b.re, d = b.im * t + b.re;
+        r.re = (a.im * t + a.re) / d;
+        r.im = (a.im - a.re * t) / d;
+    }
     return r;
 }
 
-/* operator state: padded component arrays are (nx+2g) x (ny+2g) x (nz+2g), x fastest */
+/* operator state: padded component arrays are (nx+2g) x (ny+2gy) x (nz+2gz), x fastest, with
+ * ghosts only along the active axes (ny = nz = 1 in 1D, nz = 1 in 2D); 4 components in 1D
+ * (pl_x, pl_y, mi_x, mi_y), 6 otherwise (pl_x, pl_y, pl_z, mi_x, mi_y, mi_z) */
 typedef struct {
-    int nx, ny, nz, g, n_der, boundaries[3];
+    int dims, ncomp, nx, ny, nz, g, gy, gz, n_der, boundaries[3];
     double dr, w0;
     double coef[9];            /* coef_der(-n..n) / dr at coef[n + ii] */
     cplx *sx, *sy, *sz;        /* s_inv per interior index (0-based) */
@@ -44,23 +58,30 @@ typedef struct {
 
 static long long fd_idx(const fd_op *A, int i, int j, int k)   /* 1-based interior indices */
 {
-    const long long px = A->nx + 2 * A->g, py = A->ny + 2 * A->g;
-    return (long long)(i - 1 + A->g) + px * ((long long)(j - 1 + A->g) + py * (long long)(k - 1 + A->g));
+    const long long px = A->nx + 2 * A->g, py = A->ny + 2 * A->gy;
+    return (long long)(i - 1 + A->g) + px * ((long long)(j - 1 + A->gy) + py * (long long)(k - 1 + A->gz));
 }
 
-long long fd_vec_len(int nx, int ny, int nz, int n_der)
+/* padded length of one component */
+long long fd_vec_len(int dims, int nx, int ny, int nz, int n_der)
 {
-    return (long long)(nx + 2 * n_der) * (ny + 2 * n_der) * (nz + 2 * n_der);
+    const int gy = dims >= 2 ? n_der : 0, gz = dims == 3 ? n_der : 0;
+    return (long long)(nx + 2 * n_der) * (ny + 2 * gy) * (nz + 2 * gz);
 }
+static long long fd_len(const fd_op *A) { return fd_vec_len(A->dims, A->nx, A->ny, A->nz, A->g); }
 
 /* operator_mod.f90:97-140 (coefficients) and :185-232 (stretch factors) */
-fd_op *fd_create(int nx, int ny, int nz, int n_pml, int n_der, const int boundaries[3], double dr, double w0,
-                 const double *eps_re_im)
+fd_op *fd_create(int dims, int nx, int ny, int nz, int n_pml, int n_der, const int boundaries[3], double dr,
+                 double w0, const double *eps_re_im)
 {
     static const double C1[3] = {-0.5, 0.0, 0.5};
     fd_op *A = (fd_op *)calloc(1, sizeof(fd_op));
     int i, q;
+    if (dims < 3) nz = 1;
+    if (dims < 2) ny = 1;
+    A->dims = dims; A->ncomp = dims == 1 ? 4 : 6;
     A->nx = nx; A->ny = ny; A->nz = nz; A->g = n_der; A->n_der = n_der;
+    A->gy = dims >= 2 ? n_der : 0; A->gz = dims == 3 ? n_der : 0;
     for (q = 0; q < 3; ++q) A->boundaries[q] = boundaries[q];
     A->dr = dr; A->w0 = w0;
     {
@@ -89,7 +110,7 @@ fd_op *fd_create(int nx, int ny, int nz, int n_pml, int n_der, const int boundar
         cplx *s[3] = {A->sx, A->sy, A->sz};
         const int n[3] = {nx, ny, nz};
         int a;
-        for (a = 0; a < 3; ++a) {
+        for (a = 0; a < dims; ++a) {
             if (boundaries[a] != 3) continue;
             for (i = 1; i <= n_pml; ++i) {
                 const double r = (double)(n_pml - i + 1) / (double)n_pml;
@@ -114,25 +135,27 @@ void fd_destroy(fd_op *A)
     free(A->sx); free(A->sy); free(A->sz); free(A->eps); free(A);
 }
 
-/* periodic ghost copies, operator_mod.f90:549-621 (non-MPI branch), in the reference's order:
- * x ghosts over interior y, z; y ghosts over interior x, z; z ghosts over interior x, y.  The
- * y block copies mi_x only into the low ghosts and mi_y only into the high ghosts (as written
- * in the reference), so the other two stay zero. */
-static void fd_ghosts(const fd_op *A, cplx *f[6])
+/* periodic ghost copies (non-MPI branches), in the reference's order.  1D (operator_mod.f90:
+ * 316-329): the four components along x.  2D (:389-452): all six components, x ghosts over the
+ * interior rows, then y ghosts over the interior columns.  3D (:549-621): x ghosts over interior
+ * y, z; y ghosts over interior x, z; z ghosts over interior x, y -- and the 3D y block copies
+ * mi_x only into the low ghosts and mi_y only into the high ghosts (as written in the
+ * reference), so the other two stay zero. */
+static void fd_ghosts(const fd_op *A, cplx **f)
 {
     const int nx = A->nx, ny = A->ny, nz = A->nz, g = A->g;
     int c, i, j, k, t;
     if (A->boundaries[0] == 2)
-        for (c = 0; c < 6; ++c)
+        for (c = 0; c < A->ncomp; ++c)
             for (k = 1; k <= nz; ++k)
                 for (j = 1; j <= ny; ++j)
                     for (t = 1; t <= g; ++t) {
                         f[c][fd_idx(A, 1 - t, j, k)] = f[c][fd_idx(A, nx + 1 - t, j, k)];
                         f[c][fd_idx(A, nx + t, j, k)] = f[c][fd_idx(A, t, j, k)];
                     }
-    if (A->boundaries[1] == 2)
+    if (A->dims >= 2 && A->boundaries[1] == 2)
         for (c = 0; c < 6; ++c) {
-            const int lo = !(c == 4), hi = !(c == 3);   /* mi_x (3): low only; mi_y (4): high only */
+            const int lo = A->dims == 2 || c != 4, hi = A->dims == 2 || c != 3;   /* the 3D quirk */
             for (k = 1; k <= nz; ++k)
                 for (t = 1; t <= g; ++t)
                     for (i = 1; i <= nx; ++i) {
@@ -140,7 +163,7 @@ static void fd_ghosts(const fd_op *A, cplx *f[6])
                         if (hi) f[c][fd_idx(A, i, ny + t, k)] = f[c][fd_idx(A, i, t, k)];
                     }
         }
-    if (A->boundaries[2] == 2)
+    if (A->dims == 3 && A->boundaries[2] == 2)
         for (c = 0; c < 6; ++c)
             for (t = 1; t <= g; ++t)
                 for (j = 1; j <= ny; ++j)
@@ -150,22 +173,106 @@ static void fd_ghosts(const fd_op *A, cplx *f[6])
                     }
 }
 
-/* apply_operator_3D (operator_mod.f90:518-710); f and Af are 6 padded complex arrays
- * (pl_x, pl_y, pl_z, mi_x, mi_y, mi_z); the ghosts of f are refreshed first */
+/* apply_operator_1D (operator_mod.f90:293-361): the derivative runs along the grid's one axis
+ * (named z there); the products keep the reference's left-to-right order, C1 * d * s_inv, and
+ * the y components carry no medium term (as written in the reference) */
+static void fd_apply1(const fd_op *A, cplx **f, cplx **Af, cplx C1, cplx C2, cplx C3, cplx C4)
+{
+    const int n = A->n_der;
+    int i, q;
+    for (i = 1; i <= A->nx; ++i) {
+        cplx dpxdz = {0, 0}, dpydz = {0, 0}, dmxdz = {0, 0}, dmydz = {0, 0};
+        const long long p = fd_idx(A, i, 1, 1);
+        for (q = -n; q <= n; ++q) {
+            const double a = A->coef[n + q];
+            dpxdz = cadd(dpxdz, cscale(f[0][p + q], a));
+            dpydz = cadd(dpydz, cscale(f[1][p + q], a));
+            dmxdz = cadd(dmxdz, cscale(f[2][p + q], a));
+            dmydz = cadd(dmydz, cscale(f[3][p + q], a));
+        }
+        {
+            const cplx Ex = cadd(f[0][p], f[2][p]);
+            const cplx s = A->sx[i - 1], e = A->eps[i - 1];
+            const cplx m3 = cmul(C3, csub(e, C4));
+            const cplx mC1 = {-C1.re, -C1.im};
+            Af[0][p] = cadd(cadd(cmul(cmul(mC1, dpydz), s), cmul(C2, f[0][p])), cmul(m3, Ex));
+            Af[1][p] = cadd(cmul(cmul(C1, dpxdz), s), cmul(C2, f[1][p]));
+            Af[2][p] = cadd(cadd(cmul(cmul(C1, dmydz), s), cmul(C2, f[2][p])), cmul(m3, Ex));
+            Af[3][p] = cadd(cmul(cmul(mC1, dmxdz), s), cmul(C2, f[3][p]));
+        }
+    }
+}
+
+/* apply_operator_2D (operator_mod.f90:364-514): its curl terms carry the opposite sign of the 3D
+ * operator's (pl_x = -C1 dpz/dy ..., as written in the reference) */
+static void fd_apply2(const fd_op *A, cplx **f, cplx **Af, cplx C1, cplx C2, cplx C3, cplx C4)
+{
+    const int n = A->n_der;
+    const long long sy = A->nx + 2 * A->g;
+    int i, j, q;
+    for (j = 1; j <= A->ny; ++j)
+        for (i = 1; i <= A->nx; ++i) {
+            cplx dpxdy = {0, 0}, dpydx = {0, 0}, dpzdx = {0, 0}, dpzdy = {0, 0};
+            cplx dmxdy = {0, 0}, dmydx = {0, 0}, dmzdx = {0, 0}, dmzdy = {0, 0};
+            const long long p = fd_idx(A, i, j, 1);
+            for (q = -n; q <= n; ++q) {
+                const double a = A->coef[n + q];
+                dpydx = cadd(dpydx, cscale(f[1][p + q], a));
+                dpzdx = cadd(dpzdx, cscale(f[2][p + q], a));
+                dmydx = cadd(dmydx, cscale(f[4][p + q], a));
+                dmzdx = cadd(dmzdx, cscale(f[5][p + q], a));
+            }
+            for (q = -n; q <= n; ++q) {
+                const double a = A->coef[n + q];
+                dpxdy = cadd(dpxdy, cscale(f[0][p + q * sy], a));
+                dpzdy = cadd(dpzdy, cscale(f[2][p + q * sy], a));
+                dmxdy = cadd(dmxdy, cscale(f[3][p + q * sy], a));
+                dmzdy = cadd(dmzdy, cscale(f[5][p + q * sy], a));
+            }
+            {
+                const cplx Ex = cadd(f[0][p], f[3][p]), Ey = cadd(f[1][p], f[4][p]), Ez = cadd(f[2][p], f[5][p]);
+                const cplx sxi = A->sx[i - 1], syj = A->sy[j - 1];
+                const cplx e = A->eps[(size_t)(i - 1) + (size_t)A->nx * (j - 1)];
+                const cplx m3 = cmul(C3, csub(e, C4));
+                const cplx mC1 = {-C1.re, -C1.im};
+                dpxdy = cmul(dpxdy, syj); dpydx = cmul(dpydx, sxi);
+                dpzdx = cmul(dpzdx, sxi); dpzdy = cmul(dpzdy, syj);
+                dmxdy = cmul(dmxdy, syj); dmydx = cmul(dmydx, sxi);
+                dmzdx = cmul(dmzdx, sxi); dmzdy = cmul(dmzdy, syj);
+                Af[0][p] = cadd(cadd(cmul(mC1, dpzdy), cmul(C2, f[0][p])), cmul(m3, Ex));
+                Af[1][p] = cadd(cadd(cmul(C1, dpzdx), cmul(C2, f[1][p])), cmul(m3, Ey));
+                Af[2][p] = cadd(cadd(cmul(mC1, csub(dpydx, dpxdy)), cmul(C2, f[2][p])), cmul(m3, Ez));
+                Af[3][p] = cadd(cadd(cmul(C1, dmzdy), cmul(C2, f[3][p])), cmul(m3, Ex));
+                Af[4][p] = cadd(cadd(cmul(mC1, dmzdx), cmul(C2, f[4][p])), cmul(m3, Ey));
+                Af[5][p] = cadd(cadd(cmul(C1, csub(dmydx, dmxdy)), cmul(C2, f[5][p])), cmul(m3, Ez));
+            }
+        }
+}
+
+/* apply_operator (operator_mod.f90:261-289) for 1D / 2D / 3D; f and Af are ncomp padded complex
+ * arrays; the ghosts of f are refreshed first */
 void fd_apply(const fd_op *A, double *f_flat, double *Af_flat, int transpose)
 {
-    const long long len = fd_vec_len(A->nx, A->ny, A->nz, A->g);
+    const long long len = fd_len(A);
     cplx *f[6], *Af[6];
     int c, i, j, k, q;
     const double sign = transpose ? -1.0 : 1.0;
     /* C1 = sign c0 i, C2 = -w0 i, C3 = -w0 i / (2 eps0), C4 = eps0 */
     const cplx C1 = {0.0, sign}, C2 = {0.0, -A->w0}, C3 = {0.0, -A->w0 / 2.0}, C4 = {1.0, 0.0};
     const int n = A->n_der;
-    for (c = 0; c < 6; ++c) {
+    for (c = 0; c < A->ncomp; ++c) {
         f[c] = (cplx *)f_flat + c * len;
         Af[c] = (cplx *)Af_flat + c * len;
     }
     fd_ghosts(A, f);
+    if (A->dims == 1) {
+        fd_apply1(A, f, Af, C1, C2, C3, C4);
+        return;
+    }
+    if (A->dims == 2) {
+        fd_apply2(A, f, Af, C1, C2, C3, C4);
+        return;
+    }
     for (k = 1; k <= A->nz; ++k)
         for (j = 1; j <= A->ny; ++j)
             for (i = 1; i <= A->nx; ++i) {
@@ -173,7 +280,7 @@ void fd_apply(const fd_op *A, double *f_flat, double *Af_flat, int transpose)
                 cplx dpxdy = {0, 0}, dpzdy = {0, 0}, dmxdy = {0, 0}, dmzdy = {0, 0};
                 cplx dpxdz = {0, 0}, dpydz = {0, 0}, dmxdz = {0, 0}, dmydz = {0, 0};
                 const long long p = fd_idx(A, i, j, k);
-                const long long sy = A->nx + 2 * A->g, sz = sy * (A->ny + 2 * A->g);
+                const long long sy = A->nx + 2 * A->g, sz = sy * (A->ny + 2 * A->gy);
                 for (q = -n; q <= n; ++q) {
                     const double a = A->coef[n + q];
                     dpydx = cadd(dpydx, cscale(f[1][p + q], a));
@@ -223,10 +330,10 @@ void fd_apply(const fd_op *A, double *f_flat, double *Af_flat, int transpose)
 /* ---- BiCGStab(L), bicgstab_mod.f90:76-243 ------------------------------------------------- */
 static cplx fd_dot(const fd_op *A, const double *v1, const double *v2)
 {
-    const long long len = fd_vec_len(A->nx, A->ny, A->nz, A->g);
+    const long long len = fd_len(A);
     cplx s = {0, 0};
     int c, i, j, k;
-    for (c = 0; c < 6; ++c) {
+    for (c = 0; c < A->ncomp; ++c) {
         cplx sc = {0, 0};
         for (k = 1; k <= A->nz; ++k)
             for (j = 1; j <= A->ny; ++j)
@@ -242,9 +349,9 @@ static cplx fd_dot(const fd_op *A, const double *v1, const double *v2)
 /* v1 = v1 + a v2 (interior) */
 static void fd_axpy(const fd_op *A, double *v1, const double *v2, cplx a)
 {
-    const long long len = fd_vec_len(A->nx, A->ny, A->nz, A->g);
+    const long long len = fd_len(A);
     int c, i, j, k;
-    for (c = 0; c < 6; ++c)
+    for (c = 0; c < A->ncomp; ++c)
         for (k = 1; k <= A->nz; ++k)
             for (j = 1; j <= A->ny; ++j)
                 for (i = 1; i <= A->nx; ++i) {
@@ -257,9 +364,9 @@ static void fd_axpy(const fd_op *A, double *v1, const double *v2, cplx a)
 /* v1 = a v1 (interior) */
 static void fd_scale(const fd_op *A, double *v1, cplx a)
 {
-    const long long len = fd_vec_len(A->nx, A->ny, A->nz, A->g);
+    const long long len = fd_len(A);
     int c, i, j, k;
-    for (c = 0; c < 6; ++c)
+    for (c = 0; c < A->ncomp; ++c)
         for (k = 1; k <= A->nz; ++k)
             for (j = 1; j <= A->ny; ++j)
                 for (i = 1; i <= A->nx; ++i) {
@@ -272,9 +379,9 @@ static void fd_scale(const fd_op *A, double *v1, cplx a)
 /* v1 = a v1 + v2 (interior) */
 static void fd_xpay(const fd_op *A, double *v1, const double *v2, cplx a)
 {
-    const long long len = fd_vec_len(A->nx, A->ny, A->nz, A->g);
+    const long long len = fd_len(A);
     int c, i, j, k;
-    for (c = 0; c < 6; ++c)
+    for (c = 0; c < A->ncomp; ++c)
         for (k = 1; k <= A->nz; ++k)
             for (j = 1; j <= A->ny; ++j)
                 for (i = 1; i <= A->nx; ++i) {
@@ -289,7 +396,7 @@ static void fd_xpay(const fd_op *A, double *v1, const double *v2, cplx a)
 int fd_bicgstab_l(const fd_op *A, const double *j_vec, double *f_out, int transpose, double tol, int n_max, int L,
                   int *converged, double *abs_err)
 {
-    const long long len2 = 12 * fd_vec_len(A->nx, A->ny, A->nz, A->g);   /* doubles per vector */
+    const long long len2 = 2LL * A->ncomp * fd_len(A);   /* doubles per vector */
     double *r0 = (double *)calloc(len2, sizeof(double));
     double *r = (double *)calloc(len2 * (L + 1), sizeof(double));
     double *u = (double *)calloc(len2 * (L + 1), sizeof(double));

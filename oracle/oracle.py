@@ -95,9 +95,10 @@ def lib():
             "orc_emitter_step": (None, [C.c_int, _PD, _PD, C.c_double, C.c_double]),
             "orc_sample": (None, [_VP, C.c_int, C.c_int, C.c_int, _P32, _PD]),
             "orc_num_threads": (C.c_int, []),
-            "fd_create": (_VP, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _PI, C.c_double, C.c_double, _PD]),
+            "fd_create": (_VP, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _PI, C.c_double, C.c_double,
+                                _PD]),
             "fd_destroy": (None, [_VP]),
-            "fd_vec_len": (C.c_longlong, [C.c_int, C.c_int, C.c_int, C.c_int]),
+            "fd_vec_len": (C.c_longlong, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]),
             "fd_apply": (None, [_VP, _PD, _PD, C.c_int]),
             "fd_bicgstab_l": (C.c_int, [_VP, _PD, _PD, C.c_int, C.c_double, C.c_int, C.c_int, _PI, _PD]),
         }
@@ -296,22 +297,30 @@ class Grid:
         return out
 
 
+def fd_shape(n, n_der):
+    """Array shape of a frequency-domain vector on grid n (1, 2 or 3 sizes): 3D [6][nz+2g][ny+2g]
+    [nx+2g], 2D [6][ny+2g][nx+2g], 1D [4][nx+2g] (components pl_x, pl_y, (pl_z,) mi_x, mi_y,
+    (mi_z); g = n_der ghost cells on each side of every axis)."""
+    g = n_der
+    pad = tuple(v + 2 * g for v in reversed(n))
+    return ((4,) if len(n) == 1 else (6,)) + pad
+
+
 class FDOperator:
-    """The frequency-domain operator and its BiCGStab(L) solver (fd_oracle.c).  Vectors are
-    complex arrays [6][nz + 2g][ny + 2g][nx + 2g] (components pl_x, pl_y, pl_z, mi_x, mi_y,
-    mi_z; g = n_der ghost cells on every side)."""
+    """The frequency-domain operator and its BiCGStab(L) solver (fd_oracle.c) on a 1D, 2D or 3D
+    grid n; vectors as fd_shape describes, eps_r of shape n."""
 
     def __init__(self, n, n_pml, n_der, boundaries, dr, w0, eps):
-        self.n, self.g = tuple(n), n_der
-        eps = np.ascontiguousarray(np.asarray(eps, np.complex128).transpose(2, 1, 0))   # x fastest
-        b = np.asarray(boundaries, np.int32)
-        self._h = lib().fd_create(n[0], n[1], n[2], n_pml, n_der, b.ctypes.data_as(_PI), float(dr), float(w0),
-                                  eps.view(np.float64).ctypes.data_as(_PD))
+        self.n, self.g = tuple(int(v) for v in n), n_der
+        dims = len(self.n)
+        nn = list(self.n) + [1] * (3 - dims)
+        eps = np.ascontiguousarray(np.asarray(eps, np.complex128).reshape(self.n).transpose())   # x fastest
+        b = np.asarray(list(boundaries) + [1] * (3 - len(boundaries)), np.int32)
+        self._h = lib().fd_create(dims, nn[0], nn[1], nn[2], n_pml, n_der, b.ctypes.data_as(_PI), float(dr),
+                                  float(w0), eps.view(np.float64).ctypes.data_as(_PD))
 
     def shape(self):
-        nx, ny, nz = self.n
-        g = self.g
-        return (6, nz + 2 * g, ny + 2 * g, nx + 2 * g)
+        return fd_shape(self.n, self.g)
 
     def zeros(self):
         return np.zeros(self.shape(), np.complex128)

@@ -81,3 +81,50 @@ def test_set_eps_replaces_the_permittivity():
     f[:, g:-g, g:-g, g:-g] = rng.normal(size=f[:, g:-g, g:-g, g:-g].shape) + 0.5j
     assert np.array_equal(G.apply(f)[:, g:-g, g:-g, g:-g], O.apply(f)[:, g:-g, g:-g, g:-g])
     G.kill()
+
+
+def interior_nd(g, v, n):
+    return v[(slice(None),) + tuple(slice(g, g + m) for m in reversed(n))]
+
+
+@pytest.mark.parametrize("n,n_der,bnd,transpose", [
+    ((37,), 1, (2,), False),                 # apply_operator_1D, periodic
+    ((40,), 3, (3,), True),                  # 1D PML, adjoint sign
+    ((21, 17), 2, (2, 2), False),            # apply_operator_2D, periodic on both axes
+    ((24, 19), 4, (3, 2), True),             # 2D PML x / periodic y, eighth order, adjoint
+    ((18, 26), 1, (3, 3), False),            # 2D PML on every face
+])
+def test_operator_1d_2d_bit_identical(n, n_der, bnd, transpose):
+    rng = np.random.default_rng(sum(n) + n_der)
+    eps = 1.0 + 11.1 * (rng.random(n) < 0.4) + 0.02j * rng.random(n)
+    G = omx.FDOperator(n, 3, n_der, bnd, 0.3, 0.9, eps)
+    O = oracle.FDOperator(n, 3, n_der, bnd, 0.3, 0.9, eps)
+    assert G.shape() == O.shape()
+    f = G.zeros()
+    fi = interior_nd(n_der, f, n)
+    fi[:] = rng.normal(size=fi.shape) + 1j * rng.normal(size=fi.shape)
+    a = interior_nd(n_der, G.apply(f, transpose), n)
+    b = interior_nd(n_der, O.apply(f, transpose), n)
+    assert np.max(np.abs(b)) > 0
+    assert np.array_equal(a, b)
+    G.kill()
+
+
+@pytest.mark.parametrize("n,bnd", [((80,), (3,)), ((26, 22), (3, 3)), ((20, 24), (2, 3))])
+def test_bicgstab_1d_2d_matches_oracle(n, bnd):
+    rng = np.random.default_rng(len(n) + 7)
+    eps = 1.0 + 1.25 * (rng.random(n) < 0.3) + 0.05j
+    G = omx.FDOperator(n, 4, 2, bnd, 0.3, 1.2, eps)
+    O = oracle.FDOperator(n, 4, 2, bnd, 0.3, 1.2, eps)
+    j = G.zeros()
+    ji = interior_nd(2, j, n)
+    ji[:] = rng.normal(size=ji.shape) + 1j * rng.normal(size=ji.shape)
+    fg, cg, eg, ig = G.solve(j, G.zeros(), 1e-10, 2000, 2)
+    fo, co, eo, io = O.solve(j, O.zeros(), 1e-10, 2000, 2)
+    assert co and eo <= 1e-10
+    assert cg and eg <= 1e-10, (cg, eg, ig, io)
+    res = interior_nd(2, O.apply(fg), n) - ji
+    assert np.linalg.norm(res) <= 1e-9 * np.linalg.norm(ji)
+    d = interior_nd(2, fg - fo, n)
+    assert np.linalg.norm(d) <= 1e-7 * np.linalg.norm(interior_nd(2, fo, n))
+    G.kill()
