@@ -2500,6 +2500,7 @@ struct omx_batch {
     cudaStream_t stream = nullptr;
     int kch = 0;            // z planes per tile of the batched passes (0 = the default)
     int blocks = 0;         // persistent grid of the batched passes
+    int own_launch_tiles_per_sm = 8;   // grids with at least this many tiles per SM launch alone (0: none)
     long long launches = 0;
     DevBuf<unsigned char> dgrid, dsrc, ddet;
     cudaEvent_t done = nullptr;   // recorded after a batched call; member streams wait on it
@@ -2514,6 +2515,9 @@ constexpr int BATCH_DEFAULT_KCH = 16;
 template <class R> struct BatchTables {
     const BatchGrid<R> *grids = nullptr;
     long long tiles = 0;
+    // grids large enough to fill the GPU on their own: they keep their own H / E launches (in the
+    // same graph) and add no tiles to the batched passes
+    std::vector<char> own;
     std::vector<const BatchSrc<R> *> src;
     std::vector<int> nsrc;
     std::vector<long long> src_pts;
@@ -2533,6 +2537,10 @@ BatchTables<R> batch_tables(omx_batch *b, const std::vector<RunPlan> *plans, int
     std::vector<BatchGrid<R>> grids(n);
     long long t0 = 0;
     size_t rounds = 0;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    T.own.assign(n, 0);
     for (int i = 0; i < n; ++i) {
         omx_ctx *c = b->ctx[i];
         std::memset(&grids[i], 0, sizeof(BatchGrid<R>));
@@ -2541,7 +2549,13 @@ BatchTables<R> batch_tables(omx_batch *b, const std::vector<RunPlan> *plans, int
         grids[i].tx = (c->L.nx + 31) / 32;
         grids[i].ty = (c->L.ny + 3) / 4;
         grids[i].tile0 = t0;
-        t0 += (long long)grids[i].tx * grids[i].ty * ((c->L.nz + kch - 1) / kch);
+        const long long tiles = (long long)grids[i].tx * grids[i].ty * ((c->L.nz + kch - 1) / kch);
+        // a grid of at least 8 tiles per SM fills the GPU by itself: its own launches beat the
+        // persistent pass's per-tile lookup (an empty tile range is skipped by the lookup)
+        if (b->own_launch_tiles_per_sm > 0 && tiles >= (long long)b->own_launch_tiles_per_sm * (sms > 0 ? sms : 152))
+            T.own[i] = 1;
+        else
+            t0 += tiles;
         rounds = std::max(rounds, c->sources.size());
     }
     T.tiles = t0;
@@ -2661,6 +2675,12 @@ template <class R> long long batch_step(omx_batch *b, const BatchTables<R> &T, c
     long long k = 0;
     launch_batch3<R>(0, T.grids, n, T.tiles, kch, b->blocks, b->stream);
     ++k;
+    for (int i = 0; i < n; ++i)
+        if (T.own[i]) {
+            omx_ctx *c = b->ctx[i];
+            launch_h<R>(field_ptrs<R>(c), grid_args<R>(c), b->stream);
+            ++k;
+        }
     for (size_t r = 0; r < T.src.size(); ++r) {
         if (T.nsrc[r] > 0) {
             launch_src_batch<R>(T.src[r], T.nsrc[r], T.src_pts[r], b->stream);
@@ -2679,6 +2699,14 @@ template <class R> long long batch_step(omx_batch *b, const BatchTables<R> &T, c
         }
     launch_batch3<R>(1, T.grids, n, T.tiles, kch, b->blocks, b->stream);
     ++k;
+    for (int i = 0; i < n; ++i)
+        if (T.own[i]) {
+            omx_ctx *c = b->ctx[i];
+            GridArgs<R> G = grid_args<R>(c);
+            G.ade_n = 0;   // the dispersive cells ran above with every grid's
+            launch_e<R>(field_ptrs<R>(c), G, b->stream);
+            ++k;
+        }
     for (int i = 0; i < n; ++i) {
         omx_ctx *c = b->ctx[i];
         const long long before = c->launches;

@@ -56,6 +56,34 @@ def test_batch_equals_solo_runs(precision, use_graph, autotune):
         g.kill()
 
 
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_batch_with_a_grid_that_launches_alone(precision):
+    """A grid of at least 8 tiles per SM (160^3 here) keeps its own H / E launches inside the
+    batched step while the small grids share the persistent passes; every grid still equals its
+    solo run bit for bit."""
+    sizes, steps = (160, 36, 29), 40
+    solo, batch = [], []
+    for k, n in enumerate(sizes):
+        d, g = build(n, 300 + k, precision)
+        g.set_step_form(omx.STEP_TWO_PASS)
+        g.run(1, steps, d["n_skip"], d["t_det_print"], use_graph=True)
+        solo.append((fields(g), g.drain_detectors()[1]))
+        g.kill()
+        batch.append(build(n, 300 + k, precision))
+    b = omx.Batch([g for _, g in batch])
+    d0 = batch[0][0]
+    b.run(1, steps, d0["n_skip"], d0["t_det_print"], use_graph=True)
+    for (d, g), (f_solo, tr_solo) in zip(batch, solo):
+        tr = g.drain_detectors()[1]
+        assert tr.shape == tr_solo.shape and np.array_equal(tr, tr_solo)
+        assert max(np.max(np.abs(f)) for f in f_solo) > 0     # the source has driven every grid
+        for a, s_ in zip(fields(g), f_solo):
+            assert np.array_equal(a, s_)
+    b.kill()
+    for _, g in batch:
+        g.kill()
+
+
 def test_batch_rejects_bad_members():
     d, g3 = build(32, 1, "fp32")
     _, g64 = build(32, 2, "fp64")
