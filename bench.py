@@ -425,6 +425,7 @@ def gpu_arm(args, dist):
     plain = None
     if not args.skip_plain:
         g64, groups64 = build_gpu(deck, "fp64")
+        g64.autotune(reps=5)
         g64.run(1, W, deck["n_skip"], tdp, use_graph=True)
         g64.synchronize()
         g64.timer_start()
