@@ -50,6 +50,8 @@ def parse():
     p.add_argument("--train-steps", type=int, default=300, help="cfg4: Adam steps of the closure training")
     p.add_argument("--trajectories", type=int, default=16384, help="cfg4: training trajectories (plain propagator)")
     p.add_argument("--cpu-seconds", type=float, default=12.0)
+    p.add_argument("--no-autotune", action="store_true",
+                   help="keep the library's default launch shape (a fixed kernel form, e.g. for a profiler)")
     p.add_argument("--grid", type=int, default=None,
                    help="cfg3: cube side instead of 512 (a smaller case of the same scene, e.g. for a profiler)")
     p.add_argument("--skip-plain", action="store_true")
@@ -330,7 +332,7 @@ def gpu_arm(args, dist):
     # ---- chosen path: FP32 fused, device loop in a CUDA graph; the launch shape from the
     # library's autotuner (omx_autotune, timed on the zero initial fields before the first step)
     gpu, groups = build_gpu(deck, "fp32")
-    shape = gpu.autotune(reps=5)
+    shape = gpu.autotune(reps=20) if not args.no_autotune else (44 if deck["dimensions"] == 2 else 16)
     gpu.run(1, W, deck["n_skip"], tdp, use_graph=True)
     gpu.synchronize()
     dist.barrier()
@@ -366,11 +368,12 @@ def gpu_arm(args, dist):
         per["fused_HE"] = per.pop("E")
         per.pop("H")
         dom, kernel_name = "fused_HE", ("k_fused3 (3D H+E step in one pass)" if deck["dimensions"] == 3 else
-                                        "k_fused_tmz_* (H+E step in one pass; form from OMX_FUSED_KERNEL, default ws4)")
+                                        "k_fused_tmz_ws (H+E step in one pass; form from omx_autotune)")
     alg_bytes = gpu.algorithmic_bytes(kc_dom)
     traffic, traffic_src = (None, None)
-    if dom == "fused_HE" and args.config == "cfg2" and os.environ.get("OMX_FUSED_KERNEL", "ws4") == "ws4":
-        traffic, traffic_src = recorded_traffic("k_fused_tmz_ws<0, 4, 1> tmz4096")
+    recorded = {14: "k_fused_tmz_ws<0, 4, 1, 4> tmz4096", 44: "k_fused_tmz_ws<0, 4, 1, 8> tmz4096"}
+    if dom == "fused_HE" and args.config == "cfg2" and shape in recorded:
+        traffic, traffic_src = recorded_traffic(recorded[shape])
     avg_s = per[dom]["ms_total"] / per[dom]["launches"] / 1e3
     peak, peak_kind = peaks()
     achieved = alg_bytes / avg_s / 1e9
@@ -384,7 +387,8 @@ def gpu_arm(args, dist):
 
     def e2e_run(one_step):
         g, grp = build_gpu(deck, "fp32")
-        g.autotune(reps=5)
+        if not args.no_autotune:
+            g.autotune(reps=20)
         pend = [None]
         for tt in range(1, W + 1):
             one_step(g, grp, tt, pend)
@@ -425,7 +429,8 @@ def gpu_arm(args, dist):
     plain = None
     if not args.skip_plain:
         g64, groups64 = build_gpu(deck, "fp64")
-        g64.autotune(reps=5)
+        if not args.no_autotune:
+            g64.autotune(reps=20)
         g64.run(1, W, deck["n_skip"], tdp, use_graph=True)
         g64.synchronize()
         g64.timer_start()
@@ -462,7 +467,8 @@ def gpu_arm(args, dist):
                        "l2": "working set %.0f MB > 126 MB L2, no flush" % (cells * 3 * 4 / 1e6),
                        "loop": "device-side loop captured in a CUDA graph, one graph launch per step",
                        "launch_shape": ("fused-kernel form %d" % shape if deck["dimensions"] == 2 else
-                                        "planes marched per thread %d" % shape) + " (omx_autotune)"},
+                                        "planes marched per thread %d" % shape) +
+                                       (" (library default)" if args.no_autotune else " (omx_autotune)")},
             "emitter_steps_per_s": emitter_rate,
             "roofline": {"bound": "hbm", "kernel": kernel_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "traffic_source": traffic_src,

@@ -1396,35 +1396,48 @@ template <class R> int autotune_impl(omx_ctx *c, int reps)
     const bool fused = std::is_same<R, float>::value && c->fused_ok;
     std::vector<int> cand;
     if (fused && c->dims == 3) cand = {8, 16, 32};
-    else if (fused) cand = {0, 4, 5, 6, 8, 14, 15, 16, 24, 25, 34, 36};
+    else if (fused) cand = {0, 4, 5, 6, 8, 14, 15, 16, 24, 25, 34, 36, 44, 45};
     else if (c->dims == 3) cand = {4, 8, 16, 32};
     else if (c->dims == 2) cand = {8, 16, 32, 64};
     else return 0;
-    float best = 0.f;
+    auto select = [&](int v) {
+        if (fused && c->dims == 2) c->fused_form = v;
+        else c->march = v;
+    };
+    auto once = [&]() {
+        if (fused) {
+            fused_step<R>(c);
+        } else {
+            do_H<R>(c);
+            do_E<R>(c, imm(0.0), imm(0.0));
+        }
+    };
+    // first use of every form sets its kernel attributes; then `reps` rounds, each timing one
+    // step of every candidate in turn (interleaved, so that clock or thermal drift affects all
+    // candidates alike); a candidate's time is its fastest round
+    for (int v : cand) {
+        select(v);
+        once();
+    }
+    std::vector<float> best(cand.size(), 1e30f);
+    for (int r = 0; r < reps; ++r)
+        for (size_t k = 0; k < cand.size(); ++k) {
+            select(cand[k]);
+            ck(cudaEventRecord(c->t0, c->stream), "autotune");
+            once();
+            ck(cudaEventRecord(c->t1, c->stream), "autotune");
+            ck(cudaEventSynchronize(c->t1), "autotune");
+            float ms = 0.f;
+            ck(cudaEventElapsedTime(&ms, c->t0, c->t1), "autotune");
+            best[k] = std::min(best[k], ms);
+        }
     int pick = cand[0];
-    for (size_t k = 0; k < cand.size(); ++k) {
-        if (fused && c->dims == 2) c->fused_form = cand[k];
-        else c->march = cand[k];
-        auto once = [&]() {
-            if (fused) {
-                fused_step<R>(c);
-            } else {
-                do_H<R>(c);
-                do_E<R>(c, imm(0.0), imm(0.0));
-            }
-        };
-        once();   // first use of a form sets its kernel attributes
-        ck(cudaEventRecord(c->t0, c->stream), "autotune");
-        for (int r = 0; r < reps; ++r) once();
-        ck(cudaEventRecord(c->t1, c->stream), "autotune");
-        ck(cudaEventSynchronize(c->t1), "autotune");
-        float ms = 0.f;
-        ck(cudaEventElapsedTime(&ms, c->t0, c->t1), "autotune");
-        if (k == 0 || ms < best) {
-            best = ms;
+    float bt = best[0];
+    for (size_t k = 1; k < cand.size(); ++k)
+        if (best[k] < bt) {
+            bt = best[k];
             pick = cand[k];
         }
-    }
     if (fused && c->dims == 2) c->fused_form = pick;
     else c->march = pick;
     ck(cudaPeekAtLastError(), "autotune");

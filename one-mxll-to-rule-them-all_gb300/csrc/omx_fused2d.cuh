@@ -416,7 +416,8 @@ template <int CH> struct FzStageT {
     float hx[FZ_W * CH];                      // columns ib0 .. ib0+W-1
 };
 using FzStage = FzStageT<1>;
-static_assert(sizeof(FzStageT<1>) % 16 == 0 && sizeof(FzStageT<2>) % 16 == 0 && (FZ_W + 8) % 4 == 0,
+static_assert(sizeof(FzStageT<1>) % 16 == 0 && sizeof(FzStageT<2>) % 16 == 0 && sizeof(FzStageT<4>) % 16 == 0 &&
+                  (FZ_W + 8) % 4 == 0,
               "bulk copies need 16-byte aligned stage arrays");
 constexpr long long FZ_WAIT_CYCLES = 2000000000LL;   // about one second at the SM clock
 
@@ -435,7 +436,7 @@ __device__ __forceinline__ FzSeg fz_segment(long long r, long long r1, long long
 // Issue the copies of item k of segment S into stage st; completes on bar (one arrival).
 template <int CH>
 __device__ __forceinline__ void fz_issue(const Fused2Args &A, const GridArgs<float> &G, const FzSeg &S, int k,
-                                         FzStageT<CH> *st, uint64_t *bar)
+                                         FzStageT<CH> *st, uint64_t *bar, uint64_t pol = 0)
 {
     constexpr int W = FZ_W * CH;
     const Lay &L = G.L;
@@ -453,6 +454,12 @@ __device__ __forceinline__ void fz_issue(const Fused2Args &A, const GridArgs<flo
     const long long e0 = L.off + (ib0 - 4) + (long long)L.px * row;   // 16-byte aligned
     const long long h0 = L.off + ib0 + (long long)L.px * row;         // 128-byte aligned
     mbar_arrive_expect_tx(bar, (ld_ez ? ezb : 0u) + (ld_hx ? hxb : 0u) + (ld_hy ? ezb : 0u));
+    if (pol) {
+        if (ld_ez) bulk_g2s_hint(st->ez, A.ez_in + e0, ezb, bar, pol);
+        if (ld_hx) bulk_g2s_hint(st->hx, A.hx_in + h0, hxb, bar, pol);
+        if (ld_hy) bulk_g2s_hint(st->hy, A.hy_in + e0, ezb, bar, pol);
+        return;
+    }
     if (ld_ez) bulk_g2s(st->ez, A.ez_in + e0, ezb, bar);
     if (ld_hx) bulk_g2s(st->hx, A.hx_in + h0, hxb, bar);
     if (ld_hy) bulk_g2s(st->hy, A.hy_in + e0, ezb, bar);
@@ -482,11 +489,12 @@ __global__ void __launch_bounds__(128, 6) k_fused_tmz_tma(Fused2Args A, GridArgs
     long long pr = rb0;
     int pk = 0;
     int issued = 0, released = 0;             // items: rows + 2 per segment (fits an int)
+    const uint64_t pol = tl == 0 ? l2_policy_evict_first() : 0;   // every row is read once per step
     auto issue_more = [&]() {
         while (pr < rb1 && issued < released + D) {
             const FzSeg S = fz_segment(pr, rb1, ny);
             const int slot = issued % D;
-            fz_issue(A, G, S, pk, &stage[slot], &bar[slot]);
+            fz_issue(A, G, S, pk, &stage[slot], &bar[slot], pol);
             ++issued;
             if (++pk == S.j1 - S.j0 + 3) {
                 pk = 0;
@@ -675,15 +683,20 @@ drain:
 // the copy warp refills a slot as soon as the last consumer has read it: no block-wide barrier
 // per row.  The copy warp follows the block's segments incrementally (no 64-bit division per
 // item), and the y coefficients of a row come from the packed row table (two float4 loads).
-constexpr int FZ_CONSUMERS = 4;
+// NW compute warps (4 or 8) and one copy warp per block; a strip chunk is 128 NW columns.
+template <int NW, int CH> constexpr int fz_min_blocks() { return NW == 8 ? 3 : (CH == 1 ? 5 : 4); }
 
-template <bool XCPML, int D, int CH>
-__global__ void __launch_bounds__(160, (CH == 1 ? 5 : 4)) k_fused_tmz_ws(Fused2Args A, GridArgs<float> G, int nstrip)
+template <bool XCPML, int D, int CH, int NW>
+__global__ void __launch_bounds__(32 * (NW + 1), (fz_min_blocks<NW, CH>())) k_fused_tmz_ws(Fused2Args A,
+                                                                                      GridArgs<float> G, int nstrip)
 {
-    constexpr int W = FZ_W * CH;               // strip width: each thread owns CH chunks of 4 cells
+    constexpr int FZ_CONSUMERS = NW;
+    constexpr int WC = 128 * NW;               // columns per chunk: NW warps x 32 lanes x 4 cells
+    constexpr int SW = WC * CH / FZ_W;         // the stage type's width in units of 512 columns
+    constexpr int W = WC * CH;                 // strip width: each thread owns CH chunks of 4 cells
     extern __shared__ __align__(128) unsigned char fz_smem[];
-    FzStageT<CH> *stage = reinterpret_cast<FzStageT<CH> *>(fz_smem);
-    uint64_t *full = reinterpret_cast<uint64_t *>(fz_smem + D * sizeof(FzStageT<CH>));
+    FzStageT<SW> *stage = reinterpret_cast<FzStageT<SW> *>(fz_smem);
+    uint64_t *full = reinterpret_cast<uint64_t *>(fz_smem + D * sizeof(FzStageT<SW>));
     uint64_t *empty = full + D;
     const Lay &L = G.L;
     const long long ny = L.ny;
@@ -709,6 +722,7 @@ __global__ void __launch_bounds__(160, (CH == 1 ? 5 : 4)) k_fused_tmz_ws(Fused2A
         long long r = rb0;
         int k = 0, q = 0;
         bool ok = true;
+        const uint64_t pol = l2_policy_evict_first();   // every row is read once per step
         for (;;) {
             const int slot = q % D;
             // item q reuses the slot of item q-D: wait until every consumer warp released it
@@ -716,7 +730,7 @@ __global__ void __launch_bounds__(160, (CH == 1 ? 5 : 4)) k_fused_tmz_ws(Fused2A
                 ok = false;
                 break;
             }
-            fz_issue<CH>(A, G, S, k, &stage[slot], &full[slot]);
+            fz_issue<SW>(A, G, S, k, &stage[slot], &full[slot], pol);
             ++q;
             if (++k == S.j1 - S.j0 + 3) {
                 k = 0;
@@ -754,7 +768,7 @@ __global__ void __launch_bounds__(160, (CH == 1 ? 5 : 4)) k_fused_tmz_ws(Fused2A
         int lhx[CH][4], lex[CH][4];
 #pragma unroll
         for (int c = 0; c < CH; ++c) {
-            const int ib = ib0 + FZ_W * c + 4 * tl;
+            const int ib = ib0 + WC * c + 4 * tl;
             active[c] = ib <= L.nx;
             ibc[c] = active[c] ? ib : 1;      // lanes past nx only join the shuffles
 #pragma unroll
@@ -803,7 +817,7 @@ __global__ void __launch_bounds__(160, (CH == 1 ? 5 : 4)) k_fused_tmz_ws(Fused2A
                 const int ly = __float_as_int(c1.z);
 #pragma unroll
                 for (int c = 0; c < CH; ++c) {
-                    const int so = FZ_W * c + 4 * tl;
+                    const int so = WC * c + 4 * tl;
                     const float4 e0 = *reinterpret_cast<const float4 *>(&stage[s0].ez[4 + so]);
                     const float4 e1 = *reinterpret_cast<const float4 *>(&stage[s1].ez[4 + so]);
                     const float4 h0 = *reinterpret_cast<const float4 *>(&stage[s0].hx[so]);
@@ -861,14 +875,14 @@ __global__ void __launch_bounds__(160, (CH == 1 ? 5 : 4)) k_fused_tmz_ws(Fused2A
                 if (lane == 0) atomicOr(A.err, 1);
                 return;
             }
-            const FzStageT<CH> &C = stage[sc];
+            const FzStageT<SW> &C = stage[sc];
             const float dhy = c0.x, dey = c0.y, bhy = c0.z, chy = c0.w, bey = c1.x, cey = c1.y;
             const int ly = __float_as_int(c1.z), lye = __float_as_int(c1.w);
             const long long pbx = (long long)G.L2 * (j - 1);
             float hx[CH][4], hy[CH][4], hy_l[CH], ez[CH][5];
 #pragma unroll
             for (int c = 0; c < CH; ++c) {
-                const int so = FZ_W * c + 4 * tl;
+                const int so = WC * c + 4 * tl;
                 const float4 ez_c = *reinterpret_cast<const float4 *>(&C.ez[4 + so]);
                 const float4 ez_n = *reinterpret_cast<const float4 *>(&stage[sn].ez[4 + so]);
                 const float4 hx_o = *reinterpret_cast<const float4 *>(&C.hx[so]);
@@ -917,8 +931,8 @@ __global__ void __launch_bounds__(160, (CH == 1 ? 5 : 4)) k_fused_tmz_ws(Fused2A
             for (int c = 0; c < CH; ++c) {
                 if (active[c]) {
                     const long long row = L.off + ibc[c] + px * j;
-                    *reinterpret_cast<float4 *>(A.hx_out + row) = make_float4(hx[c][0], hx[c][1], hx[c][2], hx[c][3]);
-                    *reinterpret_cast<float4 *>(A.hy_out + row) = make_float4(hy[c][0], hy[c][1], hy[c][2], hy[c][3]);
+                    __stcs(reinterpret_cast<float4 *>(A.hx_out + row), make_float4(hx[c][0], hx[c][1], hx[c][2], hx[c][3]));
+                    __stcs(reinterpret_cast<float4 *>(A.hy_out + row), make_float4(hy[c][0], hy[c][1], hy[c][2], hy[c][3]));
                     if (G.per[0] && ibc[c] + 3 == L.nx) A.hy_out[row + 3 - L.nx] = hy[c][3];   // Hy(0,j) = Hy(nx,j)
                     if (G.per[1] && j == L.ny)
                         *reinterpret_cast<float4 *>(A.hx_out + row - px * L.ny) =
@@ -953,7 +967,7 @@ __global__ void __launch_bounds__(160, (CH == 1 ? 5 : 4)) k_fused_tmz_ws(Fused2A
                         }
                         eo[q] = e;
                     }
-                    *reinterpret_cast<float4 *>(A.ez_out + row) = make_float4(eo[0], eo[1], eo[2], eo[3]);
+                    __stcs(reinterpret_cast<float4 *>(A.ez_out + row), make_float4(eo[0], eo[1], eo[2], eo[3]));
                 }
 #pragma unroll
                 for (int q = 0; q < 4; ++q) hxp[c][q] = hx[c][q];

@@ -39,7 +39,7 @@ static int default_fused_form()
 {
     static int form = -1;
     if (form < 0) {
-        form = 14;
+        form = 44;   // ws4w8: eight compute warps, 4-slot ring (measured fastest on 4096^2)
         if (const char *v = getenv("OMX_FUSED_KERNEL")) {
             if (!strcmp(v, "regs")) form = 0;
             else if (!strcmp(v, "tma4")) form = 4;
@@ -51,6 +51,8 @@ static int default_fused_form()
             else if (!strcmp(v, "ws6")) form = 16;
             else if (!strcmp(v, "ws4x2")) form = 24;
             else if (!strcmp(v, "ws5x2")) form = 25;
+            else if (!strcmp(v, "ws4w8")) form = 44;
+            else if (!strcmp(v, "ws5w8")) form = 45;
             else if (!strcmp(v, "rt4")) form = 34;
             else if (!strcmp(v, "rt6")) form = 36;
         }
@@ -75,20 +77,23 @@ template <bool X, int D> static void launch_tma(const Fused2Args &A, const GridA
     k_fused_tmz_tma<X, D><<<grid, 128, smem, s>>>(A, G, nstrip);
 }
 
-template <bool X, int D, int CH> static void launch_ws(const Fused2Args &A, const GridArgs<float> &G, cudaStream_t s)
+template <bool X, int D, int CH, int NW = 4>
+static void launch_ws(const Fused2Args &A, const GridArgs<float> &G, cudaStream_t s)
 {
-    const size_t smem = D * sizeof(FzStageT<CH>) + 2 * D * sizeof(uint64_t);
-    const int nstrip = (G.L.nx / 4 + 128 * CH - 1) / (128 * CH);
+    constexpr int SW = NW * CH / 4;   // stage width in units of 512 columns
+    const size_t smem = D * sizeof(FzStageT<SW>) + 2 * D * sizeof(uint64_t);
+    const int cols = 32 * NW * CH;    // float4 groups per strip
+    const int nstrip = (G.L.nx / 4 + cols - 1) / cols;
     static int nb[FZ_MAX_DEV] = {};
     int dev = 0;
     cudaGetDevice(&dev);
     int &n = nb[dev < FZ_MAX_DEV ? dev : 0];
     if (n == 0) {
-        cudaFuncSetAttribute(k_fused_tmz_ws<X, D, CH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        n = persistent_blocks((const void *)k_fused_tmz_ws<X, D, CH>, smem, 32 * (FZ_CONSUMERS + 1));
+        cudaFuncSetAttribute(k_fused_tmz_ws<X, D, CH, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        n = persistent_blocks((const void *)k_fused_tmz_ws<X, D, CH, NW>, smem, 32 * (NW + 1));
     }
     const int grid = (int)std::min<long long>(n, (long long)nstrip * G.L.ny);
-    k_fused_tmz_ws<X, D, CH><<<grid, 32 * (FZ_CONSUMERS + 1), smem, s>>>(A, G, nstrip);
+    k_fused_tmz_ws<X, D, CH, NW><<<grid, 32 * (NW + 1), smem, s>>>(A, G, nstrip);
 }
 
 template <bool X, int R> static void launch_rt(const Fused2Args &A, const GridArgs<float> &G, int nstrip, cudaStream_t s)
@@ -120,10 +125,13 @@ static void launch_form(const Fused2Args &A, const GridArgs<float> &G, int form,
     case 5: launch_tma<X, 5>(A, G, nstrip, s); break;
     case 15: launch_ws<X, 5, 1>(A, G, s); break;
     case 24: launch_ws<X, 4, 2>(A, G, s); break;
+    case 44: launch_ws<X, 4, 1, 8>(A, G, s); break;
+    case 45: launch_ws<X, 5, 1, 8>(A, G, s); break;
     case 34: launch_rt<X, 4>(A, G, nstrip, s); break;
     case 36: launch_rt<X, 6>(A, G, nstrip, s); break;
     case 25: launch_ws<X, 5, 2>(A, G, s); break;
-    default: launch_ws<X, 4, 1>(A, G, s); break;
+    case 14: launch_ws<X, 4, 1>(A, G, s); break;
+    default: launch_ws<X, 4, 1, 8>(A, G, s); break;
     }
 }
 

@@ -236,7 +236,7 @@ def test_fp32_fused_tmz_variants(orc_mod, shape, bx, by, src, steps):
     assert trace_error(tg2, tc) <= FP32_TOL
 
 
-FORMS = ("regs", "tma4", "tma5", "tma6", "tma8", "ws4", "ws5", "ws6", "ws4x2", "ws5x2", "rt4", "rt6")
+FORMS = ("regs", "tma4", "tma5", "tma6", "tma8", "ws4", "ws5", "ws6", "ws4x2", "ws5x2", "ws4w8", "ws5w8", "rt4", "rt6")
 
 
 @pytest.mark.parametrize("shape,bx,by,src,steps", [
