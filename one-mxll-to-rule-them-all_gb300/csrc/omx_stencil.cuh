@@ -154,9 +154,10 @@ __device__ __forceinline__ void h3_tile(const FieldPtrs<R> &F, const GridArgs<R>
         const R ey_kp = Ey[idx + sz], ey_ip = Ey[idx + sx];
         const R ex_kp = Ex[idx + sz], ex_jp = Ex[idx + sy];
         const R dhz = G.den_h[2][k];
-        R hx = Hx[idx] + dt_mu0 * ((ez_c - ez_jp) * dhy + (ey_kp - ey_c) * dhz);
-        R hy = Hy[idx] + dt_mu0 * ((ez_ip - ez_c) * dhx + (ex_c - ex_kp) * dhz);
-        R hz = Hz[idx] + dt_mu0 * ((ey_c - ey_ip) * dhx + (ex_jp - ex_c) * dhy);
+        // the old H of this cell is read by this thread only: streaming loads and stores
+        R hx = __ldcs(Hx + idx) + dt_mu0 * ((ez_c - ez_jp) * dhy + (ey_kp - ey_c) * dhz);
+        R hy = __ldcs(Hy + idx) + dt_mu0 * ((ez_ip - ez_c) * dhx + (ex_c - ex_kp) * dhz);
+        R hz = __ldcs(Hz + idx) + dt_mu0 * ((ey_c - ey_ip) * dhx + (ex_jp - ex_c) * dhy);
         if (lx >= 0) {  // mxll_3D_mod.f90:585-620
             const long long p = lx + (long long)G.L2 * ((j - 1) + (long long)L.ny * (k - 1));
             const R b = G.bH[0][i], c = G.cH[0][i];
@@ -188,9 +189,9 @@ __device__ __forceinline__ void h3_tile(const FieldPtrs<R> &F, const GridArgs<R>
             hx = hx + dt_mu0 * v0;
             hy = hy + dt_mu0 * v1;
         }
-        Hx[idx] = hx;
-        Hy[idx] = hy;
-        Hz[idx] = hz;
+        __stcs(Hx + idx, hx);
+        __stcs(Hy + idx, hy);
+        __stcs(Hz + idx, hz);
         // periodic ghost planes H(0) = H(n) (mxll_3D_mod.f90:725-738); the wraps run one after the
         // other over whole planes, so a corner ghost ends up equal to H(n, n, .) as well
         const bool gx = G.per[0] && i == L.nx, gy = G.per[1] && j == L.ny, gz = G.per[2] && k == L.nz;
@@ -254,7 +255,7 @@ __device__ __forceinline__ void e3_tile(const FieldPtrs<R> &F, const GridArgs<R>
         const R rx = (hz_c - hz_jm) * dey + (hy_km - hy_c) * dez;
         const R ry = (hz_im - hz_c) * dex + (hx_c - hx_km) * dez;
         const R rz = (hy_c - hy_im) * dex + (hx_jm - hx_c) * dey;
-        R ex = Ex[idx], ey = Ey[idx], ez = Ez[idx];
+        R ex = __ldcs(Ex + idx), ey = __ldcs(Ey + idx), ez = __ldcs(Ez + idx);   // read by this thread only
         if (bb_ij && k >= G.bb0[2] && k <= G.bb1[2]) {
             const long long b = (i - G.bb0[0]) + (long long)G.bbd[0] * ((j - G.bb0[1]) + (long long)G.bbd[1] * (k - G.bb0[2]));
             ex = plain_update<R>(ex, rx, G.mat[0][b], G);
@@ -296,9 +297,9 @@ __device__ __forceinline__ void e3_tile(const FieldPtrs<R> &F, const GridArgs<R>
             ex = ex + dt_eps0 * v0;
             ey = ey + dt_eps0 * v1;
         }
-        Ex[idx] = ex;
-        Ey[idx] = ey;
-        Ez[idx] = ez;
+        __stcs(Ex + idx, ex);
+        __stcs(Ey + idx, ey);
+        __stcs(Ez + idx, ez);
         hx_km = hx_c;
         hy_km = hy_c;
     }
