@@ -214,7 +214,7 @@ __device__ __forceinline__ void h3_tile(const FieldPtrs<R> &F, const GridArgs<R>
 }
 
 // FP32: at most 48 registers, 10 blocks per SM (measured 8 % faster than the unbounded 64
-// registers at 512^3; the E pass measured slower under the same bound and keeps its own)
+// registers at 512^3; the E pass takes its own bound, 9 blocks)
 template <class R, bool EXACT>
 __global__ void __launch_bounds__(128, (sizeof(R) == 4 ? 10 : 1)) k_h3(FieldPtrs<R> F, GridArgs<R> G, int kch)
 {
@@ -305,8 +305,10 @@ __device__ __forceinline__ void e3_tile(const FieldPtrs<R> &F, const GridArgs<R>
     }
 }
 
+// FP32: at most 56 registers, 9 blocks per SM (4 % faster than the unbounded 64 registers at
+// 512^3 and 256^3)
 template <class R, bool EXACT>
-__global__ void __launch_bounds__(128) k_e3(FieldPtrs<R> F, GridArgs<R> G, int kch)
+__global__ void __launch_bounds__(128, (sizeof(R) == 4 ? 9 : 1)) k_e3(FieldPtrs<R> F, GridArgs<R> G, int kch)
 {
     e3_tile<R, EXACT>(F, G, kch, blockIdx.x, blockIdx.y, blockIdx.z);
 }
