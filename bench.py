@@ -153,6 +153,10 @@ def make_deck(cfg, grid=None):
     if cfg == "cfg1":
         return decks.deck_cfg1(), "cfg1: 3D 128^3 dr 2 nm, 10-cell CPML, Drude-Lorentz Au sphere r 20 nm, " \
                                   "x-polarised 2.2 eV plane-wave soft source, 16 point detectors"
+    if cfg == "cfg4":
+        return decks.deck_cfg3(n=384, n_emitters=1_000_000), \
+            "cfg4: 3D 384^3 dr 1 nm, 10-cell CPML, 4x4 Au nanorod dimers, 1e6 three-level emitters (plain " \
+            "density-matrix propagator), chirped 1.8-2.6 eV drive"
     if cfg == "cfg3":
         n = grid or 512
         ne = 100000 if n == 512 else max(1000, int(100000 * (n / 512) ** 3))
@@ -289,8 +293,52 @@ def cpu_run(deck, seconds, max_steps=None):
     return n, el, orc.lib().orc_num_threads()
 
 
+def reference_arm_fdop(args):
+    """The FP64 C oracle applying the 160^3 frequency-domain operator (same operator and input as
+    the GPU arm), a bounded number of applications per timed step."""
+    import numpy as np
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import build_oracle
+
+    build_oracle.build()
+    import oracle as orc
+
+    rng = np.random.default_rng(CFG5_SEED + 7)
+    n, n_der = (160, 160, 160), 2
+    eps = 1.0 + 11.1 * (rng.random(n) < 0.4) + 0.0j
+    O = orc.FDOperator(n, 8, n_der, (3, 3, 3), 0.05, 2.0 * np.pi / 1.55, eps)
+    f = O.zeros()
+    g = n_der
+    f[:, g:-g, g:-g, g:-g] = 1.0 + 0.5j
+    O.apply(f)                          # warm-up application outside the clock
+    budget = min(2.0 * args.steps, 150.0)
+    k, t0 = 0, time.perf_counter()
+    while True:
+        O.apply(f)
+        k += 1
+        el = time.perf_counter() - t0
+        if (el >= budget and k >= 2) or k >= args.steps:
+            break
+    cells = n[0] * n[1] * n[2]
+    v = cells * k / el / 1e9
+    line = {"impl": "reference", "metric": "frequency-domain operator applications, Gcell/s (and BiCGStab(2) "
+            "solve time)", "value": v, "unit": "Gcell-applications/s", "n_gpus": 0, "steps": k, "warmup": 1,
+            "ms_per_step": el / k * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "c128", "data": "synthetic (seeded binary permittivity map)",
+            "config": {"workload": "apply_operator_3D on 160^3, n_der 2 (4th order), 8-cell PML, eps 1 / 12.1 "
+                                   "(fill 0.4)", "cells": cells},
+            "cpu_baseline": {"value": v, "unit": "Gcell-applications/s", "cores": 1, "kind": "port",
+                             "sample": f"{k} applications of the C oracle (single-threaded loops)"},
+            "e2e": {"value": v, "unit": "Gcell-applications/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
 def reference_arm(args, dist):
     if dist.rank != 0:
+        return
+    if args.config == "fdop":
+        reference_arm_fdop(args)
         return
     if args.config == "cfg5":
         # the sweep's grids are independent: the sample is its smallest grid
