@@ -167,6 +167,7 @@ struct omx_ctx {
     DevBuf<long long> inj_e;
     DevBuf<int> inj_c, inj_a, inj_b;
     int inj_n = 0;
+    std::vector<int4> inj_host;    // (i, j, k, component) of every emitter-current point
     bool j_dirty = false;
     // detectors
     struct Det {
@@ -264,6 +265,7 @@ struct omx_ctx {
     int cur = 0;
     bool fused_ok = false;
     bool fused_dirty = true;    // media or sources changed since the last eligibility check
+    bool post_ok = false;       // the work after the fused pass goes in one launch (post_eligible)
     int step_form = OMX_STEP_DEFAULT;   // omx_set_step_form; a batch sets TWO_PASS on its members
     int *run_step = nullptr;    // device step counter while omx_run issues a step sequence
     std::string err;
@@ -701,7 +703,7 @@ void rebuild_injection(omx_ctx *c)
 {
     const int np = (int)c->jkeys.size();
     const int avg = (c->dims == 3 || (c->dims == 2 && c->desc.mode == OMX_TEZ_2D_MODE)) ? 1 : 0;
-    struct Ent { long long e; int comp, a, b; };
+    struct Ent { long long e; int comp, a, b; int4 cell; };
     std::map<std::pair<int, long long>, Ent> ents;
     const int nxx = c->n[0] + 2, nyy = c->n[1] + 2;
     for (int p = 0; p < np; ++p) {
@@ -739,6 +741,7 @@ void rebuild_injection(omx_ctx *c)
                 Ent en;
                 en.e = eindex(c, ci, cj, cz);
                 en.comp = q;
+                en.cell = make_int4(ci, cj, cz, q);
                 auto fa = c->jslot.find(ck_);
                 en.a = fa == c->jslot.end() ? -1 : fa->second;
                 en.b = -1;
@@ -754,7 +757,9 @@ void rebuild_injection(omx_ctx *c)
     }
     std::vector<long long> e;
     std::vector<int> comp, a, b;
+    c->inj_host.clear();
     for (auto &kv : ents) {
+        c->inj_host.push_back(kv.second.cell);
         e.push_back(kv.second.e);
         comp.push_back(kv.second.comp);
         a.push_back(kv.second.a);
@@ -903,8 +908,27 @@ bool fused_eligible(const omx_ctx *c)
     return true;
 }
 
+// The dispersive cells, the sources and the emitter current after a fused pass can share one
+// launch when they write disjoint E words: at most one source, a plane (the plane holds no
+// dispersive cell on the fused path, and the emitter current skips dispersive cells), and no
+// emitter-current point on the plane.
+bool post_eligible(const omx_ctx *c)
+{
+    if (!c->fused_ok || c->sources.size() > 1) return false;
+    if (c->sources.empty()) return true;
+    const SourceRec &S = *c->sources[0];
+    if (S.kind != 1) return false;
+    const int ax = S.pd.plane_axis - 1, comp = S.pd.comp - 1;
+    for (const int4 &p : c->inj_host) {
+        const int at = ax == 0 ? p.x : (ax == 1 ? p.y : p.z);
+        if (p.w == comp && at == S.pd.plane_index) return false;
+    }
+    return true;
+}
+
 void prepare(omx_ctx *c)
 {
+    const bool recheck = c->j_dirty || c->fused_dirty;
     if (c->j_dirty || c->det_dirty || c->fused_dirty) c->epoch++;
     if (c->j_dirty) rebuild_jpoints(c);
     if (c->det_dirty) rebuild_detectors(c);
@@ -913,6 +937,7 @@ void prepare(omx_ctx *c)
         c->fused_ok = fused_eligible(c);
         c->fused_dirty = false;
     }
+    if (recheck) c->post_ok = post_eligible(c);
     if (c->fused_ok && !c->ff2[2].p) {
         for (int q = 0; q < 6; ++q)
             if (c->field_used[q]) c->ff2[q].alloc(c->felems);
@@ -1054,9 +1079,9 @@ template <class R> void do_sample(omx_ctx *c, StepParam slot, StepParam time)
 
 // One FP32 fused TMz step: bulk H+E pass from the current buffer set into the other, then the
 // dispersive cells; the caller adds sources and the emitter current to the new set.
-template <class R> void fused_step(omx_ctx *c);
-template <> void fused_step<double>(omx_ctx *) {}
-template <> void fused_step<float>(omx_ctx *c)
+template <class R> void fused_step(omx_ctx *c, bool ade = true);
+template <> void fused_step<double>(omx_ctx *, bool) {}
+template <> void fused_step<float>(omx_ctx *c, bool ade)
 {
     ProfScope ps(c, KC_E);
     const int in = c->cur, out = 1 - c->cur;
@@ -1069,8 +1094,8 @@ template <> void fused_step<float>(omx_ctx *c)
         for (int a = 0; a < 3; ++a)
             for (int q = 0; q < 2; ++q) A.psiH_out[a][q] = in == 0 ? c->psiH2[a][q].p : c->psif[a][1][q].p;
         launch_fused3(A, G, c->march, c->stream);
-        launch_ade_post(Fin, Fout, G, c->stream);
-        c->launches += 1 + (c->ade_n > 0 ? 1 : 0);
+        if (ade) launch_ade_post(Fin, Fout, G, c->stream);
+        c->launches += 1 + (ade && c->ade_n > 0 ? 1 : 0);
         c->cur = out;
         return;
     }
@@ -1090,9 +1115,50 @@ template <> void fused_step<float>(omx_ctx *c)
     A.err = c->d_err.p;
     A.rowc = reinterpret_cast<const float4 *>(c->rowc.p);
     launch_fused_tmz(A, G, c->fused_form, c->stream);
-    launch_ade_post(Fin, Fout, G, c->stream);
-    c->launches += 1 + (c->ade_n > 0 ? 1 : 0);
+    if (ade) launch_ade_post(Fin, Fout, G, c->stream);
+    c->launches += 1 + (ade && c->ade_n > 0 ? 1 : 0);
     c->cur = out;
+}
+
+// After fused_step(c, false): the dispersive cells, the source (a plane, or none) and the
+// emitter current in one launch (post_eligible holds).
+template <class R> void do_post(omx_ctx *c, StepParam amp, StepParam time, StepParam t_skip);
+template <> void do_post<double>(omx_ctx *, StepParam, StepParam, StepParam) {}
+template <> void do_post<float>(omx_ctx *c, StepParam amp, StepParam time, StepParam t_skip)
+{
+    ProfScope ps(c, KC_SRC);
+    const FieldPtrs<float> Fin = field_ptrs<float>(c, 1 - c->cur), Fout = field_ptrs<float>(c, c->cur);
+    const GridArgs<float> G = grid_args<float>(c);
+    PostArgs Q{};
+    Q.nb_ade = (c->ade_n + 127) / 128;
+    if (!c->sources.empty()) {
+        const SourceRec &S = *c->sources[0];
+        Q.P.comp = S.pd.comp - 1;
+        Q.P.axis = S.pd.plane_axis - 1;
+        Q.P.index = S.pd.plane_index;
+        Q.P.c_src = S.c_src;
+        const int ax0 = Q.P.axis == 0 ? 1 : 0, ax1 = c->dims == 2 ? -1 : (Q.P.axis == 2 ? 1 : 2);
+        Q.plane_n0 = c->n[ax0];
+        Q.plane_cells = c->n[ax0] * (ax1 >= 0 ? c->n[ax1] : 1);
+        Q.nb_plane = (Q.plane_cells + 127) / 128;
+        Q.amp = amp;
+    }
+    if (c->inj_n > 0) {
+        Q.I.n = c->inj_n;
+        Q.I.eidx = c->inj_e.p;
+        Q.I.comp = c->inj_c.p;
+        Q.I.sa = c->inj_a.p;
+        Q.I.sb = c->inj_b.p;
+        Q.I.avg = (c->dims == 3 || (c->dims == 2 && c->desc.mode == OMX_TEZ_2D_MODE)) ? 1 : 0;
+        Q.nb_inj = (c->inj_n + 127) / 128;
+        Q.J = jstate(c);
+        Q.time = time;
+        Q.tskip = t_skip;
+        Q.dt_eps0 = c->desc.dt / omx::consts().eps0;
+    }
+    if (Q.nb_ade + Q.nb_plane + Q.nb_inj == 0) return;
+    launch_post_fused(Fin, Fout, G, Q, c->stream);
+    c->launches++;
 }
 
 // Order the main stream after the side-stream work a one-step omx_run left running.
@@ -1268,12 +1334,17 @@ template <class R> void run_impl(omx_ctx *c, int tt0, int nsteps, int n_skip, in
     // values as the graph schedule.
     if (fused && nsteps == 1 && use_graph && !c->prof && (has_det || !c->groups.empty())) {
         const double *row = plan.stage->p;    // this step's table row, on the host
-        fused_step<R>(c);
+        const bool post = c->post_ok;
+        fused_step<R>(c, !post);
         join_side(c);
         std::vector<StepParam> amps;
         for (int q = 0; q < nsrc; ++q) amps.push_back(imm(row[4 + q]));
-        do_sources<R>(c, amps);
-        do_inject<R>(c, imm(row[0]), imm(row[1]));
+        if (post) {
+            do_post<R>(c, nsrc ? amps[0] : imm(0.0), imm(row[0]), imm(row[1]));
+        } else {
+            do_sources<R>(c, amps);
+            do_inject<R>(c, imm(row[0]), imm(row[1]));
+        }
         ck(cudaEventRecord(c->ev_fork, c->stream), "fork");
         ck(cudaStreamWaitEvent(c->side, c->ev_fork, 0), "fork");
         std::swap(c->stream, c->side);
@@ -1294,8 +1365,12 @@ template <class R> void run_impl(omx_ctx *c, int tt0, int nsteps, int n_skip, in
         for (auto &g : c->groups) do_group<R>(c, *g, P(2));
         if (has_det) do_sample<R>(c, P(3), P(0));
     };
+    const bool post = fused && c->post_ok;
     auto one_step = [&]() {
-        if (fused) {
+        if (post) {
+            fused_step<R>(c, false);
+            do_post<R>(c, nsrc ? amps[0] : imm(0.0), P(0), P(1));
+        } else if (fused) {
             fused_step<R>(c);
             do_sources<R>(c, amps);
             do_inject<R>(c, P(0), P(1));
@@ -1313,10 +1388,16 @@ template <class R> void run_impl(omx_ctx *c, int tt0, int nsteps, int n_skip, in
     // the wait on the scatter also orders it before the pass that overwrites its buffer set.
     // Same operations on the same values as one_step: results are identical.
     auto overlapped_step = [&](bool wait_prev) {
-        fused_step<R>(c);
-        do_sources<R>(c, amps);
-        if (wait_prev) ck(cudaStreamWaitEvent(c->stream, c->ev_join, 0), "wait");
-        do_inject<R>(c, P(0), P(1));
+        if (post) {
+            fused_step<R>(c, false);
+            if (wait_prev) ck(cudaStreamWaitEvent(c->stream, c->ev_join, 0), "wait");
+            do_post<R>(c, nsrc ? amps[0] : imm(0.0), P(0), P(1));
+        } else {
+            fused_step<R>(c);
+            do_sources<R>(c, amps);
+            if (wait_prev) ck(cudaStreamWaitEvent(c->stream, c->ev_join, 0), "wait");
+            do_inject<R>(c, P(0), P(1));
+        }
         ck(cudaEventRecord(c->ev_fork, c->stream), "fork");
         ck(cudaStreamWaitEvent(c->side, c->ev_fork, 0), "fork");
         std::swap(c->stream, c->side);

@@ -17,6 +17,7 @@
 // rounding.  The host enables this path only when no dispersive cell lies in a CPML slab and no
 // source point lies in a dispersive cell.
 #pragma once
+#include "omx_post.cuh"
 #include "omx_stencil.cuh"
 #include "omx_tma.cuh"
 
@@ -980,10 +981,9 @@ __global__ void __launch_bounds__(32 * (NW + 1), (fz_min_blocks<NW, CH>())) k_fu
 
 // Dispersive cells after the fused pass: E_out = ADE(E_in, curl H_out) (no CPML term: the host
 // keeps dispersive cells out of the CPML slabs on this path).
-__global__ void k_ade_post(FieldPtrs<float> Fin, FieldPtrs<float> Fout, GridArgs<float> G)
+__device__ __forceinline__ void ade_post_cell(const FieldPtrs<float> &Fin, const FieldPtrs<float> &Fout,
+                                              const GridArgs<float> &G, int q)
 {
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= G.ade_n) return;
     const int4 en = G.ade_ent[q];
     const int b = G.ade_b[q];
     const int c = en.w;
@@ -992,6 +992,37 @@ __global__ void k_ade_post(FieldPtrs<float> Fin, FieldPtrs<float> Fout, GridArgs
     const long long idx = L.off + en.x + (long long)L.px * en.y + L.pz * en.z;
     const ClsR<float> cl = G.cls[G.mat[c][b]];
     Fout.f[c][idx] = ade_update<float>(Fin.f[c][idx], rot, cl, c, b, G);
+}
+__global__ void k_ade_post(FieldPtrs<float> Fin, FieldPtrs<float> Fout, GridArgs<float> G)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < G.ade_n) ade_post_cell(Fin, Fout, G, q);
+}
+
+// Dispersive cells, the plane source and the emitter current after the fused pass in one launch:
+// the first nb_ade blocks take the dispersive cells, the next nb_plane the plane's cells, the
+// rest the emitter-current points.  The lists write disjoint E words (the host checks), and each
+// word gets the operation of its separate kernel, so the result is the same.
+__global__ void __launch_bounds__(128) k_post_fused(FieldPtrs<float> Fin, FieldPtrs<float> Fout, GridArgs<float> G,
+                                                    PostArgs Q)
+{
+    int b = blockIdx.x;
+    const int t = threadIdx.x;
+    if (b < Q.nb_ade) {
+        const int q = b * 128 + t;
+        if (q < G.ade_n) ade_post_cell(Fin, Fout, G, q);
+        return;
+    }
+    b -= Q.nb_ade;
+    if (b < Q.nb_plane) {
+        const double amp = sp_get(Q.amp);
+        const int q = b * 128 + t;
+        if (amp != 0.0 && q < Q.plane_cells) plane_point<float>(Fout, G.L, Q.P, amp, q % Q.plane_n0, q / Q.plane_n0);
+        return;
+    }
+    b -= Q.nb_plane;
+    const int q = b * 128 + t;
+    if (q < Q.I.n) inject_point<float>(Fout, Q.J, Q.I, sp_get(Q.time) - sp_get(Q.tskip), Q.dt_eps0, q);
 }
 
 }  // namespace omx

@@ -183,6 +183,21 @@ struct Fused3Args {
 // kch: planes marched per thread (0 = default)
 void launch_fused3(const Fused3Args &A, const GridArgs<float> &G, int kch, void *stream);
 void launch_ade_post(const FieldPtrs<float> &Fin, const FieldPtrs<float> &Fout, const GridArgs<float> &G, void *stream);
+// The work after a fused pass in one launch: the dispersive cells (as launch_ade_post), one
+// plane source (as launch_plane) and the emitter current (as launch_inject).  Only for lists
+// that write disjoint E words (the host checks), so the result equals the separate launches.
+struct PostArgs {
+    int nb_ade, nb_plane, nb_inj;   // blocks of 128 threads per list
+    int plane_n0, plane_cells;      // plane cells along the first in-plane axis, in all
+    PlaneArgs P;
+    StepParam amp;
+    InjArgs I;
+    JState J;
+    StepParam time, tskip;
+    double dt_eps0;
+};
+void launch_post_fused(const FieldPtrs<float> &Fin, const FieldPtrs<float> &Fout, const GridArgs<float> &G,
+                       const PostArgs &Q, void *stream);
 void launch_flush(float *buf, long long n, void *stream);
 // FP64 electromagnetic energy of the interior: 0.5 * dV * sum(eps0 E^2 + mu0 H^2) over the fields
 // present (vacuum constants; each component over its own interior index range)

@@ -167,4 +167,12 @@ void launch_ade_post(const FieldPtrs<float> &Fin, const FieldPtrs<float> &Fout, 
     k_ade_post<<<(G.ade_n + 127) / 128, 128, 0, (cudaStream_t)s>>>(Fin, Fout, G);
 }
 
+void launch_post_fused(const FieldPtrs<float> &Fin, const FieldPtrs<float> &Fout, const GridArgs<float> &G,
+                       const PostArgs &Q, void *s)
+{
+    const int nb = Q.nb_ade + Q.nb_plane + Q.nb_inj;
+    if (nb <= 0) return;
+    k_post_fused<<<nb, 128, 0, (cudaStream_t)s>>>(Fin, Fout, G, Q);
+}
+
 }  // namespace omx

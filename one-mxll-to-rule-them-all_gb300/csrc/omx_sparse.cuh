@@ -5,13 +5,9 @@
 #pragma once
 #include "omx_internal.h"
 #include "omx_emitter.cuh"
+#include "omx_post.cuh"
 
 namespace omx {
-
-__device__ __forceinline__ double sp_get(const StepParam &p)
-{
-    return p.tab ? p.tab[(long long)(*p.step) * p.stride] : p.val;
-}
 
 // ---- source_interactions (interactions_mod.f90:21-163) ----------------------------------------
 // J_mat = amp*ker (amp = j_amp*envelope*cos, computed on the host with the reference's libm
@@ -45,23 +41,7 @@ __global__ void k_plane(FieldPtrs<R> F, Lay L, PlaneArgs P, StepParam amp_p)
 {
     const double amp = sp_get(amp_p);
     if (amp == 0.0) return;
-    const int a = blockIdx.x * blockDim.x + threadIdx.x;
-    const int b = blockIdx.y;
-    int n[3] = {L.nx, L.ny, L.nz};
-    int ax0 = (P.axis == 0) ? 1 : 0;
-    int ax1 = (P.axis == 2) ? 1 : 2;
-    if (L.dims == 2) ax1 = -1;
-    if (a >= n[ax0]) return;
-    int c[3] = {0, 0, 0};
-    c[P.axis] = P.index;
-    c[ax0] = a + 1;
-    if (ax1 >= 0) {
-        if (b >= n[ax1]) return;
-        c[ax1] = b + 1;
-    }
-    R *E = F.f[P.comp];
-    const long long e = L.off + c[0] + (long long)L.px * c[1] + L.pz * c[2];
-    E[e] = (R)((double)E[e] + P.c_src * amp);
+    plane_point<R>(F, L, P, amp, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y);
 }
 
 // ---- emitter current in the E update (mxll_3D_mod.f90:756-761 and 2D/1D analogues) --------
@@ -73,20 +53,7 @@ __global__ void k_inject(FieldPtrs<R> F, JState J, InjArgs I, StepParam time_p, 
 {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= I.n) return;
-    const double tt = sp_get(time_p) - sp_get(tskip_p);
-    const int c = I.comp[q];
-    const int a = I.sa[q], b = I.sb[q];
-    const double ao = (a >= 0) ? J.Jo[c][a] : 0.0, ad = (a >= 0) ? J.dJ[c][a] : 0.0;
-    double jav;
-    if (I.avg) {
-        const double bo = (b >= 0) ? J.Jo[c][b] : 0.0, bd = (b >= 0) ? J.dJ[c][b] : 0.0;
-        jav = 0.5 * (ao + tt * ad + bo + tt * bd);
-    } else {
-        jav = ao + tt * ad;
-    }
-    R *E = F.f[c];
-    const long long e = I.eidx[q];
-    E[e] = (R)((double)E[e] - dt_eps0 * jav);
+    inject_point<R>(F, J, I, sp_get(time_p) - sp_get(tskip_p), dt_eps0, q);
 }
 
 // send_E_to_J_ranks (interactions_mod.f90:656-691, 2D :486-526, 1D :329-346) fused with
