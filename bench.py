@@ -430,34 +430,36 @@ def gpu_arm(args, dist):
     # ---- end to end through the C-ABI: one omx_run call per step (the step's time / source
     # table goes host->device from pinned memory inside the call) and an asynchronous drain of
     # that step's detector samples (device->host into a pinned slot), collected into host arrays
-    # one step later; the last step's samples are collected before the clock stops -------------
+    # two steps later (the drain ring holds four tickets); the last steps' samples are collected
+    # before the clock stops ----------------------------------------------------------------------
     npts = sum(len(d["idx"]) for d in deck["detectors"])
+    LAG = 2
 
     def e2e_run(one_step):
         g, grp = build_gpu(deck, "fp32")
         if not args.no_autotune:
             g.autotune(reps=20)
-        pend = [None]
+        pend = []
         for tt in range(1, W + 1):
             one_step(g, grp, tt, pend)
-        g.collect(pend[0])
-        pend[0] = None
+        while pend:
+            g.collect(pend.pop(0))
         g.synchronize()
         dist.barrier()
         t0 = time.perf_counter()
         for tt in range(W + 1, W + K + 1):
             one_step(g, grp, tt, pend)
-        g.collect(pend[0])
+        while pend:
+            g.collect(pend.pop(0))
         g.synchronize()
         el = dist.max(time.perf_counter() - t0)
         g.kill()
         return dist.world * cells * K / el / 1e9
 
     def drain_step(g, pend):
-        t = g.drain_async()
-        if pend[0] is not None:
-            g.collect(pend[0])
-        pend[0] = t
+        pend.append(g.drain_async())
+        if len(pend) > LAG:
+            g.collect(pend.pop(0))
 
     def run_step(g, grp, tt, pend):
         g.run(tt, 1, deck["n_skip"], tdp, use_graph=True)
@@ -530,7 +532,7 @@ def gpu_arm(args, dist):
                     "how": "one omx_run call per step (time/source table host->device from pinned memory; the "
                            "step's side-stream work overlaps the next call's fused pass) + "
                            "omx_detectors_drain_async of the step's samples and error word (device->host, pinned "
-                           "slot) every step, collected into host arrays one step later",
+                           "slot) every step, collected into host arrays two steps later",
                     "per_call_sequence": {"value": e2e_calls, "unit": "Gcell-updates/s",
                                           "how": "the reference's per-step call sequence through the C-ABI "
                                                  "(omx_step_H, omx_source_interactions, omx_step_E, "

@@ -213,6 +213,11 @@ struct omx_ctx {
     // next call's fused pass overlaps it; every other entry point first orders the main stream
     // after it (join_side)
     bool side_pending = false;
+    // an asynchronous drain behind pending side work queues its copies on the side stream and
+    // marks their end with ev_drain: the next one-step call orders its emitter current after the
+    // side kernels only (ev_join), every other entry point after the copies as well
+    cudaEvent_t ev_drain = nullptr;
+    bool drain_pending = false;
     // the reference's per-call sequence on the fused FP32 TMz path: omx_step_H is deferred and
     // fused with the next omx_step_E (sources requested in between are added after the fused
     // pass, as omx_run does); any other entry point first runs the deferred work unfused
@@ -1162,11 +1167,24 @@ template <> void do_post<float>(omx_ctx *c, StepParam amp, StepParam time, StepP
 }
 
 // Order the main stream after the side-stream work a one-step omx_run left running.
-void join_stream(omx_ctx *c)
+// Order the main stream after the side stream's kernels (not after the detector copies an
+// asynchronous drain queued behind them: the next side sequence follows those on the side
+// stream anyway).
+void join_side_kernels(omx_ctx *c)
 {
     if (c && c->side_pending) {
         ck(cudaStreamWaitEvent(c->stream, c->ev_join, 0), "join");
         c->side_pending = false;
+    }
+}
+
+void join_stream(omx_ctx *c)
+{
+    if (!c) return;
+    join_side_kernels(c);
+    if (c->drain_pending) {
+        ck(cudaStreamWaitEvent(c->stream, c->ev_drain, 0), "join");
+        c->drain_pending = false;
     }
 }
 
@@ -1336,7 +1354,7 @@ template <class R> void run_impl(omx_ctx *c, int tt0, int nsteps, int n_skip, in
         const double *row = plan.stage->p;    // this step's table row, on the host
         const bool post = c->post_ok;
         fused_step<R>(c, !post);
-        join_side(c);
+        join_side_kernels(c);
         std::vector<StepParam> amps;
         for (int q = 0; q < nsrc; ++q) amps.push_back(imm(row[4 + q]));
         if (post) {
@@ -1732,6 +1750,7 @@ int omx_destroy(omx_ctx *c)
     }
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     if (c->ev_join) cudaEventDestroy(c->ev_join);
+    if (c->ev_drain) cudaEventDestroy(c->ev_drain);
     for (auto &d : c->drain_slots) {
         if (d.h) cudaFreeHost(d.h);
         if (d.err) cudaFreeHost(d.err);
@@ -2351,7 +2370,13 @@ int omx_detectors_drain_async(omx_ctx *c, long long *ticket)
     }
     ck(cudaMemcpyAsync(d->err, c->d_err.p, sizeof(int), cudaMemcpyDeviceToHost, st), "drain");
     ck(cudaEventRecord(d->ev, st), "drain");
-    if (c->side_pending) ck(cudaEventRecord(c->ev_join, c->side), "join");   // the side sequence now ends here
+    if (c->side_pending) {
+        // the copies end the side stream's queue: entry points that write the records or the
+        // error word on the main stream wait for them (join_stream)
+        if (!c->ev_drain) ck(cudaEventCreateWithFlags(&c->ev_drain, cudaEventDisableTiming), "event");
+        ck(cudaEventRecord(c->ev_drain, c->side), "drain");
+        c->drain_pending = true;
+    }
     // the records are taken: later steps write from slot 0 again (stream order keeps the copy first)
     c->rec_count = 0;
     d->n = n;
