@@ -247,7 +247,9 @@ int omx_detectors_drain(omx_ctx *ctx, double *times, double *values, int max_rec
  * library, clear the device records and return at once with a ticket; later steps may be
  * launched right away.  omx_detectors_collect waits for that ticket's copy and hands its records
  * to the caller (times[n_rec], values[n_rec x total_points]; max_records must cover them) and
- * frees the slot.  OMX_ERR_STATE when every slot holds an uncollected ticket. */
+ * frees the slot.  OMX_ERR_STATE when every slot holds an uncollected ticket.  Behind a
+ * one-step omx_run the copies go on the library's side stream and the next one-step call does
+ * not wait for them; a host that collects each ticket two steps later never waits either. */
 #define OMX_DRAIN_SLOTS 4
 int omx_detectors_drain_async(omx_ctx *ctx, long long *ticket);
 int omx_detectors_collect(omx_ctx *ctx, long long ticket, double *times, double *values, int max_records,
