@@ -271,6 +271,7 @@ struct omx_ctx {
     bool fused_ok = false;
     bool fused_dirty = true;    // media or sources changed since the last eligibility check
     bool post_ok = false;       // the work after the fused pass goes in one launch (post_eligible)
+    bool plane_fold = false;    // the 3D bulk E pass adds the plane source (plane_fold_eligible)
     int step_form = OMX_STEP_DEFAULT;   // omx_set_step_form; a batch sets TWO_PASS on its members
     int *run_step = nullptr;    // device step counter while omx_run issues a step sequence
     std::string err;
@@ -931,6 +932,20 @@ bool post_eligible(const omx_ctx *c)
     return true;
 }
 
+// The two-pass 3D step can add its single plane source inside the bulk E pass (to E_old, before
+// the update, as the separate launch before the pass does) when no dispersive component-cell lies
+// on the plane: those are updated before the bulk pass from the E that already holds the source.
+bool plane_fold_eligible(const omx_ctx *c)
+{
+    if (c->dims != 3 || c->fused_ok || c->sources.size() != 1 || c->sources[0]->kind != 1) return false;
+    const SourceRec &S = *c->sources[0];
+    for (const int4 &e : c->ade_host) {
+        const int at = S.pd.plane_axis == 1 ? e.x : (S.pd.plane_axis == 2 ? e.y : e.z);
+        if (e.w == S.pd.comp - 1 && at == S.pd.plane_index) return false;
+    }
+    return true;
+}
+
 void prepare(omx_ctx *c)
 {
     const bool recheck = c->j_dirty || c->fused_dirty;
@@ -942,7 +957,10 @@ void prepare(omx_ctx *c)
         c->fused_ok = fused_eligible(c);
         c->fused_dirty = false;
     }
-    if (recheck) c->post_ok = post_eligible(c);
+    if (recheck) {
+        c->post_ok = post_eligible(c);
+        c->plane_fold = plane_fold_eligible(c);
+    }
     if (c->fused_ok && !c->ff2[2].p) {
         for (int q = 0; q < 6; ++q)
             if (c->field_used[q]) c->ff2[q].alloc(c->felems);
@@ -1001,11 +1019,23 @@ template <class R> void do_sources(omx_ctx *c, const std::vector<StepParam> &amp
 
 template <class R> void do_inject(omx_ctx *c, StepParam time, StepParam t_skip);
 
-template <class R> void do_E(omx_ctx *c, StepParam time, StepParam t_skip)
+// plane: the amplitude of the context's single plane source when the 3D bulk E pass adds it
+// (plane_fold holds), in place of a k_plane launch before the pass; nullptr otherwise
+template <class R> void do_E(omx_ctx *c, StepParam time, StepParam t_skip, const StepParam *plane = nullptr)
 {
     {
         ProfScope ps(c, KC_E);
-        launch_e<R>(field_ptrs<R>(c), grid_args<R>(c), c->stream);
+        GridArgs<R> G = grid_args<R>(c);
+        if (plane) {
+            const SourceRec &S = *c->sources[0];
+            G.pl_on = 1;
+            G.pl_comp = S.pd.comp - 1;
+            G.pl_axis = S.pd.plane_axis - 1;
+            G.pl_index = S.pd.plane_index;
+            G.pl_c_src = S.c_src;
+            G.pl_amp = *plane;
+        }
+        launch_e<R>(field_ptrs<R>(c), G, c->stream);
         c->launches += 1 + (c->ade_n > 0 ? 1 : 0);
     }
     do_inject<R>(c, time, t_skip);
@@ -1392,6 +1422,9 @@ template <class R> void run_impl(omx_ctx *c, int tt0, int nsteps, int n_skip, in
             fused_step<R>(c);
             do_sources<R>(c, amps);
             do_inject<R>(c, P(0), P(1));
+        } else if (c->plane_fold) {
+            do_H<R>(c);
+            do_E<R>(c, P(0), P(1), &amps[0]);
         } else {
             do_H<R>(c);
             do_sources<R>(c, amps);

@@ -82,6 +82,12 @@ template <class R> struct GridArgs {
     int *step_inc;
     // planes (3D) or rows (2D) marched per thread by the unfused kernels; 0 = default
     int march;
+    // a plane soft source added by the 3D bulk E pass to E_old before the update, as k_plane
+    // does before the pass (pl_on = 0: none); the host enables it only when no plane cell is
+    // dispersive
+    int pl_on, pl_comp, pl_axis, pl_index;
+    double pl_c_src;
+    StepParam pl_amp;
 };
 
 template <class R> struct FieldPtrs {

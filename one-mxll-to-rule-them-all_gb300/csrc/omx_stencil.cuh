@@ -16,6 +16,7 @@
 // already loaded into the next iteration, so each field value is read from memory once.
 #pragma once
 #include "omx_internal.h"
+#include "omx_post.cuh"
 
 namespace omx {
 
@@ -256,6 +257,16 @@ __device__ __forceinline__ void e3_tile(const FieldPtrs<R> &F, const GridArgs<R>
         const R ry = (hz_im - hz_c) * dex + (hx_c - hx_km) * dez;
         const R rz = (hy_c - hy_im) * dex + (hx_jm - hx_c) * dey;
         R ex = __ldcs(Ex + idx), ey = __ldcs(Ey + idx), ez = __ldcs(Ez + idx);   // read by this thread only
+        if (G.pl_on && (G.pl_axis == 0 ? i : (G.pl_axis == 1 ? j : k)) == G.pl_index) {
+            // the plane source of this step (source_interactions before the E update)
+            const double a = sp_get(G.pl_amp);
+            if (a != 0.0) {
+                const double add = __dmul_rn(G.pl_c_src, a);
+                if (G.pl_comp == 0) ex = (R)__dadd_rn((double)ex, add);
+                else if (G.pl_comp == 1) ey = (R)__dadd_rn((double)ey, add);
+                else ez = (R)__dadd_rn((double)ez, add);
+            }
+        }
         if (bb_ij && k >= G.bb0[2] && k <= G.bb1[2]) {
             const long long b = (i - G.bb0[0]) + (long long)G.bbd[0] * ((j - G.bb0[1]) + (long long)G.bbd[1] * (k - G.bb0[2]));
             ex = plain_update<R>(ex, rx, G.mat[0][b], G);
