@@ -48,6 +48,15 @@ inline void req(bool ok, const std::string &msg, int code = OMX_ERR_ARG)
     if (!ok) throw Fail{code, msg};
 }
 
+// Host-to-device copy that has landed when it returns: cudaMemcpy from pageable memory may
+// return before its DMA ends, and the legacy stream it uses does not order the library's
+// non-blocking streams.
+void h2d(void *dst, const void *src, size_t bytes, const char *what)
+{
+    ck(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice), what);
+    ck(cudaStreamSynchronize(0), what);
+}
+
 template <class T> struct DevBuf {
     T *p = nullptr;
     size_t n = 0;
@@ -71,12 +80,16 @@ template <class T> struct DevBuf {
             throw Fail{OMX_ERR_NOMEM, std::string("cudaMalloc failed: ") + cudaGetErrorString(e)};
         }
         n = count;
-        if (zero) ck(cudaMemset(p, 0, count * sizeof(T)), "cudaMemset");
+        if (zero) {
+            // the legacy stream does not order the library's non-blocking streams: wait for it
+            ck(cudaMemset(p, 0, count * sizeof(T)), "cudaMemset");
+            ck(cudaStreamSynchronize(0), "cudaMemset");
+        }
     }
     void upload(const std::vector<T> &v)
     {
         alloc(v.size(), false);
-        if (!v.empty()) ck(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice), "upload");
+        if (!v.empty()) h2d(p, v.data(), v.size() * sizeof(T), "upload");
     }
 };
 
@@ -648,7 +661,7 @@ void build_media(omx_ctx *c, const int32_t *map, const double *eps[3])
     for (int q = 0; q < 3; ++q) {
         if (c->bbV > 0 && act[q]) {
             c->mat[q].alloc((size_t)c->bbV, false);
-            ck(cudaMemcpy(c->mat[q].p, c->host_mat[q].data(), (size_t)c->bbV, cudaMemcpyHostToDevice), "mat");
+            h2d(c->mat[q].p, c->host_mat[q].data(), (size_t)c->bbV, "mat");
         } else {
             c->mat[q].release();
         }
@@ -1247,7 +1260,7 @@ void sync_checked(omx_ctx *c, const char *what)
     ck(cudaStreamSynchronize(c->stream), what);
     if (*c->h_err) {
         *c->h_err = 0;
-        ck(cudaMemset(c->d_err.p, 0, sizeof(int)), what);
+        ck(cudaMemsetAsync(c->d_err.p, 0, sizeof(int), c->stream), what);
         throw Fail{OMX_ERR_CUDA, "fused TMz kernel: a bulk-copy wait ran out; the fields of that step are invalid"};
     }
 }
@@ -1293,10 +1306,10 @@ void stage_upload(omx_ctx *c, const RunPlan &plan, bool first_counted)
     ck(cudaMemcpyAsync(c->tab.p, plan.stage->p, plan.need * sizeof(double), cudaMemcpyHostToDevice, c->stream),
        "tab");
     ck(cudaEventRecord(plan.stage->ev, c->stream), "staging");
-    if (!c->d_step.p) c->d_step.alloc(1);
+    if (!c->d_step.p) c->d_step.alloc(1, false);
     // the first kernel of every step advances the counter, so it starts one below step 0
     ck(cudaMemsetAsync(c->d_step.p, first_counted ? 0x00 : 0xff, sizeof(int), c->stream), "step");
-    if (!c->d_step2.p) c->d_step2.alloc(1);
+    if (!c->d_step2.p) c->d_step2.alloc(1, false);
     ck(cudaMemsetAsync(c->d_step2.p, 0xff, sizeof(int), c->stream), "step");
     c->run_step = c->d_step.p;
 }
@@ -1459,6 +1472,32 @@ template <class R> void run_impl(omx_ctx *c, int tt0, int nsteps, int n_skip, in
         std::swap(c->stream, c->side);
         ck(cudaEventRecord(c->ev_join, c->side), "join");
     };
+    // Two-pass path inside a graph: step s's emitter work and detector sampling (which read E
+    // only) run on the side stream next to step s+1's H pass (which writes H only); step s+1's
+    // sources and E pass, which write E and take the emitter current, wait for them.  Same
+    // operations on the same values as one_step.
+    bool taps_e = true;
+    for (int f : c->tap_field) taps_e = taps_e && f < 3;
+    const bool split = !fused && c->dims >= 2 && (has_det || !c->groups.empty()) && (taps_e || !has_det);
+    auto split_step = [&](bool wait_prev) {
+        do_H<R>(c);
+        if (wait_prev) ck(cudaStreamWaitEvent(c->stream, c->ev_join, 0), "wait");
+        if (c->plane_fold) {
+            do_E<R>(c, P(0), P(1), &amps[0]);
+        } else {
+            do_sources<R>(c, amps);
+            do_E<R>(c, P(0), P(1));
+        }
+        ck(cudaEventRecord(c->ev_fork, c->stream), "fork");
+        ck(cudaStreamWaitEvent(c->side, c->ev_fork, 0), "fork");
+        std::swap(c->stream, c->side);
+        launch_step_advance(c->d_step2.p, c->stream);
+        c->launches++;
+        for (auto &g : c->groups) do_group<R>(c, *g, P2(2));
+        if (has_det) do_sample<R>(c, P2(3), P2(0));
+        std::swap(c->stream, c->side);
+        ck(cudaEventRecord(c->ev_join, c->side), "join");
+    };
     // a captured graph of `steps` steps starting from the current buffer set, from the cache
     // when the configuration is unchanged
     auto launch_graph = [&](int steps, int times) {
@@ -1486,6 +1525,9 @@ template <class R> void run_impl(omx_ctx *c, int tt0, int nsteps, int n_skip, in
             if (fused && (has_det || !c->groups.empty())) {
                 for (int q = 0; q < steps; ++q) overlapped_step(q > 0);
                 ck(cudaStreamWaitEvent(c->stream, c->ev_join, 0), "join");   // the last side sequence
+            } else if (split && steps > 1) {
+                for (int q = 0; q < steps; ++q) split_step(q > 0);
+                ck(cudaStreamWaitEvent(c->stream, c->ev_join, 0), "join");
             } else {
                 for (int q = 0; q < steps; ++q) one_step();
             }
@@ -1506,7 +1548,7 @@ template <class R> void run_impl(omx_ctx *c, int tt0, int nsteps, int n_skip, in
     };
     // the fused path alternates buffer sets, so its graphs cover an even number of steps; long
     // graphs keep the side stream's work overlapped across all but one step boundary per graph
-    const int per_graph = fused ? (nsteps >= 16 ? 16 : 2) : 1;
+    const int per_graph = (fused || split) ? (nsteps >= 16 ? 16 : (fused ? 2 : 1)) : 1;
     if (use_graph && !c->prof) {
         const int ngraph = nsteps / per_graph;
         if (ngraph > 0) launch_graph(per_graph, ngraph);
@@ -1610,7 +1652,7 @@ template <class R> void write_field_impl(omx_ctx *c, int field, const double *ho
     for (int k = lo[2]; k <= hi[2]; ++k)
         for (int j = lo[1]; j <= hi[1]; ++j)
             for (int i = lo[0]; i <= hi[0]; ++i) tmp[(size_t)eindex(c, i, j, k)] = (R)host[o++];
-    ck(cudaMemcpy(field_ptrs<R>(c).f[q], tmp.data(), c->felems * sizeof(R), cudaMemcpyHostToDevice), "write field");
+    h2d(field_ptrs<R>(c).f[q], tmp.data(), c->felems * sizeof(R), "write field");
 }
 
 }  // namespace
@@ -2362,8 +2404,8 @@ int omx_detectors_drain(omx_ctx *c, double *times, double *values, int max_recor
         std::vector<double> tv(rest), vv(rest * (size_t)npts);
         ck(cudaMemcpy(tv.data(), c->rec_times.p + n, sizeof(double) * rest, cudaMemcpyDeviceToHost), "drain");
         ck(cudaMemcpy(vv.data(), c->rec.p + (size_t)n * npts, sizeof(double) * vv.size(), cudaMemcpyDeviceToHost), "drain");
-        ck(cudaMemcpy(c->rec_times.p, tv.data(), sizeof(double) * rest, cudaMemcpyHostToDevice), "drain");
-        ck(cudaMemcpy(c->rec.p, vv.data(), sizeof(double) * vv.size(), cudaMemcpyHostToDevice), "drain");
+        h2d(c->rec_times.p, tv.data(), sizeof(double) * rest, "drain");
+        h2d(c->rec.p, vv.data(), sizeof(double) * vv.size(), "drain");
     }
     c->rec_count -= n;
     *n_records = n;

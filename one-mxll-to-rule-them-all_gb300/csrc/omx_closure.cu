@@ -141,6 +141,8 @@ extern "C" int omx_tc_gemm_bf16(const uint16_t *A, const uint16_t *B, const floa
         cudaMemcpy(dB, B, sizeof(uint16_t) * N * (size_t)K, cudaMemcpyHostToDevice);
         if (bias) cudaMemcpy(dbias, bias, sizeof(float) * N, cudaMemcpyHostToDevice);
         cudaMemset(derr, 0, sizeof(int));
+        cudaStreamSynchronize(0);   // the legacy stream does not order non-blocking streams, and pageable
+                                    // copies may return before their DMA ends
         GemmEpi E{};
         E.d_f32 = dD;
         E.ld_f32 = N;
@@ -664,7 +666,7 @@ static bool cl_finish(omx_closure *c, std::string &err)
     int h = 0;
     CL_CK(cudaMemcpy(&h, c->err.p, sizeof(int), cudaMemcpyDeviceToHost));
     if (h) {
-        cudaMemset(c->err.p, 0, sizeof(int));
+        cudaMemsetAsync(c->err.p, 0, sizeof(int), c->stream);
         err = "closure: a tensor-core pipeline wait ran out";
         return false;
     }
@@ -795,7 +797,8 @@ int omx_closure_create(omx_closure **out)
     if (ok) ok = cudaMemset(c->p.p, 0, sizeof(float) * CL_NPARAM) == cudaSuccess &&
                  cudaMemset(c->m.p, 0, sizeof(float) * CL_NPARAM) == cudaSuccess &&
                  cudaMemset(c->v.p, 0, sizeof(float) * CL_NPARAM) == cudaSuccess &&
-                 cudaMemset(c->err.p, 0, sizeof(int)) == cudaSuccess;
+                 cudaMemset(c->err.p, 0, sizeof(int)) == cudaSuccess &&
+                 cudaStreamSynchronize(0) == cudaSuccess;   // before the closure's own stream runs
     if (!ok) {
         if (c->stream) cudaStreamDestroy(c->stream);
         delete c;
@@ -922,6 +925,7 @@ int omx_closure_trajectories(int model, int n, int T, int K, double dt, const do
         return cl_fail(OMX_ERR_NOMEM, "device allocation failed");
     cudaMemcpy(dp.p, params, sizeof(double) * n * npar, cudaMemcpyHostToDevice);
     cudaMemcpy(dd.p, drive, sizeof(double) * n * (1 + 3 * K), cudaMemcpyHostToDevice);
+    cudaStreamSynchronize(0);   // pageable copies may return before their DMA ends
     ClTrajArgs A{};
     A.n = n;
     A.T = T;

@@ -398,10 +398,12 @@ int omx_fd_create(int dimensions, const int grid_Ndims[3], int n_pml, int n_der,
         for (int a = 0; a < 3; ++a) {
             fck(cudaMalloc(dst[a], sizeof(cplx) * n[a]), "alloc");
             fck(cudaMemcpy(*dst[a], s[a].data(), sizeof(cplx) * n[a], cudaMemcpyHostToDevice), "upload");
+            fck(cudaStreamSynchronize(0), "upload");   // pageable copies may return before their DMA ends
         }
         const size_t ncell = (size_t)G.nx * G.ny * G.nz;
         fck(cudaMalloc(&op->eps, sizeof(cplx) * ncell), "alloc");
         fck(cudaMemcpy(op->eps, eps_r, sizeof(cplx) * ncell, cudaMemcpyHostToDevice), "upload");
+        fck(cudaStreamSynchronize(0), "upload");   // pageable copies may return before their DMA ends
         fck(cudaMalloc(&op->part, sizeof(cplx) * (size_t)G.ny * G.nz), "alloc");
         fck(cudaMallocHost(&op->hpart, sizeof(cplx) * (size_t)G.ny * G.nz), "alloc");
     } catch (const FdErr &e) {
@@ -446,7 +448,8 @@ int omx_fd_apply(omx_fdop *op, const double *f, double *Af, int transpose)
         fck(cudaMalloc(&df, bytes), "alloc");
         fck(cudaMalloc(&dAf, bytes), "alloc");
         fck(cudaMemcpy(df, f, bytes, cudaMemcpyHostToDevice), "upload");
-        fck(cudaMemset(dAf, 0, bytes), "memset");
+        fck(cudaStreamSynchronize(0), "upload");   // pageable copies may return before their DMA ends
+        fck(cudaMemsetAsync(dAf, 0, bytes, op->s), "memset");
         fd_apply_dev(op, df, dAf);
         fck(cudaStreamSynchronize(op->s), "apply");
         fck(cudaMemcpy(Af, dAf, bytes, cudaMemcpyDeviceToHost), "download");
@@ -481,6 +484,7 @@ int omx_fd_time_apply(omx_fdop *op, int reps, double *ms_per_apply)
         fck(cudaMalloc(&df, n * sizeof(cplx)), "alloc");
         fck(cudaMalloc(&dAf, n * sizeof(cplx)), "alloc");
         fck(cudaMemcpy(df, h.data(), n * sizeof(cplx), cudaMemcpyHostToDevice), "upload");
+        fck(cudaStreamSynchronize(0), "upload");   // pageable copies may return before their DMA ends
         fck(cudaEventCreate(&e0), "event");
         fck(cudaEventCreate(&e1), "event");
         for (int r = 0; r < 2; ++r) fd_apply_dev(op, df, dAf);
