@@ -1393,18 +1393,34 @@ template <class R> void run_impl(omx_ctx *c, int tt0, int nsteps, int n_skip, in
     // and the side sequence is left running for the next call (every other entry point joins it
     // first; an asynchronous drain queues its copies behind it).  Same operations on the same
     // values as the graph schedule.
-    if (fused && nsteps == 1 && use_graph && !c->prof && (has_det || !c->groups.empty())) {
+    // The two-pass path does the same with its H pass in place of the fused pass (when the
+    // side work reads E only: every detector samples an E component).
+    bool taps_e = true;
+    for (int f : c->tap_field) taps_e = taps_e && f < 3;
+    const bool split = !fused && c->dims >= 2 && (has_det || !c->groups.empty()) && (taps_e || !has_det);
+    if ((fused || split) && nsteps == 1 && use_graph && !c->prof && (has_det || !c->groups.empty())) {
         const double *row = plan.stage->p;    // this step's table row, on the host
-        const bool post = c->post_ok;
-        fused_step<R>(c, !post);
-        join_side_kernels(c);
         std::vector<StepParam> amps;
         for (int q = 0; q < nsrc; ++q) amps.push_back(imm(row[4 + q]));
-        if (post) {
-            do_post<R>(c, nsrc ? amps[0] : imm(0.0), imm(row[0]), imm(row[1]));
+        if (fused) {
+            const bool post = c->post_ok;
+            fused_step<R>(c, !post);
+            join_side_kernels(c);
+            if (post) {
+                do_post<R>(c, nsrc ? amps[0] : imm(0.0), imm(row[0]), imm(row[1]));
+            } else {
+                do_sources<R>(c, amps);
+                do_inject<R>(c, imm(row[0]), imm(row[1]));
+            }
         } else {
-            do_sources<R>(c, amps);
-            do_inject<R>(c, imm(row[0]), imm(row[1]));
+            do_H<R>(c);
+            join_side_kernels(c);
+            if (c->plane_fold) {
+                do_E<R>(c, imm(row[0]), imm(row[1]), &amps[0]);
+            } else {
+                do_sources<R>(c, amps);
+                do_E<R>(c, imm(row[0]), imm(row[1]));
+            }
         }
         ck(cudaEventRecord(c->ev_fork, c->stream), "fork");
         ck(cudaStreamWaitEvent(c->side, c->ev_fork, 0), "fork");
@@ -1476,9 +1492,6 @@ template <class R> void run_impl(omx_ctx *c, int tt0, int nsteps, int n_skip, in
     // only) run on the side stream next to step s+1's H pass (which writes H only); step s+1's
     // sources and E pass, which write E and take the emitter current, wait for them.  Same
     // operations on the same values as one_step.
-    bool taps_e = true;
-    for (int f : c->tap_field) taps_e = taps_e && f < 3;
-    const bool split = !fused && c->dims >= 2 && (has_det || !c->groups.empty()) && (taps_e || !has_det);
     auto split_step = [&](bool wait_prev) {
         do_H<R>(c);
         if (wait_prev) ck(cudaStreamWaitEvent(c->stream, c->ev_join, 0), "wait");
