@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <functional>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -1993,16 +1994,51 @@ int omx_media_map_from_voxels(int dims, const int grid_Ndims[3], double dr, int 
     OMX_API_END(nullptr)
 }
 
+// The reference's per-call sequence keeps the overlap of the step graphs: q-group steps and
+// detector records that read E only run on the side stream, next to the next step's first pass
+// (the fused pass writes the other buffer set; the two-pass H pass writes H only).  Entry points
+// that write E wait for the side kernels first; every other entry point joins fully (join_side).
+bool side_capable(const omx_ctx *c, bool reads_h)
+{
+    if (c->prof) return false;
+    if (c->fp32 && c->fused_ok) return true;
+    return c->dims >= 2 && !reads_h;
+}
+
+void on_side(omx_ctx *c, const std::function<void()> &launch)
+{
+    ck(cudaEventRecord(c->ev_fork, c->stream), "fork");
+    ck(cudaStreamWaitEvent(c->side, c->ev_fork, 0), "fork");
+    std::swap(c->stream, c->side);
+    try {
+        launch();
+    } catch (...) {
+        std::swap(c->stream, c->side);
+        throw;
+    }
+    std::swap(c->stream, c->side);
+    ck(cudaEventRecord(c->ev_join, c->side), "join");
+    c->side_pending = true;
+}
+
+// Before an entry point that reads E only, or writes H only: the deferred H half and a pending
+// configuration change still join fully.
+void settle_for_side(omx_ctx *c)
+{
+    if (c->h_pending || c->j_dirty || c->det_dirty || c->fused_dirty) join_side(c);
+}
+
 int omx_step_H(omx_ctx *c)
 {
     OMX_API_BEGIN
-    join_side(c);
     req(c, "null context");
+    settle_for_side(c);
     prepare(c);
     if (c->fp32 && c->fused_ok && !c->prof) {
         c->h_pending = true;                 // runs with the next omx_step_E as one fused pass
         return OMX_OK;
     }
+    // the H pass writes H only: side work left pending reads E only (side_capable)
     if (c->fp32) do_H<float>(c);
     else do_H<double>(c);
     ck(cudaPeekAtLastError(), "H launch");
@@ -2015,10 +2051,11 @@ int omx_step_E(omx_ctx *c, double time, double t_skip)
     req(c, "null context");
     if (c->h_pending) {
         // the deferred H half and this E half in one pass, then the sources requested between
-        // them and the emitter current: the order of omx_run's fused step
-        join_stream(c);
+        // them and the emitter current: the order of omx_run's fused step.  The pass reads one
+        // buffer set and writes the other, so it goes before the wait for the side kernels.
         c->h_pending = false;
         fused_step<float>(c);
+        join_side_kernels(c);
         if (c->src_pending) {
             c->src_pending = false;
             std::vector<StepParam> amps;
@@ -2029,7 +2066,8 @@ int omx_step_E(omx_ctx *c, double time, double t_skip)
         ck(cudaPeekAtLastError(), "E launch");
         return OMX_OK;
     }
-    join_side(c);
+    settle_for_side(c);
+    join_side_kernels(c);        // the E pass writes what the side work reads
     prepare(c);
     if (c->fp32) do_E<float>(c, imm(time), imm(t_skip));
     else do_E<double>(c, imm(time), imm(t_skip));
@@ -2124,7 +2162,8 @@ int omx_source_interactions(omx_ctx *c, double time)
         c->src_time = time;
         return OMX_OK;
     }
-    join_side(c);
+    settle_for_side(c);
+    join_side_kernels(c);        // the sources write what the side work reads
     prepare(c);
     std::vector<StepParam> amps;
     for (auto &s : c->sources) amps.push_back(imm(source_amp(*s, time)));
@@ -2209,9 +2248,22 @@ int omx_qgroup_create(omx_ctx *c, const omx_qgroup_desc *d, const int32_t *cell,
 int omx_qgroup_step(omx_ctx *c, int gid, int tq_step)
 {
     OMX_API_BEGIN
-    join_side(c);
     (void)tq_step;
     req(c && gid >= 0 && gid < (int)c->groups.size(), "bad group id");
+    // reads E, writes the group's own state and the current the next E half takes
+    if (side_capable(c, false)) {
+        settle_for_side(c);
+        prepare(c);
+        if (side_capable(c, false)) {
+            on_side(c, [&]() {
+                if (c->fp32) do_group<float>(c, *c->groups[gid], imm(1.0));
+                else do_group<double>(c, *c->groups[gid], imm(1.0));
+            });
+            ck(cudaPeekAtLastError(), "emitter launch");
+            return OMX_OK;
+        }
+    }
+    join_side(c);
     prepare(c);
     if (c->fp32) do_group<float>(c, *c->groups[gid], imm(1.0));
     else do_group<double>(c, *c->groups[gid], imm(1.0));
@@ -2387,13 +2439,26 @@ int omx_detectors_set_capacity(omx_ctx *c, int records)
 int omx_detectors_record(omx_ctx *c, double time)
 {
     OMX_API_BEGIN
-    join_side(c);
     req(c, "null context");
     req(!c->tap_field.empty(), "no detectors");
+    bool reads_h = false;
+    for (int f : c->tap_field) reads_h = reads_h || f >= 3;
+    const bool side = side_capable(c, reads_h);
+    if (side) settle_for_side(c);
+    else join_side(c);
     prepare(c);
-    ensure_rec_capacity(c, c->rec_count + 1);
-    if (c->fp32) do_sample<float>(c, imm((double)c->rec_count), imm(time));
-    else do_sample<double>(c, imm((double)c->rec_count), imm(time));
+    ensure_rec_capacity(c, c->rec_count + 1);   // joins fully when it moves the records
+    if (side && side_capable(c, reads_h)) {
+        // the records are written on the side stream, behind any copies queued there
+        on_side(c, [&]() {
+            if (c->fp32) do_sample<float>(c, imm((double)c->rec_count), imm(time));
+            else do_sample<double>(c, imm((double)c->rec_count), imm(time));
+        });
+    } else {
+        join_side(c);
+        if (c->fp32) do_sample<float>(c, imm((double)c->rec_count), imm(time));
+        else do_sample<double>(c, imm((double)c->rec_count), imm(time));
+    }
     ck(cudaPeekAtLastError(), "sample launch");
     c->rec_count++;
     OMX_API_END(c)
