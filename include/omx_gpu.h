@@ -179,6 +179,11 @@ int omx_media_map_from_voxels(int dimensions, const int grid_Ndims[3], double dr
                               const int *n_vox, const double *vox_nm, int32_t *media_map);
 
 /* ---- time stepping (TMxll%td_propagate_*) --------------------------------------------------- */
+/* Every call queues device work and returns.  In the reference's per-step order (omx_step_H,
+ * omx_source_interactions, omx_step_E, omx_qgroup_step, omx_detectors_record) the q-group step
+ * and the detector record (when every detector samples an E component, or on the fused FP32
+ * path) run on the library's side stream next to the next step's first pass; the calls that
+ * write E wait for them on the device, and every other entry point orders itself after them. */
 int omx_step_H(omx_ctx *ctx);                                  /* td_propagate_H_field */
 int omx_step_E(omx_ctx *ctx, double time, double t_skip);      /* td_propagate_E_field */
 
