@@ -422,6 +422,8 @@ def gpu_arm(args, dist):
     recorded = {14: "k_fused_tmz_ws<0, 4, 1, 4> tmz4096", 44: "k_fused_tmz_ws<0, 4, 1, 8> tmz4096"}
     if dom == "fused_HE" and args.config == "cfg2" and shape in recorded:
         traffic, traffic_src = recorded_traffic(recorded[shape])
+    elif args.config == "cfg3" and (args.grid or 512) == 512 and dom in ("H", "E"):
+        traffic, traffic_src = recorded_traffic("k_%s3<float, 0> cfg3 512^3" % dom.lower())
     avg_s = per[dom]["ms_total"] / per[dom]["launches"] / 1e3
     peak, peak_kind = peaks()
     achieved = alg_bytes / avg_s / 1e9
