@@ -1,7 +1,9 @@
-// omx_post.cuh -- per-cell operations that follow an E update, shared by both kernel translation
-// units: the step-parameter read, the plane source and the emitter-current term.  They are
-// written with explicit round-to-nearest operations, so a unit compiled with FMA contraction
-// gives the same bits as the contraction-free unit (FP64 arithmetic, as the reference's).
+// omx_post.cuh -- per-cell source and current terms of the E update, shared by both kernel
+// translation units and by several kernels (the separate source / current kernels, the merged
+// launch after a fused pass, the 3D bulk E pass): the step-parameter read, the plane source and
+// the emitter-current term.  They are written with explicit round-to-nearest operations, so a
+// unit compiled with FMA contraction gives the same bits as the contraction-free unit (FP64
+// arithmetic, as the reference's).
 #pragma once
 #include "omx_internal.h"
 
