@@ -3002,20 +3002,28 @@ template <class R> void batch_run_impl(omx_batch *b, int tt0, int nsteps, int n_
     if (b->blocks == 0) b->blocks = batch3_blocks<R>();
     const BatchTables<R> T = batch_tables<R>(b, &plans, kch);
     if (use_graph) {
-        cudaGraph_t graph;
-        ck(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "capture");
-        const long long per = batch_step<R>(b, T, plans, kch);
-        ck(cudaStreamEndCapture(b->stream, &graph), "end capture");
-        cudaGraphExec_t exec = nullptr;
-        const cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
-        cudaGraphDestroy(graph);
-        ck(e, "instantiate");
-        struct Destroy {
-            cudaGraphExec_t x;
-            ~Destroy() { cudaGraphExecDestroy(x); }
-        } destroy{exec};
-        for (int s = 0; s < nsteps; ++s) ck(cudaGraphLaunch(exec, b->stream), "graph launch");
-        b->launches += per * nsteps;   // (an executable graph destroyed in flight is freed on completion)
+        // graphs of up to 8 steps (the step counters advance on the device, so every replay
+        // runs the next steps); the remainder in one shorter graph
+        auto run_graph = [&](int steps, int times) {
+            cudaGraph_t graph;
+            ck(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "capture");
+            long long per = 0;
+            for (int q = 0; q < steps; ++q) per += batch_step<R>(b, T, plans, kch);
+            ck(cudaStreamEndCapture(b->stream, &graph), "end capture");
+            cudaGraphExec_t exec = nullptr;
+            const cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+            cudaGraphDestroy(graph);
+            ck(e, "instantiate");
+            struct Destroy {
+                cudaGraphExec_t x;
+                ~Destroy() { cudaGraphExecDestroy(x); }
+            } destroy{exec};
+            for (int s = 0; s < times; ++s) ck(cudaGraphLaunch(exec, b->stream), "graph launch");
+            b->launches += per * times;   // (an executable graph destroyed in flight is freed on completion)
+        };
+        const int per_graph = std::min(nsteps, 8);
+        if (per_graph > 0) run_graph(per_graph, nsteps / per_graph);
+        if (per_graph > 0 && nsteps % per_graph) run_graph(nsteps % per_graph, 1);
     } else {
         for (int s = 0; s < nsteps; ++s) b->launches += batch_step<R>(b, T, plans, kch);
     }
