@@ -263,29 +263,35 @@ def error_statement(deck, nsteps):
 
 
 # ---------------------------------------------------------------------------------- CPU leg
-def cpu_run(deck, seconds, max_steps=None):
-    """The FP64 oracle (CPU restatement of the reference) stepping the same workload."""
+def cpu_run(deck, seconds, max_steps=None, warmup=1):
+    """The FP64 oracle (CPU restatement of the reference) stepping the same workload: `warmup`
+    untimed steps, then timed steps until `max_steps` or until `seconds` have passed.  Everything
+    on this leg is the oracle's own (media map, media, sources, emitters): the GPU library is not
+    loaded."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    sys.path.insert(0, os.path.join(ROOT, "tests"))
     import build_oracle
 
     build_oracle.build()
-    import omx
     import oracle as orc
-    from omx import decks
-    from gpu_harness import OracleFactory
+    from omx import decks       # the seeded deck generator (pure Python, no library)
 
     g = orc.Grid(deck["dimensions"], deck["grid_Ndims"], deck["npml"], deck["boundaries"], deck["dt"], deck["dr"],
                  mode=deck["mode"])
-    mm = decks.media_map(deck, omx.media_map_from_voxels)
-    groups = decks.apply_deck(g, deck, OracleFactory(orc), mm)
+    mm = decks.media_map(deck, orc.media_map) if deck["voxels"] else None
+    groups = decks.apply_deck(g, deck, orc, mm)
     loop = Loop(deck)
-    loop.step(g, groups, 1)            # first step outside the clock
-    n, t0 = 0, time.perf_counter()
-    while True:
-        loop.step(g, groups, 2 + n)
+
+    def step(tt):
+        loop.step(g, groups, tt)
         for det in deck["detectors"]:
             g.sample(det["type"], det["field"], det["idx"])
+
+    w = max(1, int(warmup))
+    for tt in range(1, w + 1):         # warm-up steps outside the clock
+        step(tt)
+    n, t0 = 0, time.perf_counter()
+    while True:
+        step(w + 1 + n)
         n += 1
         el = time.perf_counter() - t0
         if (el >= seconds and n >= 2) or (max_steps and n >= max_steps):
@@ -351,10 +357,11 @@ def reference_arm(args, dist):
     # W warm-up steps and K timed steps of the CPU restatement, each bounded: the whole run is
     # sized to finish within a few minutes (about 2 s per timed step at most).
     per_step_budget = 2.0
-    n, el, cores = cpu_run(deck, seconds=min(per_step_budget * args.steps, 150.0), max_steps=args.steps)
+    W = max(1, args.warmup)
+    n, el, cores = cpu_run(deck, seconds=min(per_step_budget * args.steps, 150.0), max_steps=args.steps, warmup=W)
     v = cells * n / el / 1e9
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "Gcell-updates/s", "n_gpus": 0,
-            "steps": n, "warmup": 1, "ms_per_step": el / n * 1e3, "higher_is_better": True, "scaling": "weak",
+            "steps": n, "warmup": W, "ms_per_step": el / n * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": desc, "cells": cells, "emitters": n_emitters(deck)},
             "cpu_baseline": {"value": v, "unit": "Gcell-updates/s", "cores": cores, "kind": "port",
@@ -382,6 +389,8 @@ def gpu_arm(args, dist):
     gpu, groups = build_gpu(deck, "fp32")
     shape = gpu.autotune(reps=20) if not args.no_autotune else (44 if deck["dimensions"] == 2 else 16)
     gpu.run(1, W, deck["n_skip"], tdp, use_graph=True)
+    # the step graphs of the timed call are captured and instantiated here, outside the clock
+    gpu.prepare_run(1 + W, K, deck["n_skip"], tdp)
     gpu.synchronize()
     dist.barrier()
     clocks = ClockSampler(dist.local_rank)
@@ -484,6 +493,7 @@ def gpu_arm(args, dist):
         if not args.no_autotune:
             g64.autotune(reps=20)
         g64.run(1, W, deck["n_skip"], tdp, use_graph=True)
+        g64.prepare_run(1 + W, K, deck["n_skip"], tdp)
         g64.synchronize()
         g64.timer_start()
         g64.run(1 + W, K, deck["n_skip"], tdp, use_graph=True)
@@ -704,6 +714,7 @@ def gpu_arm_cfg4(args, dist):
 
     def timed(g):
         g.run(1, W, deck["n_skip"], 0, use_graph=True)
+        g.prepare_run(1 + W, K, deck["n_skip"], 0)
         g.synchronize()
         dist.barrier()
         g.timer_start()

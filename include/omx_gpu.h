@@ -208,11 +208,11 @@ int omx_qgroup_state_size(int model);
 /* ---- emitter step without allocation --------------------------------------------------------- */
 /* No counterpart in the reference (an addition of this library).
  *
- * For callers that cannot call cudaMalloc -- code that runs while a CUDA graph is being
- * captured, or a host that owns all device memory through its own pool or device arrays and
- * forbids the device-wide synchronisation of cudaMalloc / cudaFree in its time loop -- this
- * entry point advances a batch of few-level emitters and updates their current arrays entirely
- * in caller-provided device memory, and allocates nothing.  It computes what omx_qgroup_step does
+ * For callers that cannot call cudaMalloc -- a host that owns all device memory through its
+ * own pool or through Fortran/OpenACC device arrays, and forbids allocation in its time loop
+ * because cudaMalloc / cudaFree synchronise the whole device -- this entry point advances a
+ * batch of few-level emitters and updates their current arrays entirely in caller-provided
+ * device memory, and allocates nothing.  It computes what omx_qgroup_step does
  * after its field gather, from the gathered E samples:
  *   E       n_emitters x 3 device doubles, the E at each emitter (input)
  *   params  n_emitters x 7 | 9 (model), as omx_qgroup_create (input)
@@ -228,8 +228,10 @@ int omx_qgroup_state_size(int model);
  * loading the library holds until the process exits.  n_emitters above
  * OMX_NOALLOC_MAX_EMITTERS is rejected with OMX_ERR_ARG.  All calls share that array: calls
  * that overlap on the GPU (other streams, other host threads) race and must be serialised by the
- * caller.  The first call on each device looks the array's device address up (no allocation);
- * make that first call before any stream capture.  Errors are read with omx_last_error(NULL). */
+ * caller.  The first call on each device looks the array's device address up (no allocation)
+ * and must be made with that device current; make that first call before any stream capture.
+ * The array keeps the last call's values; every call overwrites the part it uses before
+ * reading it.  Errors are read with omx_last_error(NULL). */
 #define OMX_NOALLOC_MAX_EMITTERS 65536
 int omx_emitter_step_noalloc(int model, int n_emitters, const double *E, const double *params,
                              double *rho, double *dipole, int n_points, const int *winner,
@@ -286,6 +288,12 @@ int omx_qgroup_write_text(omx_ctx *ctx, int group, const char *dir, double time,
  * mxim_mxll.f90:73-83.  use_graph != 0 runs the step sequence as a captured CUDA graph; the
  * graph is kept and reused by later calls until a configuration call changes the context. */
 int omx_run(omx_ctx *ctx, int tt0, int nsteps, int n_skip_steps, int t_det_print, int use_graph);
+/* No counterpart in the reference.  Captures and instantiates the CUDA graphs that
+ * omx_run(ctx, tt0, nsteps, n_skip_steps, t_det_print, 1) launches, and sizes the step table
+ * and the detector record buffer for it, without running a step (the stepping state, fields
+ * and records are unchanged).  A host that calls it before its time loop keeps the capture
+ * and instantiation cost out of the loop. */
+int omx_run_prepare(omx_ctx *ctx, int tt0, int nsteps, int n_skip_steps, int t_det_print);
 
 /* Kernel form of the FP32 time step (no counterpart in the reference).  Every form meets the same
  * FP32 bar; they differ in rounding, and the form may be changed between steps.

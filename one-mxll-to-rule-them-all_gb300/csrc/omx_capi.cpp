@@ -1298,19 +1298,25 @@ struct RunPlan {
 };
 // The device side of the staging: the table copy and the step counters.  first_counted: the
 // step's first kernel already ran without a counter, so the main counter starts at step 0.
-void stage_upload(omx_ctx *c, const RunPlan &plan, bool first_counted)
+// The device table and the step counters exist with room for the plan (a larger table is a new
+// allocation, which invalidates the captured graphs).
+void stage_reserve(omx_ctx *c, const RunPlan &plan)
 {
     if (plan.need > c->tab.n) {
         c->tab.alloc(std::max(plan.need, 2 * c->tab.n), false);
         c->epoch++;
     }
+    if (!c->d_step.p) c->d_step.alloc(1, false);
+    if (!c->d_step2.p) c->d_step2.alloc(1, false);
+}
+void stage_upload(omx_ctx *c, const RunPlan &plan, bool first_counted)
+{
+    stage_reserve(c, plan);
     ck(cudaMemcpyAsync(c->tab.p, plan.stage->p, plan.need * sizeof(double), cudaMemcpyHostToDevice, c->stream),
        "tab");
     ck(cudaEventRecord(plan.stage->ev, c->stream), "staging");
-    if (!c->d_step.p) c->d_step.alloc(1, false);
     // the first kernel of every step advances the counter, so it starts one below step 0
     ck(cudaMemsetAsync(c->d_step.p, first_counted ? 0x00 : 0xff, sizeof(int), c->stream), "step");
-    if (!c->d_step2.p) c->d_step2.alloc(1, false);
     ck(cudaMemsetAsync(c->d_step2.p, 0xff, sizeof(int), c->stream), "step");
     c->run_step = c->d_step.p;
 }
@@ -1368,14 +1374,25 @@ RunPlan stage_run(omx_ctx *c, int tt0, int nsteps, int n_skip, int t_det_print, 
 
 StepParam plan_param(omx_ctx *c, const RunPlan &plan, int row) { return StepParam{0.0, c->tab.p + row, c->d_step.p, plan.W}; }
 
-template <class R> void run_impl(omx_ctx *c, int tt0, int nsteps, int n_skip, int t_det_print, int use_graph)
+// prepare_only: capture and instantiate the step graphs that the same call without it launches,
+// with the device table and the record buffer sized for it, and run nothing (the stepping state
+// and the record count stay as they are).
+template <class R> void run_impl(omx_ctx *c, int tt0, int nsteps, int n_skip, int t_det_print, int use_graph,
+                                 bool prepare_only = false)
 {
     if (c->h_pending) join_side(c);
     // a configuration change, or anything but a one-step graph call, first waits for the side
     // sequence a previous one-step call left running
-    if (c->j_dirty || c->det_dirty || c->fused_dirty || !c->started || nsteps != 1 || !use_graph || c->prof)
+    if (c->j_dirty || c->det_dirty || c->fused_dirty || !c->started || nsteps != 1 || !use_graph || c->prof ||
+        prepare_only)
         join_side(c);
+    const double t_skip0 = c->t_skip;
+    const int tq_old0 = c->tq_step_old;
     const RunPlan plan = stage_run(c, tt0, nsteps, n_skip, t_det_print, false);
+    if (prepare_only) {
+        c->t_skip = t_skip0;
+        c->tq_step_old = tq_old0;
+    }
     struct Reset {
         omx_ctx *c;
         ~Reset() { c->run_step = nullptr; }
@@ -1399,7 +1416,7 @@ template <class R> void run_impl(omx_ctx *c, int tt0, int nsteps, int n_skip, in
     bool taps_e = true;
     for (int f : c->tap_field) taps_e = taps_e && f < 3;
     const bool split = !fused && c->dims >= 2 && (has_det || !c->groups.empty()) && (taps_e || !has_det);
-    if ((fused || split) && nsteps == 1 && use_graph && !c->prof && (has_det || !c->groups.empty())) {
+    if (!prepare_only && (fused || split) && nsteps == 1 && use_graph && !c->prof && (has_det || !c->groups.empty())) {
         const double *row = plan.stage->p;    // this step's table row, on the host
         std::vector<StepParam> amps;
         for (int q = 0; q < nsrc; ++q) amps.push_back(imm(row[4 + q]));
@@ -1436,7 +1453,8 @@ template <class R> void run_impl(omx_ctx *c, int tt0, int nsteps, int n_skip, in
         return;
     }
     join_side(c);
-    stage_upload(c, plan, false);
+    if (prepare_only) stage_reserve(c, plan);
+    else stage_upload(c, plan, false);
     std::vector<StepParam> amps;
     for (int q = 0; q < nsrc; ++q) amps.push_back(P(4 + q));
     auto tail = [&]() {
@@ -1558,22 +1576,25 @@ template <class R> void run_impl(omx_ctx *c, int tt0, int nsteps, int n_skip, in
         }
         for (int s = 0; s < times; ++s) ck(cudaGraphLaunch(hit->exec, c->stream), "graph launch");
         c->launches += hit->launches * times;
-        c->cur = hit->cur_after;   // after an even number of fused steps this is the starting set
+        // after an even number of fused steps this is the starting set; a graph only captured
+        // (times == 0) leaves the set as it is
+        if (times > 0) c->cur = hit->cur_after;
     };
     // the fused path alternates buffer sets, so its graphs cover an even number of steps; long
     // graphs keep the side stream's work overlapped across all but one step boundary per graph
     const int per_graph = (fused || split) ? (nsteps >= 16 ? 16 : (fused ? 2 : 1)) : 1;
     if (use_graph && !c->prof) {
         const int ngraph = nsteps / per_graph;
-        if (ngraph > 0) launch_graph(per_graph, ngraph);
+        const int k = prepare_only ? 0 : 1;
+        if (ngraph > 0) launch_graph(per_graph, k * ngraph);
         int left = nsteps - ngraph * per_graph;
-        if (left >= 2) launch_graph(2, left / 2);
-        if (left % 2) launch_graph(1, 1);
-    } else {
+        if (left >= 2) launch_graph(2, k * (left / 2));
+        if (left % 2) launch_graph(1, k);
+    } else if (!prepare_only) {
         for (int s = 0; s < nsteps; ++s) one_step();
     }
     ck(cudaPeekAtLastError(), "launch");
-    c->rec_count += nrec;
+    if (!prepare_only) c->rec_count += nrec;
 }
 
 // Time each candidate launch shape on the device and keep the fastest.  Runs on fields that are
@@ -2731,6 +2752,18 @@ int omx_run(omx_ctx *c, int tt0, int nsteps, int n_skip_steps, int t_det_print, 
     if (nsteps == 0) return OMX_OK;
     if (c->fp32) run_impl<float>(c, tt0, nsteps, n_skip_steps, t_det_print, use_graph);
     else run_impl<double>(c, tt0, nsteps, n_skip_steps, t_det_print, use_graph);
+    OMX_API_END(c)
+}
+
+int omx_run_prepare(omx_ctx *c, int tt0, int nsteps, int n_skip_steps, int t_det_print)
+{
+    OMX_API_BEGIN
+    req(c && nsteps >= 0 && n_skip_steps >= 1 && tt0 >= 1, "bad argument");
+    req(!c->prof, "profiling is on: runs launch kernels one by one", OMX_ERR_STATE);
+    if (nsteps == 0) return OMX_OK;
+    if (c->fp32) run_impl<float>(c, tt0, nsteps, n_skip_steps, t_det_print, 1, true);
+    else run_impl<double>(c, tt0, nsteps, n_skip_steps, t_det_print, 1, true);
+    sync_checked(c, "prepare");
     OMX_API_END(c)
 }
 

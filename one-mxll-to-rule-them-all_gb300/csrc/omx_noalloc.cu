@@ -1,18 +1,19 @@
 // omx_noalloc.cu -- an emitter step that allocates nothing.
 //
-// Some callers cannot call cudaMalloc: code running while a CUDA graph is being captured (an
-// allocation there is not allowed and would break the capture), and hosts that own all device
-// memory through their own pool or through Fortran/OpenACC device arrays and forbid the
-// implicit device-wide synchronisation of cudaMalloc / cudaFree in their time loop.  For them
-// this file provides one entry point that advances a batch of few-level emitters and updates
-// the emitter current arrays entirely in caller-provided device memory.  The only extra memory
-// it needs -- the dP/dt of every emitter, produced by the density-matrix step and consumed by
-// the current scatter -- lives in a fixed file-scope device array below.
+// Some callers cannot call cudaMalloc: hosts that own all device memory through their own pool
+// or through Fortran/OpenACC device arrays, and that forbid allocation in their time loop
+// because cudaMalloc / cudaFree synchronise the whole device and would stall every stream the
+// host keeps busy.  For them this file provides one entry point that advances a batch of
+// few-level emitters and updates the emitter current arrays entirely in caller-provided device
+// memory.  The only extra memory it needs -- the dP/dt of every emitter, produced by the
+// density-matrix step and consumed by the current scatter -- lives in a fixed file-scope
+// device array below.
 //
 // Compiled without FMA contraction, like every FP64 kernel of the library: the results equal
 // the context API's (omx_qgroup_step) bit for bit for the same inputs.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <string>
 
 #include "../../include/omx_gpu.h"
@@ -29,9 +30,13 @@ namespace {
 __device__ __align__(256) double g_noalloc_dpdt[3 * OMX_NOALLOC_MAX_EMITTERS];
 
 // Address of g_noalloc_dpdt on each device, looked up once per device (host code cannot use the
-// symbol's name as a device address).
+// symbol's name as a device address: on the host it names a stand-in, not device memory).  Two
+// host threads making their first call on a device at the same time may both look it up; they
+// store the same value, and the atomic makes that store well defined.  The address belongs to
+// the device's primary context: after cudaDeviceReset the library's state on that device,
+// this cache included, is no longer valid, and the process must not call into it again.
 constexpr int kMaxDevices = 64;
-double *g_scratch_addr[kMaxDevices] = {nullptr};
+std::atomic<double *> g_scratch_addr[kMaxDevices] = {};
 
 // td_propagate for every emitter from caller-provided E samples (the gathered E of
 // send_E_to_J_ranks): RK4 density-matrix step, dipole, dP/dt into the scratch.
@@ -116,18 +121,19 @@ extern "C" int omx_emitter_step_noalloc(int model, int n_emitters, const double 
         cudaGetLastError();
         return fail(OMX_ERR_NODEV, "omx_emitter_step_noalloc: no usable CUDA device");
     }
-    // first call on this device: look the scratch address up (no allocation); make this first
-    // call before any stream capture
-    if (!g_scratch_addr[dev]) {
+    // first call on this device, with the device current: look the scratch address up (no
+    // allocation); make this first call before any stream capture
+    double *dpdt = g_scratch_addr[dev].load(std::memory_order_acquire);
+    if (!dpdt) {
         void *p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_dpdt);
         if (e != cudaSuccess || !p) {
             cudaGetLastError();
             return fail(OMX_ERR_CUDA, "omx_emitter_step_noalloc: cudaGetSymbolAddress failed");
         }
-        g_scratch_addr[dev] = static_cast<double *>(p);
+        dpdt = static_cast<double *>(p);
+        g_scratch_addr[dev].store(dpdt, std::memory_order_release);
     }
-    double *dpdt = g_scratch_addr[dev];
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const int npar = model == OMX_EMITTER_TWO_LEVEL ? 7 : 9;
     const int nst = model == OMX_EMITTER_TWO_LEVEL ? 3 : 8;

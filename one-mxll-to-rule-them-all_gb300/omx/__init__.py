@@ -293,6 +293,10 @@ class TMxll:
         self._chk(lib().omx_run(self._ctx, int(tt0), int(nsteps), int(n_skip_steps), int(t_det_print),
                                 1 if use_graph else 0))
 
+    def prepare_run(self, tt0, nsteps, n_skip_steps=1, t_det_print=0):
+        """Capture the step graphs `run(tt0, nsteps, ...)` launches, without running a step."""
+        self._chk(lib().omx_run_prepare(self._ctx, int(tt0), int(nsteps), int(n_skip_steps), int(t_det_print)))
+
     def write_detectors_text(self, directory):
         """Drain the records into the reference's detector file layout; returns the count."""
         n = C.c_int()

@@ -108,6 +108,7 @@ SIGNATURES = {
     "omx_set_step_form": (_I, [_VP, _I]),
     "omx_detectors_collect": (_I, [_VP, C.c_longlong, _PD, _PD, _I, _PI]),
     "omx_run": (_I, [_VP, _I, _I, _I, _I, _I]),
+    "omx_run_prepare": (_I, [_VP, _I, _I, _I, _I]),
     "omx_detectors_write_text": (_I, [_VP, C.c_char_p, _PI]),
     "omx_detectors_dft_setup": (_I, [_VP, _I, _PD, _D]),
     "omx_detectors_dft_read": (_I, [_VP, _PD, _PD]),
