@@ -57,6 +57,11 @@ def parse():
     p.add_argument("--skip-plain", action="store_true")
     p.add_argument("--error-steps", type=int, default=None,
                    help="length of the FP32-vs-FP64 error run (default: the configuration's full run)")
+    p.add_argument("--no-subrecords", action="store_true",
+                   help="cfg2: leave out the records of the 3D configurations (cfg1, cfg3)")
+    p.add_argument("--cfg3-error-steps", type=int, default=2000,
+                   help="prefix of the 512^3 run over which its FP32 error is stated in the cfg2 line")
+    p.add_argument("--sub-cpu-seconds", type=float, default=4.0)
     return p.parse_args()
 
 
@@ -236,9 +241,13 @@ def recorded_traffic(key):
 
 
 def rel_err(a, b):
+    """max over detectors and samples of |a - b| / max|b| of that detector, the normaliser
+    floored at 1e-6 of the largest detector's: a detector the pulse has not reached holds
+    numerical precursor values (1e-30 and below) that FP32 does not represent."""
     import numpy as np
 
-    scale = np.maximum(np.max(np.abs(b), axis=0), 1e-300)
+    m = np.max(np.abs(b), axis=0)
+    scale = np.maximum(m, max(1e-6 * float(np.max(m)), 1e-300))
     return float(np.max(np.abs(a - b) / scale))
 
 
@@ -371,23 +380,23 @@ def reference_arm(args, dist):
 
 
 # ---------------------------------------------------------------------------------- GPU arm
-def gpu_arm(args, dist):
-    import numpy as np
-
+def measure(args, dist, config, grid, K, W, err_steps, cpu_seconds):
+    """One configuration on this GPU: the chosen FP32 path device-timed over K steps of the
+    device loop (pre-instantiated CUDA graphs), per-kernel times, the roofline of the dominant
+    kernel, the end-to-end C-ABI rates, the plain FP64 path with the FP32 error statement over
+    `err_steps` steps, and the CPU oracle on rank 0 (a bounded sample)."""
     import omx
 
-    if dist.world > 1:
-        omx.select_device(dist.local_rank % max(1, omx.device_count()))
-    deck, desc = make_deck(args.config, args.grid)
+    deck, desc = make_deck(config, grid)
     cells = cells_of(deck)
     ne = n_emitters(deck)
-    K, W = args.steps, max(3, args.warmup)
     tdp = deck["t_det_print"]
+    dims = deck["dimensions"]
 
-    # ---- chosen path: FP32 fused, device loop in a CUDA graph; the launch shape from the
-    # library's autotuner (omx_autotune, timed on the zero initial fields before the first step)
+    # ---- chosen path: FP32 (one fused pass per step where eligible), device loop in CUDA
+    # graphs; the launch shape from the library's autotuner (timed on the zero initial fields)
     gpu, groups = build_gpu(deck, "fp32")
-    shape = gpu.autotune(reps=20) if not args.no_autotune else (44 if deck["dimensions"] == 2 else 16)
+    shape = gpu.autotune(reps=20) if not args.no_autotune else None
     gpu.run(1, W, deck["n_skip"], tdp, use_graph=True)
     # the step graphs of the timed call are captured and instantiated here, outside the clock
     gpu.prepare_run(1 + W, K, deck["n_skip"], tdp)
@@ -421,18 +430,14 @@ def gpu_arm(args, dist):
     dom = max(("H", "E"), key=lambda k: per[k]["ms_total"])
     kc_dom = omx.KC_H if dom == "H" else omx.KC_E
     kernel_name = {"H": "k_h2/k_h3 (H half-step)", "E": "k_e2/k_e3 (E half-step)"}[dom]
-    if per["H"]["launches"] == 0:      # FP32 2D TMz: one fused pass per step
+    if per["H"]["launches"] == 0:      # one fused pass per step
         per["fused_HE"] = per.pop("E")
         per.pop("H")
-        dom, kernel_name = "fused_HE", ("k_fused3 (3D H+E step in one pass)" if deck["dimensions"] == 3 else
+        dom, kernel_name = "fused_HE", ("k_fused3_tma (3D H+E step in one pass, planes staged by TMA)"
+                                        if dims == 3 else
                                         "k_fused_tmz_ws (H+E step in one pass; form from omx_autotune)")
     alg_bytes = gpu.algorithmic_bytes(kc_dom)
-    traffic, traffic_src = (None, None)
-    recorded = {14: "k_fused_tmz_ws<0, 4, 1, 4> tmz4096", 44: "k_fused_tmz_ws<0, 4, 1, 8> tmz4096"}
-    if dom == "fused_HE" and args.config == "cfg2" and shape in recorded:
-        traffic, traffic_src = recorded_traffic(recorded[shape])
-    elif args.config == "cfg3" and (args.grid or 512) == 512 and dom in ("H", "E"):
-        traffic, traffic_src = recorded_traffic("k_%s3<float, 0> cfg3 512^3" % dom.lower())
+    traffic, traffic_src = recorded_traffic("%s %s" % (dom, config + ("" if grid is None else "@%d" % grid)))
     avg_s = per[dom]["ms_total"] / per[dom]["launches"] / 1e3
     peak, peak_kind = peaks()
     achieved = alg_bytes / avg_s / 1e9
@@ -448,8 +453,8 @@ def gpu_arm(args, dist):
 
     def e2e_run(one_step):
         g, grp = build_gpu(deck, "fp32")
-        if not args.no_autotune:
-            g.autotune(reps=20)
+        if shape is not None:
+            g.set_launch_shape(shape)
         pend = []
         for tt in range(1, W + 1):
             one_step(g, grp, tt, pend)
@@ -501,59 +506,87 @@ def gpu_arm(args, dist):
         g64.drain_detectors()
         v64 = dist.world * cells * K / (ms64 / 1e3) / 1e9
         g64.kill()
-        nerr = args.error_steps or deck["steps"]
-        field_err, dip_err = error_statement(deck, nerr)
+        field_err, dip_err = error_statement(deck, err_steps)
         plain = {"value": v64, "unit": "Gcell-updates/s", "ms_per_step": ms64 / K,
                  "emitter_steps_per_s": dist.world * ne * K / (ms64 / 1e3),
                  "speedup_fp32_over_fp64": value / v64,
                  "fp32_max_rel_detector_error": field_err, "fp32_max_rel_dipole_error": dip_err,
-                 "error_run_steps": nerr,
+                 "error_run_steps": err_steps, "configuration_steps": deck["steps"],
                  "error_definition": "max over detectors and steps of |fp32 - fp64| / max|fp64 trace| of that "
-                                     "detector; dipoles: max |fp32 - fp64| / max |fp64| at the end of the run"}
+                                     "detector (floored at 1e-6 of the largest detector's); dipoles: "
+                                     "max |fp32 - fp64| / max |fp64| at the end of the run"}
 
     # ---- CPU baseline: bounded sample of the oracle on rank 0 --------------------------------
     cpu = None
-    if dist.rank == 0:
-        n, el, cores = cpu_run(deck, seconds=args.cpu_seconds)
+    if dist.rank == 0 and cpu_seconds > 0:
+        n, el, cores = cpu_run(deck, seconds=cpu_seconds)
         cpu = {"value": cells * n / el / 1e9, "unit": "Gcell-updates/s", "cores": cores, "kind": "port",
                "sample": f"{n} full steps of the same workload, FP64 oracle (C restatement of the reference, "
                          f"OpenMP on the bulk loops as in the reference)"}
+    if shape is None:
+        shape_desc = "library default"
+    elif dims == 3 and shape >= 1000:
+        shape_desc = "fused 3D tile 32 x %d, %d planes per block (omx_autotune)" % (shape // 1000, shape % 1000)
+    elif dims == 2:
+        shape_desc = "fused-kernel form %d (omx_autotune)" % shape
+    else:
+        shape_desc = "planes marched per thread %d (omx_autotune)" % shape
+    return {
+        "value": value, "ms_per_step": ms_max / K, "steps": K, "warmup": W,
+        "config": {"workload": desc, "cells": cells, "emitters": ne, "precision": "fp32 fields, fp64 emitters",
+                   "parallelism": f"replicas x{dist.world}" if dist.world > 1 else "single GPU",
+                   "l2": "working set %.0f MB > 126 MB L2, no flush" % (cells * (3 if dims == 2 else 6) * 4 / 1e6)
+                   if cells * (3 if dims == 2 else 6) * 4 > 126e6 else
+                   "working set %.0f MB fits in L2: no flush (the metric is the steady-state rate)" %
+                   (cells * 6 * 4 / 1e6),
+                   "loop": "device-side loop in pre-instantiated CUDA graphs",
+                   "launch_shape": shape_desc},
+        "emitter_steps_per_s": emitter_rate,
+        "roofline": {"bound": "hbm", "kernel": kernel_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "traffic_source": traffic_src,
+                     "peak_source": peak_kind, "algorithmic_bytes_per_launch": alg_bytes},
+        "kernels": per, "plain_fp64": plain, "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": "Gcell-updates/s",
+                "h2d_bytes_per_step": 8 * (4 + len(deck["sources"]) + len(deck["plane_sources"])),
+                "d2h_bytes_per_step": 8 * (npts + 1) + 4,
+                "how": "one omx_run call per step (time/source table host->device from pinned memory; the "
+                       "step's side-stream work overlaps the next call's first pass) + "
+                       "omx_detectors_drain_async of the step's samples and error word (device->host, pinned "
+                       "slot) every step, collected into host arrays two steps later",
+                "per_call_sequence": {"value": e2e_calls, "unit": "Gcell-updates/s",
+                                      "how": "the reference's per-step call sequence through the C-ABI "
+                                             "(omx_step_H, omx_source_interactions, omx_step_E, "
+                                             "omx_qgroup_step, omx_detectors_record) + asynchronous drain "
+                                             "every step; omx_step_H is deferred into the fused pass of "
+                                             "omx_step_E"}},
+        "gpu_launches": launches, "clocks": clk,
+    }
 
+
+def gpu_arm(args, dist):
+    import omx
+
+    if dist.world > 1:
+        omx.select_device(dist.local_rank % max(1, omx.device_count()))
+    K, W = args.steps, max(3, args.warmup)
+    deck, _ = make_deck(args.config, args.grid)
+    err_steps = args.error_steps or deck["steps"]
+    r = measure(args, dist, args.config, args.grid, K, W, err_steps, args.cpu_seconds)
+    others = {}
+    if args.config == "cfg2" and not args.no_subrecords:
+        # the 3D configurations on the same box, same clock rules: the plain 3D scene at full
+        # size and length, the 512^3 dimer scene with its FP32 error over a stated prefix
+        others["cfg1"] = measure(args, dist, "cfg1", None, max(K, 200), W, 4000, args.sub_cpu_seconds)
+        others["cfg3"] = measure(args, dist, "cfg3", None, K, W, args.cfg3_error_steps, args.sub_cpu_seconds)
     if dist.rank == 0:
-        line = {
-            "metric": METRIC, "value": value, "unit": "Gcell-updates/s", "n_gpus": dist.world, "steps": K,
-            "warmup": W, "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded deck of the configuration's shape)",
-            "config": {"workload": desc, "cells": cells, "emitters": ne, "precision": "fp32 fields, fp64 emitters",
-                       "parallelism": f"replicas x{dist.world}" if dist.world > 1 else "single GPU",
-                       "l2": "working set %.0f MB > 126 MB L2, no flush" % (cells * 3 * 4 / 1e6),
-                       "loop": "device-side loop captured in a CUDA graph, one graph launch per step",
-                       "launch_shape": ("fused-kernel form %d" % shape if deck["dimensions"] == 2 else
-                                        "planes marched per thread %d" % shape) +
-                                       (" (library default)" if args.no_autotune else " (omx_autotune)")},
-            "emitter_steps_per_s": emitter_rate,
-            "roofline": {"bound": "hbm", "kernel": kernel_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": traffic, "traffic_source": traffic_src,
-                         "peak_source": peak_kind, "algorithmic_bytes_per_launch": alg_bytes},
-            "kernels": per,
-            "plain_fp64": plain,
-            "cpu_baseline": cpu,
-            "e2e": {"value": e2e_value, "unit": "Gcell-updates/s",
-                    "h2d_bytes_per_step": 8 * (4 + len(deck["sources"]) + len(deck["plane_sources"])),
-                    "d2h_bytes_per_step": 8 * (npts + 1) + 4,
-                    "how": "one omx_run call per step (time/source table host->device from pinned memory; the "
-                           "step's side-stream work overlaps the next call's fused pass) + "
-                           "omx_detectors_drain_async of the step's samples and error word (device->host, pinned "
-                           "slot) every step, collected into host arrays two steps later",
-                    "per_call_sequence": {"value": e2e_calls, "unit": "Gcell-updates/s",
-                                          "how": "the reference's per-step call sequence through the C-ABI "
-                                                 "(omx_step_H, omx_source_interactions, omx_step_E, "
-                                                 "omx_qgroup_step, omx_detectors_record) + asynchronous drain "
-                                                 "every step; omx_step_H is deferred into the fused pass of "
-                                                 "omx_step_E"}},
-            "gpu_launches": launches,
-            "clocks": clk,
-        }
+        line = {"metric": METRIC, "value": r["value"], "unit": "Gcell-updates/s", "n_gpus": dist.world, "steps": K,
+                "warmup": W, "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded deck of the configuration's shape)"}
+        for k in ("config", "emitter_steps_per_s", "roofline", "kernels", "plain_fp64", "cpu_baseline", "e2e",
+                  "gpu_launches", "clocks"):
+            line[k] = r[k]
+        if others:
+            line["other_configs"] = others
         print(json.dumps(line), flush=True)
 
 
@@ -588,8 +621,9 @@ def gpu_arm_cfg5(args, dist):
     # ---- batched: one persistent launch per pass over all grids, the step in a CUDA graph
     grids = [build_gpu(d, "fp32")[0] for d in dks]
     batch = omx.Batch(grids)
-    kch = batch.autotune(reps=3)
+    shape = batch.autotune(reps=3)
     batch.run(1, W, 1, tdp, use_graph=True)
+    batch.prepare_run(1 + W, K, 1, tdp)         # tables and step graphs built outside the clock
     batch.synchronize()
     dist.barrier()
     clocks = ClockSampler(dist.local_rank)
@@ -603,17 +637,17 @@ def gpu_arm_cfg5(args, dist):
     clk = clocks.stop()
     t_batch = dist.max(t_batch)
     traces_b = [g.drain_detectors()[1] for g in grids]
-    alg = sum(g.algorithmic_bytes(omx.KC_H) + g.algorithmic_bytes(omx.KC_E) for g in grids)
+    alg = sum(g.algorithmic_bytes(omx.KC_H) + g.algorithmic_bytes(omx.KC_E) for g in grids)   # per step
     batch.kill()
     for g in grids:
         g.kill()
-    # ---- the same grids one at a time (each its own omx_run, CUDA graph per grid) with the
-    # batch's arithmetic (traces compared bit for bit)
+    # ---- the same grids one at a time (each its own omx_run, CUDA graphs per grid, the graphs
+    # captured before the clock) with the batch's arithmetic (traces compared bit for bit)
     t_solo, same = 0.0, True
     for d, tb in zip(dks, traces_b):
         g = build_gpu(d, "fp32")[0]
-        g.set_step_form(omx.STEP_TWO_PASS)
         g.run(1, W, 1, tdp, use_graph=True)
+        g.prepare_run(1 + W, K, 1, tdp)
         g.synchronize()
         t0 = time.perf_counter()
         g.run(1 + W, K, 1, tdp, use_graph=True)
@@ -650,15 +684,17 @@ def gpu_arm_cfg5(args, dist):
                        "cells": cells, "sides": sides, "precision": "fp32",
                        "parallelism": f"replicas x{dist.world}" if dist.world > 1 else "single GPU",
                        "l2": "working set %.1f GB > 126 MB L2, no flush" % (cells * 6 * 4 / 1e9),
-                       "loop": "omx_batch_run: one persistent launch per pass over all grids' tiles, the step "
-                               "captured in a CUDA graph; tile depth %d from omx_batch_autotune" % kch,
+                       "loop": "omx_batch_run: one k_fused3_batch launch per step over every grid's tiles "
+                               "(largest grid first), the steps captured in CUDA graphs; tile %s from "
+                               "omx_batch_autotune" % ("32 x %d, %d planes per block" % (shape // 1000, shape % 1000)
+                                                       if shape >= 1000 else "depth %d" % shape),
                        "timing": "wall clock around omx_batch_run + omx_batch_synchronize"},
             "one_at_a_time": {"value": solo_value, "unit": "Gcell-updates/s",
                               "how": "the same grids, each its own omx_run (CUDA graph), run one after another",
                               "batch_speedup": value / solo_value,
                               "detector_traces_bit_identical": same,
-                              "arithmetic": "two half-step passes per grid, as the batch"},
-            "roofline": {"bound": "hbm", "kernel": "k_batch3 (H and bulk E passes over all grids)",
+                              "arithmetic": "one fused pass per grid and step, as the batch"},
+            "roofline": {"bound": "hbm", "kernel": "k_fused3_batch (the fused pass of every grid in one launch)",
                          "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": None, "peak_source": peak_kind,
                          "algorithmic_bytes_per_step": alg,

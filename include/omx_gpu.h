@@ -297,11 +297,12 @@ int omx_run_prepare(omx_ctx *ctx, int tt0, int nsteps, int n_skip_steps, int t_d
 
 /* Kernel form of the FP32 time step (no counterpart in the reference).  Every form meets the same
  * FP32 bar; they differ in rounding, and the form may be changed between steps.
- *   OMX_STEP_DEFAULT      2D TMz: one fused pass per step; 3D: the two half-step passes
+ *   OMX_STEP_DEFAULT      one fused pass per step where eligible (2D TMz; 3D with x and y not
+ *                         periodic: the planes staged by TMA, the dispersive cells and a single
+ *                         plane source inside the pass), else the two half-step passes
  *   OMX_STEP_TWO_PASS     the two half-step passes everywhere: the arithmetic of batched runs
  *                         (omx_batch_create sets it on its members)
- *   OMX_STEP_SINGLE_PASS  one fused pass per step where eligible (3D: k_fused3, nx % 32 == 0,
- *                         ny % 8 == 0; measured slower than the two passes on GB300) */
+ *   OMX_STEP_SINGLE_PASS  the same as OMX_STEP_DEFAULT */
 #define OMX_STEP_DEFAULT 0
 #define OMX_STEP_TWO_PASS 1
 #define OMX_STEP_SINGLE_PASS 2
@@ -312,13 +313,17 @@ int omx_set_step_form(omx_ctx *ctx, int form);
  * the fused FP32 TMz kernel's form (0 register prefetch, 4/5/6/8 bulk-copy ring depth, 14/15/16
  * ring depth 4/5/6 filled by a dedicated copy warp, 24/25 the same with depth 4/5 and two 4-cell
  * chunks per thread, 34/36 register tiles of 4/6 rows, 44/45 depth 4/5 with eight compute warps
- * per block -- 44 is the default) or the
- * planes / rows each thread marches in the unfused kernels.  The candidates run on the initial
+ * per block -- 44 is the default), the fused FP32 3D pass's tile (rows x 1000 + planes per block:
+ * rows 8 or 16; 8064 is the default) or the planes / rows each thread marches in the unfused
+ * kernels.  The candidates run on the initial
  * all-zero fields, which every kernel maps to zero, so the simulation state is unchanged: call it
  * after the grid is configured and before the first step or omx_write_field (OMX_ERR_STATE
  * otherwise); configuration calls are closed afterwards, as after a first step.  *choice (may
  * be NULL) receives the chosen shape. */
 int omx_autotune(omx_ctx *ctx, int reps, int *choice);
+/* Sets the launch shape directly (a value omx_autotune reported, e.g. for a grid of the same shape
+ * tuned earlier); no counterpart in the reference.  Every shape gives the same results bit for bit. */
+int omx_set_launch_shape(omx_ctx *ctx, int shape);
 
 /* ---- batched multi-grid runs (no counterpart in the reference: it runs one grid per process) -
  * A batch groups n configured 3D contexts of one precision on the current device (for example
@@ -337,6 +342,9 @@ int omx_batch_create(omx_ctx *const *ctxs, int n, omx_batch **out);
 int omx_batch_autotune(omx_batch *batch, int reps, int *choice);
 int omx_batch_run(omx_batch *batch, int tt0, int nsteps, int n_skip_steps, int t_det_print,
                   int use_graph);
+/* No counterpart in the reference: builds the batch's tables and captures the step graphs that
+ * omx_batch_run(batch, tt0, nsteps, ..., 1) launches, without running a step. */
+int omx_batch_run_prepare(omx_batch *batch, int tt0, int nsteps, int n_skip_steps, int t_det_print);
 long long omx_batch_launch_count(const omx_batch *batch);   /* kernels launched by the batch */
 /* omx_batch_run returns once the work is queued; this waits for it (and reports kernel errors). */
 int omx_batch_synchronize(omx_batch *batch);

@@ -250,6 +250,7 @@ struct omx_ctx {
     long long next_ticket = 0;
     DevBuf<float> rowc;    // packed per-row y coefficients of the fused FP32 TMz kernel
     DevBuf<int> d_err;     // kernel error word (bit 0: a bulk-copy wait of the fused kernel ran out)
+    DevBuf<int> d_done;    // finished blocks of the fused 3D pass in the device loop (zero between launches)
     int *h_err = nullptr;  // pinned host copy of it, read at every synchronisation
     // pinned staging of the per-step table, two halves used alternately (an event per half
     // marks when its last copy has been consumed)
@@ -286,6 +287,9 @@ struct omx_ctx {
     bool fused_dirty = true;    // media or sources changed since the last eligibility check
     bool post_ok = false;       // the work after the fused pass goes in one launch (post_eligible)
     bool plane_fold = false;    // the 3D bulk E pass adds the plane source (plane_fold_eligible)
+    bool fold3 = false;         // the fused 3D pass adds the single plane source (fold3_of)
+    F3tMaps f3maps[2][2];       // tensor maps of the fused 3D pass: [in set][tile rows 8 / 16]
+    const void *f3key[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};   // Ex buffer they were made for
     int step_form = OMX_STEP_DEFAULT;   // omx_set_step_form; a batch sets TWO_PASS on its members
     int *run_step = nullptr;    // device step counter while omx_run issues a step sequence
     std::string err;
@@ -553,6 +557,7 @@ template <class R> GridArgs<R> grid_args(omx_ctx *c)
     G.ade_ent = c->ade_ent.p;
     G.ade_b = c->ade_b.p;
     G.step_inc = c->run_step;
+    G.step_done = c->d_done.p;
     G.march = c->march;
     return G;
 }
@@ -886,30 +891,36 @@ DetArgs det_args(omx_ctx *c)
     return D;
 }
 
-// The FP32 fused TMz step applies dispersive cells and sources after the bulk pass; that
-// commutes with the reference's order only outside the CPML slabs and away from sources.
-// The FP32 fused passes (2D TMz: k_fused_tmz_*, 3D: k_fused3) apply dispersive cells, sources
-// and the emitter current after the bulk update, which needs no dispersive cell in a CPML slab
-// (its psi term would be lost) and no source point in a dispersive cell.
+// The FP32 fused TMz pass (k_fused_tmz_*) applies the dispersive cells, the sources and the
+// emitter current after the bulk update; that commutes with the reference's order only with no
+// dispersive cell in a CPML slab (its psi term would be lost) and no source point in a
+// dispersive cell.  The 3D pass (k_fused3_tma) updates the dispersive cells inside the pass,
+// before their CPML terms, as the reference does, and adds a single plane source to E_old before
+// the update (fold3); other sources follow the pass and must avoid dispersive cells.  x and y
+// must not be periodic (its staged halo holds the PEC ghosts there).
+bool fold3_of(const omx_ctx *c)
+{
+    return c->dims == 3 && c->sources.size() == 1 && c->sources[0]->kind == 1;
+}
+
 bool fused_eligible(const omx_ctx *c)
 {
     if (!c->fp32 || c->step_form == OMX_STEP_TWO_PASS) return false;
-    if (c->dims == 3 && c->step_form != OMX_STEP_SINGLE_PASS) return false;
     if (c->dims == 2) {
         if (c->desc.mode != OMX_TMZ_2D_MODE || c->n[0] % 4 != 0) return false;
+        const int npml = c->desc.npml;
+        for (const int4 &e : c->ade_host) {
+            for (int a = 0; a < c->dims; ++a) {
+                const int p = a == 0 ? e.x : (a == 1 ? e.y : e.z);
+                if (c->cpml_axis[a] && (p <= npml || p >= c->n[a] + 1 - npml)) return false;
+            }
+        }
     } else if (c->dims == 3) {
-        if (c->n[0] % 32 != 0 || c->n[1] % F3_BY != 0) return false;
+        if (c->per[0] || c->per[1]) return false;
     } else {
         return false;
     }
-    const int npml = c->desc.npml;
-    for (const int4 &e : c->ade_host) {
-        for (int a = 0; a < c->dims; ++a) {
-            const int p = a == 0 ? e.x : (a == 1 ? e.y : e.z);
-            if (c->cpml_axis[a] && (p <= npml || p >= c->n[a] + 1 - npml)) return false;
-        }
-    }
-    if (!c->ade_host.empty()) {
+    if (!c->ade_host.empty() && !fold3_of(c)) {
         const bool d3 = c->dims == 3;
         std::unordered_map<long long, int> disp;
         for (const int4 &e : c->ade_host) disp[cell_key(c, e.x, e.y, d3 ? e.z : 0) * 4 + e.w] = 1;
@@ -935,7 +946,7 @@ bool fused_eligible(const omx_ctx *c)
 bool post_eligible(const omx_ctx *c)
 {
     if (!c->fused_ok || c->sources.size() > 1) return false;
-    if (c->sources.empty()) return true;
+    if (c->sources.empty() || fold3_of(c)) return true;
     const SourceRec &S = *c->sources[0];
     if (S.kind != 1) return false;
     const int ax = S.pd.plane_axis - 1, comp = S.pd.comp - 1;
@@ -974,6 +985,7 @@ void prepare(omx_ctx *c)
     if (recheck) {
         c->post_ok = post_eligible(c);
         c->plane_fold = plane_fold_eligible(c);
+        c->fold3 = c->fused_ok && fold3_of(c);
     }
     if (c->fused_ok && !c->ff2[2].p) {
         for (int q = 0; q < 6; ++q)
@@ -1126,25 +1138,46 @@ template <class R> void do_sample(omx_ctx *c, StepParam slot, StepParam time)
     c->launches++;
 }
 
-// One FP32 fused TMz step: bulk H+E pass from the current buffer set into the other, then the
-// dispersive cells; the caller adds sources and the emitter current to the new set.
-template <class R> void fused_step(omx_ctx *c, bool ade = true);
-template <> void fused_step<double>(omx_ctx *, bool) {}
-template <> void fused_step<float>(omx_ctx *c, bool ade)
+// One FP32 fused step: the H+E pass from the current buffer set into the other.  2D TMz: then
+// the dispersive cells (ade); 3D: the dispersive cells are inside the pass, and so is the single
+// plane source when fold3 holds (`plane`: its amplitude).  The caller adds the other sources and
+// the emitter current to the new set.
+template <class R> void fused_step(omx_ctx *c, bool ade = true, const StepParam *plane = nullptr);
+template <> void fused_step<double>(omx_ctx *, bool, const StepParam *) {}
+template <> void fused_step<float>(omx_ctx *c, bool ade, const StepParam *plane)
 {
     ProfScope ps(c, KC_E);
     const int in = c->cur, out = 1 - c->cur;
     const FieldPtrs<float> Fin = field_ptrs<float>(c, in), Fout = field_ptrs<float>(c, out);
-    const GridArgs<float> G = grid_args<float>(c);
+    GridArgs<float> G = grid_args<float>(c);
     if (c->dims == 3) {
         Fused3Args A;
         A.in = Fin;
         A.out = Fout;
         for (int a = 0; a < 3; ++a)
             for (int q = 0; q < 2; ++q) A.psiH_out[a][q] = in == 0 ? c->psiH2[a][q].p : c->psif[a][1][q].p;
-        launch_fused3(A, G, c->march, c->stream);
-        if (ade) launch_ade_post(Fin, Fout, G, c->stream);
-        c->launches += 1 + (ade && c->ade_n > 0 ? 1 : 0);
+        if (c->fold3 && plane) {
+            const SourceRec &S = *c->sources[0];
+            G.pl_on = 1;
+            G.pl_comp = S.pd.comp - 1;
+            G.pl_axis = S.pd.plane_axis - 1;
+            G.pl_index = S.pd.plane_index;
+            G.pl_c_src = S.c_src;
+            G.pl_amp = *plane;
+            // in the device loop this pass advances the step counter when it ends, so it reads
+            // its step's row while the counter still holds the previous step
+            if (G.pl_amp.tab && G.step_inc) G.pl_amp.tab += G.pl_amp.stride;
+        }
+        if (G.step_inc && !c->d_done.p) throw Fail{OMX_ERR_STATE, "fused 3D pass: block counter missing"};
+        const int ty = f3t_rows(c->fused_form);
+        const int t = ty == 16 ? 1 : 0;
+        if (c->f3key[in][t] != Fin.f[0]) {
+            if (!encode_f3t_maps(&c->f3maps[in][t], Fin, c->L, ty))
+                throw Fail{OMX_ERR_CUDA, "cuTensorMapEncodeTiled failed for the fused 3D pass"};
+            c->f3key[in][t] = Fin.f[0];
+        }
+        ck(launch_fused3t(c->f3maps[in][t], A, G, c->fused_form, c->march, c->d_err.p, c->stream), "fused 3D launch");
+        c->launches += 1;
         c->cur = out;
         return;
     }
@@ -1179,8 +1212,8 @@ template <> void do_post<float>(omx_ctx *c, StepParam amp, StepParam time, StepP
     const FieldPtrs<float> Fin = field_ptrs<float>(c, 1 - c->cur), Fout = field_ptrs<float>(c, c->cur);
     const GridArgs<float> G = grid_args<float>(c);
     PostArgs Q{};
-    Q.nb_ade = (c->ade_n + 127) / 128;
-    if (!c->sources.empty()) {
+    Q.nb_ade = c->dims == 3 ? 0 : (c->ade_n + 127) / 128;   // the 3D pass updates them itself
+    if (!c->sources.empty() && !c->fold3) {
         const SourceRec &S = *c->sources[0];
         Q.P.comp = S.pd.comp - 1;
         Q.P.axis = S.pd.plane_axis - 1;
@@ -1422,7 +1455,7 @@ template <class R> void run_impl(omx_ctx *c, int tt0, int nsteps, int n_skip, in
         for (int q = 0; q < nsrc; ++q) amps.push_back(imm(row[4 + q]));
         if (fused) {
             const bool post = c->post_ok;
-            fused_step<R>(c, !post);
+            fused_step<R>(c, !post, c->fold3 ? &amps[0] : nullptr);
             join_side_kernels(c);
             if (post) {
                 do_post<R>(c, nsrc ? amps[0] : imm(0.0), imm(row[0]), imm(row[1]));
@@ -1462,9 +1495,10 @@ template <class R> void run_impl(omx_ctx *c, int tt0, int nsteps, int n_skip, in
         if (has_det) do_sample<R>(c, P(3), P(0));
     };
     const bool post = fused && c->post_ok;
+    const StepParam *pl3 = (fused && c->fold3) ? &amps[0] : nullptr;   // the plane source inside the 3D pass
     auto one_step = [&]() {
         if (post) {
-            fused_step<R>(c, false);
+            fused_step<R>(c, false, pl3);
             do_post<R>(c, nsrc ? amps[0] : imm(0.0), P(0), P(1));
         } else if (fused) {
             fused_step<R>(c);
@@ -1488,7 +1522,7 @@ template <class R> void run_impl(omx_ctx *c, int tt0, int nsteps, int n_skip, in
     // Same operations on the same values as one_step: results are identical.
     auto overlapped_step = [&](bool wait_prev) {
         if (post) {
-            fused_step<R>(c, false);
+            fused_step<R>(c, false, pl3);
             if (wait_prev) ck(cudaStreamWaitEvent(c->stream, c->ev_join, 0), "wait");
             do_post<R>(c, nsrc ? amps[0] : imm(0.0), P(0), P(1));
         } else {
@@ -1581,10 +1615,12 @@ template <class R> void run_impl(omx_ctx *c, int tt0, int nsteps, int n_skip, in
         if (times > 0) c->cur = hit->cur_after;
     };
     // the fused path alternates buffer sets, so its graphs cover an even number of steps; long
-    // graphs keep the side stream's work overlapped across all but one step boundary per graph
-    const int per_graph = (fused || split) ? (nsteps >= 16 ? 16 : (fused ? 2 : 1)) : 1;
+    // graphs keep the side stream's work overlapped across all but one step boundary per graph.
+    // A run of up to 64 steps is one graph (an odd fused run: one graph of the even part and a
+    // one-step graph), a longer run repeats a 16-step graph.
+    const int per_graph = (fused || split) ? (nsteps > 64 ? 16 : (fused ? (nsteps & ~1) : nsteps)) : 1;
     if (use_graph && !c->prof) {
-        const int ngraph = nsteps / per_graph;
+        const int ngraph = per_graph > 0 ? nsteps / per_graph : 0;
         const int k = prepare_only ? 0 : 1;
         if (ngraph > 0) launch_graph(per_graph, k * ngraph);
         int left = nsteps - ngraph * per_graph;
@@ -1597,6 +1633,21 @@ template <class R> void run_impl(omx_ctx *c, int tt0, int nsteps, int n_skip, in
     if (!prepare_only) c->rec_count += nrec;
 }
 
+// A launch shape as omx_autotune reports it: fused 3D pass: tile rows x 1000 + planes per block;
+// fused TMz pass: the kernel form; unfused kernels: planes (3D) or rows (2D) per thread.
+void apply_shape(omx_ctx *c, int v)
+{
+    const bool fused = c->fp32 && fused_eligible(c);
+    if (v >= 1000) {
+        c->fused_form = v / 1000;
+        c->march = v % 1000;
+    } else if (fused) {
+        c->fused_form = v;
+    } else {
+        c->march = v;
+    }
+}
+
 // Time each candidate launch shape on the device and keep the fastest.  Runs on fields that are
 // still all zero: every kernel maps zero fields, zero psi and zero ADE state to zero, so the
 // candidates leave no trace in the simulation state.
@@ -1604,15 +1655,21 @@ template <class R> int autotune_impl(omx_ctx *c, int reps)
 {
     const bool fused = std::is_same<R, float>::value && c->fused_ok;
     std::vector<int> cand;
-    if (fused && c->dims == 3) cand = {8, 16, 32};
-    else if (fused) cand = {0, 4, 5, 6, 8, 14, 15, 16, 24, 25, 34, 36, 44, 45};
-    else if (c->dims == 3) cand = {4, 8, 16, 32};
-    else if (c->dims == 2) cand = {8, 16, 32, 64};
-    else return 0;
-    auto select = [&](int v) {
-        if (fused && c->dims == 2) c->fused_form = v;
-        else c->march = v;
-    };
+    if (fused && c->dims == 3) {
+        // fused 3D pass: tile rows x 1000 + planes per block
+        for (int ty : {8, 16})
+            for (int kch : {16, 32, 64, 128})
+                if (kch <= c->n[2] * 2) cand.push_back(ty * 1000 + kch);
+    } else if (fused) {
+        cand = {0, 4, 5, 6, 8, 14, 15, 16, 24, 25, 34, 36, 44, 45};
+    } else if (c->dims == 3) {
+        cand = {4, 8, 16, 32};
+    } else if (c->dims == 2) {
+        cand = {8, 16, 32, 64};
+    } else {
+        return 0;
+    }
+    auto select = [&](int v) { apply_shape(c, v); };
     auto once = [&]() {
         if (fused) {
             fused_step<R>(c);
@@ -1647,8 +1704,7 @@ template <class R> int autotune_impl(omx_ctx *c, int reps)
             bt = best[k];
             pick = cand[k];
         }
-    if (fused && c->dims == 2) c->fused_form = pick;
-    else c->march = pick;
+    select(pick);
     ck(cudaPeekAtLastError(), "autotune");
     return pick;
 }
@@ -1822,6 +1878,7 @@ int omx_create(const omx_grid_desc *d, omx_ctx **out)
         else build_media<double>(c, nullptr, noeps);
         c->jbuf.alloc(9);
         c->d_err.alloc(1);
+        c->d_done.alloc(1);
         ck(cudaMallocHost(&c->h_err, sizeof(int)), "pinned error word");
         *c->h_err = 0;
         ck(cudaEventCreate(&c->t0), "event");
@@ -2075,7 +2132,14 @@ int omx_step_E(omx_ctx *c, double time, double t_skip)
         // them and the emitter current: the order of omx_run's fused step.  The pass reads one
         // buffer set and writes the other, so it goes before the wait for the side kernels.
         c->h_pending = false;
-        fused_step<float>(c);
+        if (c->fold3) {
+            // the single plane source goes inside the 3D pass (when it was requested)
+            const StepParam amp = imm(c->src_pending ? source_amp(*c->sources[0], c->src_time) : 0.0);
+            fused_step<float>(c, true, &amp);
+            c->src_pending = false;
+        } else {
+            fused_step<float>(c);
+        }
         join_side_kernels(c);
         if (c->src_pending) {
             c->src_pending = false;
@@ -2779,6 +2843,20 @@ int omx_set_step_form(omx_ctx *c, int form)
     OMX_API_END(c)
 }
 
+int omx_set_launch_shape(omx_ctx *c, int shape)
+{
+    OMX_API_BEGIN
+    join_side(c);
+    req(c && shape >= 1, "bad argument");
+    if (c->dims == 3 && c->fp32 && fused_eligible(c))
+        req((shape / 1000 == 8 || shape / 1000 == 16) && shape % 1000 >= 1, "fused 3D shape: (8 | 16) * 1000 + planes");
+    else
+        req(shape < 1000, "fused 3D shape for a grid that steps with two passes");
+    apply_shape(c, shape);
+    c->epoch++;
+    OMX_API_END(c)
+}
+
 int omx_autotune(omx_ctx *c, int reps, int *choice)
 {
     OMX_API_BEGIN
@@ -2799,22 +2877,6 @@ int omx_autotune(omx_ctx *c, int reps, int *choice)
 }  // extern "C"
 
 // ---- batched multi-grid runs ------------------------------------------------------------------
-struct omx_batch {
-    std::vector<omx_ctx *> ctx;
-    bool fp32 = false;
-    cudaStream_t stream = nullptr;
-    int kch = 0;            // z planes per tile of the batched passes (0 = the default)
-    int blocks = 0;         // persistent grid of the batched passes
-    int own_launch_tiles_per_sm = 8;   // grids with at least this many tiles per SM launch alone (0: none)
-    long long launches = 0;
-    DevBuf<unsigned char> dgrid, dsrc, ddet;
-    cudaEvent_t done = nullptr;   // recorded after a batched call; member streams wait on it
-};
-
-namespace {
-
-constexpr int BATCH_DEFAULT_KCH = 16;
-
 // Device tables of one batched run: the grids' tile list, the radial sources in rounds (round r
 // holds source r of every grid, so one grid's sources keep their order) and the detectors.
 template <class R> struct BatchTables {
@@ -2830,14 +2892,73 @@ template <class R> struct BatchTables {
     const BatchDet<R> *dets = nullptr;
     int ndet = 0;
     long long det_pts = 0;
+    // fused path: the grids of the batched pass (largest first) and its blocks
+    const F3tBatchGrid *f3 = nullptr;
+    long long f3_blocks = 0;
 };
+
+struct omx_batch {
+    std::vector<omx_ctx *> ctx;
+    bool fp32 = false;
+    cudaStream_t stream = nullptr;
+    int kch = 0;            // z planes per tile of the batched passes (0 = the default)
+    int blocks = 0;         // persistent grid of the batched passes
+    int own_launch_tiles_per_sm = 8;   // grids with at least this many tiles per SM launch alone (0: none)
+    long long launches = 0;
+    // device tables, one per step parity (the fused path alternates the members' buffer sets)
+    DevBuf<unsigned char> dgrid[2], dsrc[2], ddet[2], df3[2];
+    cudaEvent_t done = nullptr;   // recorded after a batched call; member streams wait on it
+    // 1: every member steps with one fused pass and the batch runs them in one k_fused3_batch
+    // launch per step; 0: the two half-step passes (k_batch3); -1: not decided yet
+    int fused = -1;
+    int f3form = 8, f3kch = 64;   // tile rows and planes per block of the fused batched pass
+    // tables and captured step graphs, kept while the key (each member's configuration epoch,
+    // buffer set, step table and the launch shapes) is unchanged
+    std::vector<long long> key;
+    BatchTables<float> Tf[2];
+    BatchTables<double> Td[2];
+    struct Graph {
+        int steps;
+        long long per;
+        cudaGraphExec_t exec;
+    };
+    std::vector<Graph> graphs;
+    void drop_graphs()
+    {
+        for (auto &g : graphs) cudaGraphExecDestroy(g.exec);
+        graphs.clear();
+    }
+};
+template <class R> BatchTables<R> (&batch_cache(omx_batch *b))[2];
+template <> BatchTables<float> (&batch_cache<float>(omx_batch *b))[2] { return b->Tf; }
+template <> BatchTables<double> (&batch_cache<double>(omx_batch *b))[2] { return b->Td; }
+
+namespace {
+
+constexpr int BATCH_DEFAULT_KCH = 16;
 
 template <class T> size_t pad16(size_t n) { return (n * sizeof(T) + 15) / 16 * 16; }
 
+// Tables of one batched step.  Two-pass path: q = 0.  Fused path: the step of parity q, whose
+// pass reads each member's buffer set cur ^ q and whose sources and detectors work on the set the
+// pass writes.
 template <class R>
-BatchTables<R> batch_tables(omx_batch *b, const std::vector<RunPlan> *plans, int kch)
+BatchTables<R> batch_tables(omx_batch *b, const std::vector<RunPlan> *plans, int kch, int q = 0)
 {
     const int n = (int)b->ctx.size();
+    const bool f3 = b->fused == 1;
+    std::vector<int> cur0;
+    for (auto *c : b->ctx) cur0.push_back(c->cur);
+    struct RestoreCur {
+        omx_batch *b;
+        const std::vector<int> &cur0;
+        ~RestoreCur()
+        {
+            for (size_t i = 0; i < b->ctx.size(); ++i) b->ctx[i]->cur = cur0[i];
+        }
+    } restore{b, cur0};
+    if (f3)
+        for (int i = 0; i < n; ++i) b->ctx[i]->cur = cur0[i] ^ q ^ 1;
     BatchTables<R> T;
     std::vector<BatchGrid<R>> grids(n);
     long long t0 = 0;
@@ -2871,18 +2992,19 @@ BatchTables<R> batch_tables(omx_batch *b, const std::vector<RunPlan> *plans, int
         for (int i = 0; i < n; ++i) {
             omx_ctx *c = b->ctx[i];
             const RunPlan &P = (*plans)[i];
-            for (size_t q = 0; q < c->sources.size(); ++q) {
-                const SourceRec &S = *c->sources[q];
+            for (size_t r = 0; r < c->sources.size(); ++r) {
+                const SourceRec &S = *c->sources[r];
+                if (f3 && c->fold3) continue;          // the single plane source is inside the pass
                 if (S.kind != 0) {
-                    T.planes[q].push_back({i, (int)q});
+                    T.planes[r].push_back({i, (int)r});
                     continue;
                 }
                 BatchSrc<R> e;
                 std::memset(&e, 0, sizeof(e));
                 e.F = field_ptrs<R>(c);
                 e.S = src_args(S);
-                e.amp = plan_param(c, P, 4 + (int)q);
-                rs[q].push_back(e);
+                e.amp = plan_param(c, P, 4 + (int)r);
+                rs[r].push_back(e);
             }
             if (P.has_det) {
                 BatchDet<R> e;
@@ -2915,9 +3037,10 @@ BatchTables<R> batch_tables(omx_batch *b, const std::vector<RunPlan> *plans, int
     T.ndet = (int)dets.size();
     // one upload per table
     size_t gbytes = pad16<BatchGrid<R>>(n);
-    b->dgrid.alloc(gbytes, false);
-    ck(cudaMemcpyAsync(b->dgrid.p, grids.data(), sizeof(BatchGrid<R>) * n, cudaMemcpyHostToDevice, b->stream), "batch");
-    T.grids = reinterpret_cast<const BatchGrid<R> *>(b->dgrid.p);
+    b->dgrid[q].alloc(gbytes, false);
+    ck(cudaMemcpyAsync(b->dgrid[q].p, grids.data(), sizeof(BatchGrid<R>) * n, cudaMemcpyHostToDevice, b->stream),
+       "batch");
+    T.grids = reinterpret_cast<const BatchGrid<R> *>(b->dgrid[q].p);
     size_t sbytes = 0;
     std::vector<size_t> soff;
     for (auto &r : rs) {
@@ -2925,19 +3048,71 @@ BatchTables<R> batch_tables(omx_batch *b, const std::vector<RunPlan> *plans, int
         sbytes += pad16<BatchSrc<R>>(r.size());
     }
     if (sbytes) {
-        b->dsrc.alloc(sbytes, false);
-        for (size_t q = 0; q < rs.size(); ++q)
-            if (!rs[q].empty())
-                ck(cudaMemcpyAsync(b->dsrc.p + soff[q], rs[q].data(), sizeof(BatchSrc<R>) * rs[q].size(),
+        b->dsrc[q].alloc(sbytes, false);
+        for (size_t r = 0; r < rs.size(); ++r)
+            if (!rs[r].empty())
+                ck(cudaMemcpyAsync(b->dsrc[q].p + soff[r], rs[r].data(), sizeof(BatchSrc<R>) * rs[r].size(),
                                    cudaMemcpyHostToDevice, b->stream), "batch");
     }
-    for (size_t q = 0; q < rs.size(); ++q)
-        T.src.push_back(rs[q].empty() ? nullptr : reinterpret_cast<const BatchSrc<R> *>(b->dsrc.p + soff[q]));
+    for (size_t r = 0; r < rs.size(); ++r)
+        T.src.push_back(rs[r].empty() ? nullptr : reinterpret_cast<const BatchSrc<R> *>(b->dsrc[q].p + soff[r]));
     if (!dets.empty()) {
-        b->ddet.alloc(pad16<BatchDet<R>>(dets.size()), false);
-        ck(cudaMemcpyAsync(b->ddet.p, dets.data(), sizeof(BatchDet<R>) * dets.size(), cudaMemcpyHostToDevice,
+        b->ddet[q].alloc(pad16<BatchDet<R>>(dets.size()), false);
+        ck(cudaMemcpyAsync(b->ddet[q].p, dets.data(), sizeof(BatchDet<R>) * dets.size(), cudaMemcpyHostToDevice,
                            b->stream), "batch");
-        T.dets = reinterpret_cast<const BatchDet<R> *>(b->ddet.p);
+        T.dets = reinterpret_cast<const BatchDet<R> *>(b->ddet[q].p);
+    }
+    std::vector<F3tBatchGrid> f3g;
+    if constexpr (std::is_same<R, float>::value) {
+        if (f3) {
+            // the fused pass of every member in one launch, largest grid first
+            std::vector<int> order(n);
+            for (int i = 0; i < n; ++i) order[i] = i;
+            std::stable_sort(order.begin(), order.end(), [&](int a, int c) {
+                const omx_ctx *x = b->ctx[a], *y = b->ctx[c];
+                return (long long)x->n[0] * x->n[1] * x->n[2] > (long long)y->n[0] * y->n[1] * y->n[2];
+            });
+            const int TY = f3t_rows(b->f3form);
+            long long item = 0;
+            for (int i : order) {
+                omx_ctx *c = b->ctx[i];
+                const int in = cur0[i] ^ q;
+                c->cur = in;
+                F3tBatchGrid e;
+                std::memset(&e, 0, sizeof(e));
+                e.G = grid_args<float>(c);
+                e.A.in = field_ptrs<float>(c, in);
+                e.A.out = field_ptrs<float>(c, 1 - in);
+                for (int a = 0; a < 3; ++a)
+                    for (int k = 0; k < 2; ++k) e.A.psiH_out[a][k] = in == 0 ? c->psiH2[a][k].p : c->psif[a][1][k].p;
+                if (c->fold3 && plans) {
+                    const SourceRec &S = *c->sources[0];
+                    e.G.pl_on = 1;
+                    e.G.pl_comp = S.pd.comp - 1;
+                    e.G.pl_axis = S.pd.plane_axis - 1;
+                    e.G.pl_index = S.pd.plane_index;
+                    e.G.pl_c_src = S.c_src;
+                    e.G.pl_amp = plan_param(c, (*plans)[i], 4);
+                    // the pass advances the step counter when it ends: its reads are one row ahead
+                    if (e.G.step_inc) e.G.pl_amp.tab += e.G.pl_amp.stride;
+                }
+                if (!encode_f3t_maps(reinterpret_cast<F3tMaps *>(e.m), e.A.in, c->L, TY))
+                    throw Fail{OMX_ERR_CUDA, "cuTensorMapEncodeTiled failed for the batched fused pass"};
+                e.kch = b->f3kch;
+                e.tx = (c->L.nx + 31) / 32;
+                e.ty = (c->L.ny + TY - 1) / TY;
+                e.tz = (c->L.nz + e.kch - 1) / e.kch;
+                e.item0 = item;
+                item += (long long)e.tx * e.ty * e.tz;
+                f3g.push_back(e);
+            }
+            b->df3[q].alloc(sizeof(F3tBatchGrid) * f3g.size(), false);
+            ck(cudaMemcpyAsync(b->df3[q].p, f3g.data(), sizeof(F3tBatchGrid) * f3g.size(), cudaMemcpyHostToDevice,
+                               b->stream),
+               "batch");
+            T.f3 = reinterpret_cast<const F3tBatchGrid *>(b->df3[q].p);
+            T.f3_blocks = item;
+        }
     }
     // the host vectors die here: wait for the copies that read them
     ck(cudaStreamSynchronize(b->stream), "batch");
@@ -2978,6 +3153,37 @@ template <class R> long long batch_step(omx_batch *b, const BatchTables<R> &T, c
 {
     const int n = (int)b->ctx.size();
     long long k = 0;
+    if (b->fused == 1) {
+        // the fused pass of every member (dispersive cells and folded plane sources inside), then
+        // the work on the sets it wrote: the other sources, the emitter current and q-groups,
+        // the detectors
+        ck(launch_fused3t_batch(T.f3, n, T.f3_blocks, b->f3form, b->ctx[0]->d_err.p, b->stream), "batched fused pass");
+        ++k;
+        for (auto *c : b->ctx) c->cur ^= 1;
+        for (size_t r = 0; r < T.src.size(); ++r) {
+            if (T.nsrc[r] > 0) {
+                launch_src_batch<R>(T.src[r], T.nsrc[r], T.src_pts[r], b->stream);
+                ++k;
+            }
+            for (auto &gp : T.planes[r]) {
+                omx_ctx *c = b->ctx[gp.first];
+                launch_one_source<R>(c, (size_t)gp.second, plan_param(c, plans[gp.first], 4 + gp.second));
+                ++k;
+            }
+        }
+        for (int i = 0; i < n; ++i) {
+            omx_ctx *c = b->ctx[i];
+            const long long before = c->launches;
+            do_inject<R>(c, plan_param(c, plans[i], 0), plan_param(c, plans[i], 1));
+            for (auto &g : c->groups) do_group<R>(c, *g, plan_param(c, plans[i], 2));
+            k += c->launches - before;
+        }
+        if (T.ndet > 0) {
+            launch_sample_batch<R>(T.dets, T.ndet, T.det_pts, b->stream);
+            ++k;
+        }
+        return k;
+    }
     launch_batch3<R>(0, T.grids, n, T.tiles, kch, b->blocks, b->stream);
     ++k;
     for (int i = 0; i < n; ++i)
@@ -3026,42 +3232,84 @@ template <class R> long long batch_step(omx_batch *b, const BatchTables<R> &T, c
     return k;
 }
 
-template <class R> void batch_run_impl(omx_batch *b, int tt0, int nsteps, int n_skip, int t_det_print, int use_graph)
+// prepare_only: build the tables and capture the step graphs that the same call without it
+// launches, and run nothing (the members' stepping state and records are unchanged).
+template <class R> void batch_run_impl(omx_batch *b, int tt0, int nsteps, int n_skip, int t_det_print, int use_graph,
+                                       bool prepare_only = false)
 {
     BatchStreams streams(b);
     std::vector<RunPlan> plans;
-    for (auto *c : b->ctx) plans.push_back(stage_run(c, tt0, nsteps, n_skip, t_det_print));
+    for (auto *c : b->ctx) {
+        const double t_skip0 = c->t_skip;
+        const int tq_old0 = c->tq_step_old;
+        plans.push_back(stage_run(c, tt0, nsteps, n_skip, t_det_print, !prepare_only));
+        if (prepare_only) {
+            c->t_skip = t_skip0;
+            c->tq_step_old = tq_old0;
+            stage_reserve(c, plans.back());
+            c->run_step = c->d_step.p;   // as stage_upload leaves it: the tables hold the counter
+        }
+    }
     const int kch = b->kch > 0 ? b->kch : BATCH_DEFAULT_KCH;
     if (b->blocks == 0) b->blocks = batch3_blocks<R>();
-    const BatchTables<R> T = batch_tables<R>(b, &plans, kch);
+    // the fused path alternates the members' buffer sets: step s of this call uses T[s & 1]
+    const bool f3 = b->fused == 1;
+    std::vector<long long> key = {b->fused, kch, b->f3form, b->f3kch, b->blocks};
+    for (size_t i = 0; i < b->ctx.size(); ++i) {
+        const omx_ctx *c = b->ctx[i];
+        key.insert(key.end(), {(long long)c->epoch, c->cur, (long long)(uintptr_t)c->tab.p, plans[i].W,
+                               plans[i].has_det ? 1 : 0});
+    }
+    BatchTables<R>(&T)[2] = batch_cache<R>(b);
+    if (key != b->key) {
+        b->drop_graphs();
+        b->key.clear();
+        T[0] = batch_tables<R>(b, &plans, kch, 0);
+        T[1] = f3 ? batch_tables<R>(b, &plans, kch, 1) : BatchTables<R>();
+        b->key = key;
+    }
     if (use_graph) {
         // graphs of up to 8 steps (the step counters advance on the device, so every replay
-        // runs the next steps); the remainder in one shorter graph
+        // runs the next steps; on the fused path a replayed graph covers an even number of
+        // steps, so it starts from the same buffer sets); the remainder in one shorter graph.
+        // A graph of an odd number of fused steps leaves the members on the other buffer sets,
+        // which changes the key: it is never replayed from the wrong sets.
         auto run_graph = [&](int steps, int times) {
-            cudaGraph_t graph;
-            ck(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "capture");
-            long long per = 0;
-            for (int q = 0; q < steps; ++q) per += batch_step<R>(b, T, plans, kch);
-            ck(cudaStreamEndCapture(b->stream, &graph), "end capture");
-            cudaGraphExec_t exec = nullptr;
-            const cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
-            cudaGraphDestroy(graph);
-            ck(e, "instantiate");
-            struct Destroy {
-                cudaGraphExec_t x;
-                ~Destroy() { cudaGraphExecDestroy(x); }
-            } destroy{exec};
-            for (int s = 0; s < times; ++s) ck(cudaGraphLaunch(exec, b->stream), "graph launch");
-            b->launches += per * times;   // (an executable graph destroyed in flight is freed on completion)
+            omx_batch::Graph *hit = nullptr;
+            for (auto &g : b->graphs)
+                if (g.steps == steps) hit = &g;
+            if (!hit) {
+                std::vector<int> cur0;
+                for (auto *c : b->ctx) cur0.push_back(c->cur);
+                cudaGraph_t graph;
+                ck(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "capture");
+                long long per = 0;
+                for (int q = 0; q < steps; ++q) per += batch_step<R>(b, T[f3 ? (q & 1) : 0], plans, kch);
+                ck(cudaStreamEndCapture(b->stream, &graph), "end capture");
+                for (size_t i = 0; i < b->ctx.size(); ++i) b->ctx[i]->cur = cur0[i];
+                cudaGraphExec_t exec = nullptr;
+                const cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+                cudaGraphDestroy(graph);
+                ck(e, "instantiate");
+                b->graphs.push_back({steps, per, exec});
+                hit = &b->graphs.back();
+            }
+            for (int s = 0; s < times; ++s) ck(cudaGraphLaunch(hit->exec, b->stream), "graph launch");
+            b->launches += hit->per * times;
+            if (f3 && (steps * times) % 2)
+                for (auto *c : b->ctx) c->cur ^= 1;
         };
-        const int per_graph = std::min(nsteps, 8);
-        if (per_graph > 0) run_graph(per_graph, nsteps / per_graph);
-        if (per_graph > 0 && nsteps % per_graph) run_graph(nsteps % per_graph, 1);
-    } else {
-        for (int s = 0; s < nsteps; ++s) b->launches += batch_step<R>(b, T, plans, kch);
+        const int per_graph = f3 ? std::min(nsteps & ~1, 8) : std::min(nsteps, 8);
+        const int k = prepare_only ? 0 : 1;
+        if (per_graph > 0) run_graph(per_graph, k * (nsteps / per_graph));
+        const int left = per_graph > 0 ? nsteps % per_graph : nsteps;
+        if (left) run_graph(left, k);
+    } else if (!prepare_only) {
+        for (int s = 0; s < nsteps; ++s) b->launches += batch_step<R>(b, T[f3 ? (s & 1) : 0], plans, kch);
     }
     ck(cudaPeekAtLastError(), "launch");
-    for (size_t i = 0; i < b->ctx.size(); ++i) b->ctx[i]->rec_count += plans[i].nrec;
+    if (!prepare_only)
+        for (size_t i = 0; i < b->ctx.size(); ++i) b->ctx[i]->rec_count += plans[i].nrec;
 }
 
 // Tile depth of the batched passes, timed on the zero initial fields (which every pass maps to
@@ -3071,6 +3319,42 @@ template <class R> int batch_autotune_impl(omx_batch *b, int reps)
     BatchStreams streams(b);
     if (b->blocks == 0) b->blocks = batch3_blocks<R>();
     const int n = (int)b->ctx.size();
+    if (b->fused == 1) {
+        // fused batched pass: tile rows x 1000 + planes per block, each candidate timed over
+        // `reps` launches on the zero initial fields (the pass maps them to zero)
+        cudaEvent_t e0, e1;
+        ck(cudaEventCreate(&e0), "event");
+        ck(cudaEventCreate(&e1), "event");
+        float best = 0.f;
+        int pick = 8064;
+        bool first = true;
+        for (int ty : {8, 16})
+            for (int kch : {16, 32, 64, 128}) {
+                b->f3form = ty;
+                b->f3kch = kch;
+                const BatchTables<R> T = batch_tables<R>(b, nullptr, kch, 0);
+                auto once = [&]() {
+                    ck(launch_fused3t_batch(T.f3, n, T.f3_blocks, ty, b->ctx[0]->d_err.p, b->stream), "autotune");
+                };
+                once();
+                ck(cudaEventRecord(e0, b->stream), "event");
+                for (int r = 0; r < reps; ++r) once();
+                ck(cudaEventRecord(e1, b->stream), "event");
+                ck(cudaEventSynchronize(e1), "batch autotune");
+                float ms = 0.f;
+                ck(cudaEventElapsedTime(&ms, e0, e1), "batch autotune");
+                if (first || ms < best) {
+                    best = ms;
+                    pick = ty * 1000 + kch;
+                    first = false;
+                }
+            }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        b->f3form = pick / 1000;
+        b->f3kch = pick % 1000;
+        return pick;
+    }
     cudaEvent_t e0, e1;
     ck(cudaEventCreate(&e0), "event");
     ck(cudaEventCreate(&e1), "event");
@@ -3108,6 +3392,24 @@ template <class R> int batch_autotune_impl(omx_batch *b, int reps)
     return pick;
 }
 
+// The batch's arithmetic, fixed at its first autotune or run: when every member steps with one
+// fused FP32 pass, one k_fused3_batch launch per step; otherwise the two half-step passes
+// (k_batch3), which every member then keeps when used on its own.
+void batch_decide(omx_batch *b)
+{
+    if (b->fused >= 0) return;
+    bool all = b->fp32;
+    for (auto *c : b->ctx) all = all && fused_eligible(c);
+    b->fused = all ? 1 : 0;
+    if (!all)
+        for (auto *c : b->ctx) {
+            c->step_form = OMX_STEP_TWO_PASS;
+            c->fused_dirty = true;
+            c->fused_ok = false;
+            c->epoch++;
+        }
+}
+
 }  // namespace
 
 extern "C" {
@@ -3127,14 +3429,7 @@ int omx_batch_create(omx_ctx *const *ctxs, int n, omx_batch **out)
         for (int k = 0; k < i; ++k) req(ctxs[k] != c, "a context appears twice in the batch");
         b->ctx.push_back(c);
     }
-    // the batched passes are the two unfused half steps of every grid; a member used on its own
-    // afterwards keeps that arithmetic
-    for (auto *c : b->ctx) {
-        join_side(c);
-        c->step_form = OMX_STEP_TWO_PASS;
-        c->fused_dirty = true;
-        c->fused_ok = false;
-    }
+    for (auto *c : b->ctx) join_side(c);
     b->fp32 = ctxs[0]->fp32;
     ck(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "stream");
     ck(cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming), "event");
@@ -3146,6 +3441,7 @@ int omx_batch_autotune(omx_batch *b, int reps, int *choice)
 {
     OMX_API_BEGIN
     req(b && reps >= 1, "bad argument");
+    batch_decide(b);
     for (auto *c : b->ctx)
         req(!c->started && !c->fields_written,
             "omx_batch_autotune times the passes on the initial zero fields: call it after the grids are "
@@ -3154,6 +3450,8 @@ int omx_batch_autotune(omx_batch *b, int reps, int *choice)
         prepare(c);
         c->epoch++;
     }
+    b->drop_graphs();
+    b->key.clear();
     const int pick = b->fp32 ? batch_autotune_impl<float>(b, reps) : batch_autotune_impl<double>(b, reps);
     if (choice) *choice = pick;
     OMX_API_END(nullptr)
@@ -3165,8 +3463,22 @@ int omx_batch_run(omx_batch *b, int tt0, int nsteps, int n_skip_steps, int t_det
     req(b && nsteps >= 0 && n_skip_steps >= 1 && tt0 >= 1, "bad argument");
     for (auto *c : b->ctx) req(!c->prof, "profiling is on for a member of the batch");
     if (nsteps == 0) return OMX_OK;
+    batch_decide(b);
     if (b->fp32) batch_run_impl<float>(b, tt0, nsteps, n_skip_steps, t_det_print, use_graph);
     else batch_run_impl<double>(b, tt0, nsteps, n_skip_steps, t_det_print, use_graph);
+    OMX_API_END(nullptr)
+}
+
+int omx_batch_run_prepare(omx_batch *b, int tt0, int nsteps, int n_skip_steps, int t_det_print)
+{
+    OMX_API_BEGIN
+    req(b && nsteps >= 0 && n_skip_steps >= 1 && tt0 >= 1, "bad argument");
+    for (auto *c : b->ctx) req(!c->prof, "profiling is on for a member of the batch");
+    if (nsteps == 0) return OMX_OK;
+    batch_decide(b);
+    if (b->fp32) batch_run_impl<float>(b, tt0, nsteps, n_skip_steps, t_det_print, 1, true);
+    else batch_run_impl<double>(b, tt0, nsteps, n_skip_steps, t_det_print, 1, true);
+    ck(cudaStreamSynchronize(b->stream), "prepare");
     OMX_API_END(nullptr)
 }
 
@@ -3185,6 +3497,7 @@ int omx_batch_destroy(omx_batch *b)
 {
     if (!b) return OMX_OK;
     if (b->stream) cudaStreamSynchronize(b->stream);
+    b->drop_graphs();
     if (b->done) cudaEventDestroy(b->done);
     cudaStream_t s = b->stream;
     delete b;

@@ -15,6 +15,8 @@
 // memory.  Material ids (uint8, one per component) and the auxiliary-differential-equation
 // state exist only inside the bounding box of non-vacuum cells.
 #pragma once
+#include <cuda.h>
+#include <cuda_runtime.h>
 #include <stdint.h>
 
 namespace omx {
@@ -78,8 +80,10 @@ template <class R> struct GridArgs {
     int ade_n;
     const int4 *ade_ent;
     const int *ade_b;
-    // device-loop step counter, advanced by the first kernel of each step (null outside omx_run)
+    // device-loop step counter, advanced by the first kernel of each step (null outside omx_run);
+    // the fused 3D pass advances it when its last block finishes (step_done counts the blocks)
     int *step_inc;
+    int *step_done;
     // planes (3D) or rows (2D) marched per thread by the unfused kernels; 0 = default
     int march;
     // a plane soft source added by the 3D bulk E pass to E_old before the update, as k_plane
@@ -180,14 +184,34 @@ struct Fused2Args {
 // form: 0 register prefetch, 4/5/6/8 bulk-copy ring depth, 14/15/16 ring depth 4/5/6 with a
 // dedicated copy warp; < 0 the default
 void launch_fused_tmz(const Fused2Args &A, const GridArgs<float> &G, int form, void *stream);
-// FP32 fused 3D step (k_fused3): in / out buffer sets, the out set's H psi
-constexpr int F3_BY = 8;   // thread rows per block of the fused 3D pass (32 x 8 threads)
+// FP32 fused 3D step (k_fused3_tma): in / out buffer sets, the out set's H psi
 struct Fused3Args {
     FieldPtrs<float> in, out;
     float *psiH_out[3][2];   // H psi of the out set (the in set's is GridArgs::psiH)
 };
-// kch: planes marched per thread (0 = default)
-void launch_fused3(const Fused3Args &A, const GridArgs<float> &G, int kch, void *stream);
+// tensor maps of the in set's six components (Ex, Ey, Ez, Hx, Hy, Hz) for the fused 3D pass:
+// coordinate x = 0 is element i = -3 of a row (so x = 32 t is 16-byte aligned and reaches the
+// halo column i = 32 t), y = j, z = k; box {40, ty + 2, 1}
+struct F3tMaps {
+    CUtensorMap m[6];
+};
+// one grid of a batched fused 3D pass: its in set's tensor maps, arguments and block range
+struct F3tBatchGrid {
+    CUtensorMap m[6];
+    GridArgs<float> G;
+    Fused3Args A;
+    long long item0;         // first block of this grid in the launch
+    int tx, ty, tz, kch;     // tiles along x (32 cells), y (tile rows), z (kch planes)
+};
+// tile rows of a fused 3D form (form <= 0: the default, 8)
+inline int f3t_rows(int form) { return form == 16 ? 16 : 8; }
+bool encode_f3t_maps(F3tMaps *M, const FieldPtrs<float> &in, const Lay &L, int ty);
+// form: tile rows (8 or 16); kch: planes per block (0 = default); err: the device error word
+cudaError_t launch_fused3t(const F3tMaps &M, const Fused3Args &A, const GridArgs<float> &G, int form, int kch,
+                           int *err, void *stream);
+// the batched pass over n grids (device table, largest grid first) with `blocks` blocks in all
+cudaError_t launch_fused3t_batch(const F3tBatchGrid *grids, int n, long long blocks, int form, int *err,
+                                 void *stream);
 void launch_ade_post(const FieldPtrs<float> &Fin, const FieldPtrs<float> &Fout, const GridArgs<float> &G, void *stream);
 // The work after a fused pass in one launch: the dispersive cells (as launch_ade_post), one
 // plane source (as launch_plane) and the emitter current (as launch_inject).  Only for lists

@@ -1,5 +1,7 @@
 // omx_kernels_fast.cu -- FP32 fused path of the Yee/CPML/ADE half-step kernels.  FP32 field
 // state with FP64-precomputed coefficients rounded once to FP32; multiply-adds contract to FMA.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <stdlib.h>
@@ -8,7 +10,7 @@
 #include <algorithm>
 #include "omx_batch.cuh"
 #include "omx_fused2d.cuh"
-#include "omx_fused3d.cuh"
+#include "omx_fused3t.cuh"
 
 namespace omx {
 
@@ -142,12 +144,96 @@ void launch_fused_tmz(const Fused2Args &A, const GridArgs<float> &G, int form, v
     else launch_form<false>(A, G, form, nstrip, (cudaStream_t)s);
 }
 
-void launch_fused3(const Fused3Args &A, const GridArgs<float> &G, int kch, void *s)
+// cuTensorMapEncodeTiled from the driver, looked up once through the runtime (no link to libcuda)
+static PFN_cuTensorMapEncodeTiled_v12000 f3t_encode_fn()
 {
-    const int m = kch > 0 ? kch : 16;
-    const dim3 b(32, F3_BY, 1), g((unsigned)((G.L.nx + 31) / 32), (unsigned)((G.L.ny + F3_BY - 1) / F3_BY),
-                                  (unsigned)((G.L.nz + m - 1) / m));
-    k_fused3<<<g, b, 0, (cudaStream_t)s>>>(A, G, m);
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    return fn;
+}
+
+// One FP32 component over the whole padded array: dims {px, ny + 2, nz + 2}, base at element
+// i = -3 of row (0, 0) (off - 3: 16-byte aligned because element i = 1 is 128-byte aligned; the
+// last element, off - 3 + px (ny + 2)(nz + 2) - 1, lies inside the allocation).  Reads past a
+// dimension return zero.
+bool encode_f3t_maps(F3tMaps *M, const FieldPtrs<float> &in, const Lay &L, int ty)
+{
+    auto fn = f3t_encode_fn();
+    if (!fn || L.dims != 3 || L.off < 3) return false;
+    const cuuint64_t dims[3] = {(cuuint64_t)L.px, (cuuint64_t)(L.ny + 2), (cuuint64_t)(L.nz + 2)};
+    const cuuint64_t strides[2] = {(cuuint64_t)L.px * 4u, (cuuint64_t)L.pz * 4u};
+    const cuuint32_t box[3] = {(cuuint32_t)F3T_BX, (cuuint32_t)(ty + 2), 1u};
+    const cuuint32_t es[3] = {1u, 1u, 1u};
+    for (int c = 0; c < 6; ++c) {
+        if (!in.f[c]) return false;
+        void *base = const_cast<float *>(in.f[c] + (L.off - 3));
+        if (fn(&M->m[c], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+               CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+            return false;
+    }
+    return true;
+}
+
+template <int TY>
+static cudaError_t launch_f3t(const F3tMaps &M, const Fused3Args &A, const GridArgs<float> &G, int kch, int *err,
+                              cudaStream_t s)
+{
+    using S = F3tShape<TY>;
+    static bool attr[FZ_MAX_DEV] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    bool &a = attr[dev < FZ_MAX_DEV ? dev : 0];
+    if (!a) {
+        const cudaError_t e =
+            cudaFuncSetAttribute(k_fused3_tma<TY>, cudaFuncAttributeMaxDynamicSharedMemorySize, S::SMEM_BATCH);
+        if (e != cudaSuccess) return e;
+        a = true;
+    }
+    const int m = kch > 0 ? kch : 64;
+    const dim3 g((unsigned)((G.L.nx + 31) / 32), (unsigned)((G.L.ny + TY - 1) / TY), (unsigned)((G.L.nz + m - 1) / m));
+    k_fused3_tma<TY><<<g, S::THREADS, S::SMEM_BATCH, s>>>(M, A, G, m, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fused3t(const F3tMaps &M, const Fused3Args &A, const GridArgs<float> &G, int form, int kch,
+                           int *err, void *s)
+{
+    if (f3t_rows(form) == 16) return launch_f3t<16>(M, A, G, kch, err, (cudaStream_t)s);
+    return launch_f3t<8>(M, A, G, kch, err, (cudaStream_t)s);
+}
+
+template <int TY>
+static cudaError_t launch_f3t_batch(const F3tBatchGrid *grids, int n, long long blocks, int *err, cudaStream_t s)
+{
+    using S = F3tShape<TY>;
+    static bool attr[FZ_MAX_DEV] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    bool &a = attr[dev < FZ_MAX_DEV ? dev : 0];
+    if (!a) {
+        const cudaError_t e =
+            cudaFuncSetAttribute(k_fused3_batch<TY>, cudaFuncAttributeMaxDynamicSharedMemorySize, S::SMEM_BATCH);
+        if (e != cudaSuccess) return e;
+        a = true;
+    }
+    if (n <= 0 || blocks <= 0) return cudaSuccess;
+    if (blocks > 0x7fffffffLL) return cudaErrorInvalidValue;
+    k_fused3_batch<TY><<<(unsigned)blocks, S::THREADS, S::SMEM_BATCH, s>>>(grids, n, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fused3t_batch(const F3tBatchGrid *grids, int n, long long blocks, int form, int *err, void *s)
+{
+    if (f3t_rows(form) == 16) return launch_f3t_batch<16>(grids, n, blocks, err, (cudaStream_t)s);
+    return launch_f3t_batch<8>(grids, n, blocks, err, (cudaStream_t)s);
 }
 
 template <> void launch_batch3<float>(int pass, const BatchGrid<float> *g, int n, long long total, int kch,

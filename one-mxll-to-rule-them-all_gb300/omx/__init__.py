@@ -327,6 +327,10 @@ class TMxll:
         self._chk(lib().omx_autotune(self._ctx, int(reps), C.byref(choice)))
         return choice.value
 
+    def set_launch_shape(self, shape):
+        """Use a launch shape omx_autotune reported (results are the same bit for bit)."""
+        self._chk(lib().omx_set_launch_shape(self._ctx, int(shape)))
+
     # -- field access ----------------------------------------------------------------------------
     def field_bounds(self, field):
         lo = (C.c_int * 3)()
@@ -436,6 +440,10 @@ class Batch:
     def run(self, tt0, nsteps, n_skip_steps=1, t_det_print=0, use_graph=True):
         A.check(lib().omx_batch_run(self._b, int(tt0), int(nsteps), int(n_skip_steps), int(t_det_print),
                                     1 if use_graph else 0))
+
+    def prepare_run(self, tt0, nsteps, n_skip_steps=1, t_det_print=0):
+        """Build the tables and capture the step graphs `run(tt0, nsteps, ...)` launches."""
+        A.check(lib().omx_batch_run_prepare(self._b, int(tt0), int(nsteps), int(n_skip_steps), int(t_det_print)))
 
     def launch_count(self):
         return int(lib().omx_batch_launch_count(self._b))

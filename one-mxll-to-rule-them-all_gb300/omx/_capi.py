@@ -109,6 +109,7 @@ SIGNATURES = {
     "omx_detectors_collect": (_I, [_VP, C.c_longlong, _PD, _PD, _I, _PI]),
     "omx_run": (_I, [_VP, _I, _I, _I, _I, _I]),
     "omx_run_prepare": (_I, [_VP, _I, _I, _I, _I]),
+    "omx_set_launch_shape": (_I, [_VP, _I]),
     "omx_detectors_write_text": (_I, [_VP, C.c_char_p, _PI]),
     "omx_detectors_dft_setup": (_I, [_VP, _I, _PD, _D]),
     "omx_detectors_dft_read": (_I, [_VP, _PD, _PD]),
@@ -118,6 +119,7 @@ SIGNATURES = {
     "omx_batch_create": (_I, [C.POINTER(_VP), _I, C.POINTER(_VP)]),
     "omx_batch_autotune": (_I, [_VP, _I, _PI]),
     "omx_batch_run": (_I, [_VP, _I, _I, _I, _I, _I]),
+    "omx_batch_run_prepare": (_I, [_VP, _I, _I, _I, _I]),
     "omx_batch_launch_count": (C.c_longlong, [_VP]),
     "omx_batch_synchronize": (_I, [_VP]),
     "omx_tc_gemm_bf16": (_I, [C.POINTER(C.c_uint16), C.POINTER(C.c_uint16), _PF, _PF, _I, _I, _I, C.c_float, _I]),

@@ -1,7 +1,8 @@
 """Batched multi-grid runs (omx_batch_*): several 3D instances of the inverse-design sweep advance
-together through one persistent launch per pass; every grid must equal its own solo run bit for
-bit (same kernels, same per-grid order), with and without the graph and after the batch
-autotuner.  Calls go through the C-ABI."""
+together -- FP32 grids that step with one fused pass in one k_fused3_batch launch per step, the
+others through one persistent launch per half-step pass; every grid must equal its own solo run
+bit for bit (same arithmetic, same per-grid order), with and without the graph and after the
+batch autotuner.  Calls go through the C-ABI."""
 import numpy as np
 import pytest
 
@@ -10,7 +11,7 @@ from omx import decks
 
 pytestmark = pytest.mark.gpu
 
-SIZES = (36, 44, 29, 52)     # uneven sides, one not a multiple of the 32 x 4 tile
+SIZES = (36, 44, 29, 52)     # uneven sides, none a multiple of the 32-cell tile width
 
 
 def build(n, seed, precision):
@@ -26,21 +27,28 @@ def fields(g):
     return [g.read_field(f) for f in (1, 2, 3, 4, 5, 6)]
 
 
-@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+@pytest.mark.parametrize("precision,form", [("fp32", omx.STEP_DEFAULT), ("fp32", omx.STEP_TWO_PASS),
+                                            ("fp64", omx.STEP_DEFAULT)])
 @pytest.mark.parametrize("use_graph,autotune", [(True, False), (False, False), (True, True)])
-def test_batch_equals_solo_runs(precision, use_graph, autotune):
+def test_batch_equals_solo_runs(precision, form, use_graph, autotune):
     steps = 70
     solo, batch = [], []
     for k, n in enumerate(SIZES):
         d, g = build(n, 100 + k, precision)
-        g.set_step_form(omx.STEP_TWO_PASS)    # the batch's arithmetic
+        g.set_step_form(form)                 # the batch runs its members' arithmetic
         g.run(1, steps, d["n_skip"], d["t_det_print"], use_graph=True)
         solo.append((fields(g), g.drain_detectors()[1]))
         g.kill()
         batch.append(build(n, 100 + k, precision))
+        batch[-1][1].set_step_form(form)
     b = omx.Batch([g for _, g in batch])
     if autotune:
-        assert b.autotune(reps=2) in (4, 8, 16, 32)
+        fused = precision == "fp32" and form == omx.STEP_DEFAULT
+        choice = b.autotune(reps=2)
+        if fused:
+            assert choice // 1000 in (8, 16) and choice % 1000 in (16, 32, 64, 128)
+        else:
+            assert choice in (4, 8, 16, 32)
     d0 = batch[0][0]
     b.run(1, 30, d0["n_skip"], d0["t_det_print"], use_graph=use_graph)   # two calls: the stepping state carries over
     b.run(31, steps - 30, d0["n_skip"], d0["t_det_print"], use_graph=use_graph)
@@ -58,9 +66,9 @@ def test_batch_equals_solo_runs(precision, use_graph, autotune):
 
 @pytest.mark.parametrize("precision", ["fp32", "fp64"])
 def test_batch_with_a_grid_that_launches_alone(precision):
-    """A grid of at least 8 tiles per SM (160^3 here) keeps its own H / E launches inside the
-    batched step while the small grids share the persistent passes; every grid still equals its
-    solo run bit for bit."""
+    """Two-pass batch: a grid of at least 8 tiles per SM (160^3 here) keeps its own H / E launches
+    inside the batched step while the small grids share the persistent passes; every grid still
+    equals its solo run bit for bit."""
     sizes, steps = (160, 36, 29), 40
     solo, batch = [], []
     for k, n in enumerate(sizes):
@@ -70,6 +78,7 @@ def test_batch_with_a_grid_that_launches_alone(precision):
         solo.append((fields(g), g.drain_detectors()[1]))
         g.kill()
         batch.append(build(n, 300 + k, precision))
+        batch[-1][1].set_step_form(omx.STEP_TWO_PASS)
     b = omx.Batch([g for _, g in batch])
     d0 = batch[0][0]
     b.run(1, steps, d0["n_skip"], d0["t_det_print"], use_graph=True)

@@ -175,23 +175,155 @@ def test_fp32_within_tolerance(orc_mod, case):
         assert np.max(np.abs(ga["dipole"] - cb["dipole"])) / ref <= 1e-3
 
 
-@pytest.mark.parametrize("n,boundaries,drude,steps", [
-    ((32, 24, 16), (2, 2, 2), False, 90),    # periodic on every axis: every recompute wraps
-    ((64, 32, 24), (3, 2, 2), True, 90),     # CPML x, periodic y / z, a Drude block (k_ade_post)
-    ((32, 40, 36), (3, 3, 3), True, 100),    # CPML on every face, several blocks along y and z
-    ((64, 24, 20), (3, 2, 3), True, 100),    # two tiles along x (lane 0 recomputes inside the grid)
+def fused3_deck(n, boundaries, npml=6, src="plane", media_in_cpml=True, emitters=True):
+    """3D scene for the single-pass FP32 step: a dielectric block, a Drude block and a
+    Drude-Lorentz gold block (one of them reaching into the low-x CPML slab when media_in_cpml),
+    a plane Ex sheet (folded into the pass) or a radial y-source plus a plane (added after the
+    pass), a three-level `material` group, point detectors on E and H near the tile edges."""
+    nx, ny, nz = n
+    d = decks._base(3, n, npml, boundaries, 2.0)
+    ev, fs = omx.UNITS["ev_to_au"], omx.UNITS["fs_to_au"]
+
+    def block(x0, x1, y0, y1, z0, z1):
+        I, J, K = np.meshgrid(np.arange(x0, x1), np.arange(y0, y1), np.arange(z0, z1), indexing="ij")
+        return np.stack([decks._cell_nm(I.ravel(), nx, 2.0), decks._cell_nm(J.ravel(), ny, 2.0),
+                         decks._cell_nm(K.ravel(), nz, 2.0)], axis=1)
+
+    zc = nz // 2
+    d["media"].append(dict(kind="dielectric", eps_r=4.0))
+    d["voxels"].append(block(nx // 3, nx // 3 + 5, 3, 9, zc - 2, zc + 2))
+    d["media"].append(dict(kind="drude", omegaD=7.0, GammaD=0.2, eps_r=1.5))
+    d["voxels"].append(block(nx // 2 + 2, nx // 2 + 7, ny // 2 - 3, ny // 2 + 3, zc - 3, zc + 2))
+    d["media"].append(dict(decks.GOLD_DL))
+    x0 = 2 if media_in_cpml else npml + 2
+    d["voxels"].append(block(x0, x0 + 6, ny - 12, ny - 5, zc - 1, zc + 3))
+    tau = 1.5 * fs
+    # the Ex sheet below the media (a sheet added after the pass must not cross a dispersive cell)
+    d["plane_sources"].append(dict(comp=1, plane_axis=3, plane_index=max(2, min(npml + 3, zc - 5)), j_amp=3.0,
+                                   w0=2.2 * ev, t0=3 * tau,
+                                   tau=tau, t_init=0.0, t_final=1e30, phase=0.0, chirp=0.0))
+    if src == "both":
+        d["sources"].append(dict(dir="y", j_amp=2.0, w0=2.0 * ev, t0=4 * fs, tau=1.5 * fs,
+                                 r0=[-6 * 2.0 * decks.NM, 4 * 2.0 * decks.NM, 0.0], radius=1.5 * d["dr"],
+                                 t_init=0.0, t_final=1e30, phase=0.0, chirp=0.0))
+    if emitters:
+        rng = np.random.default_rng(sum(n))
+        ne = 40
+        cells = np.stack([rng.integers(npml + 2, nx - npml - 1, ne), rng.integers(npml + 2, ny - npml - 1, ne),
+                          rng.integers(zc + 2, max(zc + 3, nz - npml - 1), ne)], axis=1).astype(np.int32)
+        u = rng.normal(size=(ne, 3))
+        u /= np.linalg.norm(u, axis=1, keepdims=True)
+        par = np.concatenate([np.stack([rng.normal(2.1, 0.03, ne) * ev, rng.normal(2.3, 0.03, ne) * ev,
+                                        np.full(ne, 6 * decks.DEBYE), np.full(ne, 7 * decks.DEBYE),
+                                        np.full(ne, 500 * fs), np.full(ne, 60 * fs)], axis=1), u], axis=1)
+        d["groups"].append(dict(group_type=1, model=2, cells=cells, params=par, density=3e-3 / decks.NM ** 3,
+                                dt=d["dt"]))
+    # points on tile edges (x = 32 | 33, y = 8 | 9 | 16, z = 64 | 65 where a plane chunk ends), in
+    # the gold block and near the k = 1 / nz planes, kept out of the CPML corners and off PEC walls,
+    # where the field is absorbed to values whose FP32 relative error says nothing
+    lo = [npml + 2 if b == 3 else 2 for b in boundaries]
+    hi = [m - (npml + 1 if b == 3 else 2) for m, b in zip(n, boundaries)]
+    pts = ([32, 8, zc], [33, 9, zc + 1], [32, 16, zc - 2], [nx // 2, ny // 2, lo[2]], [nx // 2, ny // 2, hi[2]],
+           [x0 + 2, ny - 8, zc + 1], [nx // 2 + 4, ny // 2, zc], [nx // 2, 9, 64], [nx // 2 - 1, 8, 65])
+    for p in pts:
+        p = [min(max(v, l), h) for v, l, h in zip(p, lo, hi)]
+        for f in (1, 2, 3, 4, 6):
+            d["detectors"].append(dict(type=1, field=f, idx=np.array([p], np.int32)))
+    return d
+
+
+def _fused3_ran(g, deck):
+    """True when the grid steps with one pass per step (no H-only launches)."""
+    g.profile(True)
+    g.run(10_000, 2, deck["n_skip"], 0, use_graph=False)
+    g.synchronize()
+    _, nh = g.profile_query(omx.KC_H)
+    _, ne = g.profile_query(omx.KC_E)
+    g.profile(False)
+    return nh == 0 and ne == 2
+
+
+@pytest.mark.parametrize("n,boundaries,src,steps", [
+    ((40, 36, 28), (3, 3, 3), "plane", 90),    # CPML on every face, partial tiles in x and y, DL in the CPML
+    ((64, 24, 20), (3, 3, 2), "plane", 90),    # periodic z: plane 0 is the image of plane nz
+    ((33, 17, 19), (1, 1, 1), "both", 80),     # PEC box, odd sizes, a radial source after the pass
+    ((48, 40, 70), (3, 1, 3), "plane", 100),   # several planes chunks along z
 ])
-def test_fp32_fused3d(orc_mod, n, boundaries, drude, steps):
-    """The FP32 single-pass 3D step (opt-in, omx_set_step_form): detector traces within the FP32 bar of
-    the FP64 oracle through the device loop and through the per-call sequence (omx_step_H
-    deferred into the fused pass)."""
-    deck = periodic_box_deck(n, boundaries, npml=6, drude=drude)
+def test_fp32_fused3d(orc_mod, n, boundaries, src, steps):
+    """The FP32 single-pass 3D step (k_fused3_tma, the default 3D FP32 form when x and y are not
+    periodic): detector traces and fields within the FP32 bar of the FP64 oracle, through the
+    device loop and through the per-call sequence (omx_step_H deferred into the fused pass)."""
+    deck = fused3_deck(n, boundaries, src=src)
     for mode in ("run", "calls"):
-        gpu, cpu, gg, cg, tc, tg = run_both(orc_mod, deck, steps, "fp32", mode, use_graph=True,
-                                            form=omx.STEP_SINGLE_PASS)
+        gpu, cpu, gg, cg, tc, tg = run_both(orc_mod, deck, steps, "fp32", mode, use_graph=True)
         assert np.max(np.abs(tc)) > 0
         assert trace_error(tg, tc) <= FP32_TOL, (mode, trace_error(tg, tc))
         assert compare_fields(gpu, cpu, deck) <= 10 * FP32_TOL
+        for a, b in zip(gg, cg):
+            ga, cb = a.read(), cpu.q_group_read(b)
+            ref = max(np.max(np.abs(cb["dipole"])), 1e-300)
+            assert np.max(np.abs(ga["dipole"] - cb["dipole"])) / ref <= 1e-3
+        assert _fused3_ran(gpu, deck)
+        gpu.kill()
+
+
+def test_fused3d_shapes_bit_identical():
+    """Every tile shape of the fused 3D pass (8 or 16 rows, any planes per block) computes each
+    cell with the same operations: the halo H a block recomputes equals its owner's bit for bit,
+    so fields, records and emitter state agree bit for bit across shapes."""
+    deck = fused3_deck((72, 44, 50), (3, 3, 3), src="plane")
+    out = []
+    for shape in (8064, 8016, 16032, 8007, 16128):
+        g = omx.TMxll(3, deck["grid_Ndims"], deck["npml"], deck["boundaries"], deck["dt"], deck["dr"],
+                      precision="fp32")
+        groups = decks.apply_deck(g, deck, omx, decks.media_map(deck, omx.media_map_from_voxels))
+        for det in deck["detectors"]:
+            g.add_detector(det["type"], det["field"], det["idx"])
+        g.set_launch_shape(shape)
+        g.run(1, 60, deck["n_skip"], 1)
+        _, tr = g.drain_detectors()
+        st = groups[0].read()
+        out.append((tr, [g.read_field(f) for f in range(1, 7)], st["rho"]))
+        assert _fused3_ran(g, deck)
+        g.kill()
+    t0, f0, r0 = out[0]
+    assert np.max(np.abs(t0)) > 0
+    for t, f, r in out[1:]:
+        assert np.array_equal(t, t0) and np.array_equal(r, r0)
+        for a, b in zip(f, f0):
+            assert np.array_equal(a, b)
+
+
+def test_cfg1_full_size_fp64_bit_exact(orc_mod):
+    """The plain 3D configuration at its full size and length: 128^3, dr 2 nm, 10-cell CPML on
+    every face, the Drude-Lorentz gold sphere (r 20 nm), the 2.2 eV plane-wave sheet, 16 point
+    detectors sampled every step, 4000 steps (the oracle takes about a minute on 16 cores).  The
+    FP64 GPU path equals the oracle bit for bit: every detector sample and every field word."""
+    deck = decks.deck_cfg1()
+    assert deck["grid_Ndims"] == [128, 128, 128] and deck["steps"] == 4000
+    gpu, cpu, gg, cg, tc, tg = run_both(orc_mod, deck, deck["steps"], "fp64", "run", use_graph=True)
+    assert tg.shape == tc.shape == (4000, 16)
+    assert np.max(np.abs(tc)) > 0
+    assert np.array_equal(tg, tc), trace_error(tg, tc)
+    assert compare_fields(gpu, cpu, deck) == 0.0
+    gpu.kill()
+
+
+def test_cfg2_full_size_fp64_prefix_bit_exact(orc_mod):
+    """The 2D TMz configuration at its full size (4096^2, periodic x / CPML y, perforated Drude
+    silver film, 1e4 two-level emitters, 16 point detectors): the first 200 steps of the FP64
+    GPU path equal the oracle bit for bit (fields, detector samples, density matrices)."""
+    deck = decks.deck_cfg2()
+    assert deck["grid_Ndims"] == [4096, 4096] and len(deck["groups"][0]["cells"]) == 10000
+    steps = 200
+    gpu, cpu, gg, cg, tc, tg = run_both(orc_mod, deck, steps, "fp64", "run", use_graph=True)
+    assert np.max(np.abs(cpu.read_field(omx.EZ))) > 0      # the pulse is on the grid
+    assert np.array_equal(tg, tc), trace_error(tg, tc)
+    assert compare_fields(gpu, cpu, deck) == 0.0
+    ga, cb = gg[0].read(), cpu.q_group_read(cg[0])
+    for key in ("dipole", "rho", "E"):
+        assert np.array_equal(ga[key], cb[key]), key
+    gpu.kill()
 
 
 def test_long_run_fp64_cfg1_shape(orc_mod):
@@ -378,17 +510,23 @@ def test_per_call_sequence_runs_the_fused_pass():
     assert trace_error(t2, t0) <= FP32_TOL
 
 
-@pytest.mark.parametrize("case,precision", [("cfg1_small", "fp32"), ("cfg3_small", "fp32"), ("cfg3_small", "fp64")])
-def test_two_pass_one_step_calls_equal_one_run(case, precision):
-    """The two-pass path driven one omx_run call per step leaves each step's sampling and emitter
-    work running next to the next call's H pass, with asynchronous drains collected two steps
-    late; records, fields and emitter state equal a single multi-step run bit for bit."""
+@pytest.mark.parametrize("case,precision,form", [("cfg1_small", "fp32", omx.STEP_TWO_PASS),
+                                                 ("cfg3_small", "fp32", omx.STEP_TWO_PASS),
+                                                 ("cfg3_small", "fp64", None),
+                                                 ("cfg1_small", "fp32", None), ("cfg3_small", "fp32", None)])
+def test_two_pass_one_step_calls_equal_one_run(case, precision, form):
+    """A 3D grid driven one omx_run call per step leaves each step's sampling and emitter work
+    running next to the next call's first pass (the two-pass path's H pass, or the fused pass),
+    with asynchronous drains collected two steps late; records, fields and emitter state equal a
+    single multi-step run bit for bit."""
     deck = CASES[case][0]()
     n = 23
     out = []
     for mode in ("one_run", "per_step"):
         g = omx.TMxll(3, deck["grid_Ndims"], deck["npml"], deck["boundaries"], deck["dt"], deck["dr"],
                       precision=precision)
+        if precision == "fp32" and form is not None:
+            g.set_step_form(form)
         mm = decks.media_map(deck, omx.media_map_from_voxels) if deck["voxels"] else None
         groups = decks.apply_deck(g, deck, omx, mm)
         for det in deck["detectors"]:
