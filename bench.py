@@ -526,7 +526,8 @@ def measure(args, dist, config, grid, K, W, err_steps, cpu_seconds):
     if shape is None:
         shape_desc = "library default"
     elif dims == 3 and shape >= 1000:
-        shape_desc = "fused 3D tile 32 x %d, %d planes per block (omx_autotune)" % (shape // 1000, shape % 1000)
+        shape_desc = "fused 3D tile 32 x %d, %d planes per block, ring of %d planes (omx_autotune)" % (
+            shape // 1000 % 100, shape % 1000, shape // 100000 or 4)
     elif dims == 2:
         shape_desc = "fused-kernel form %d (omx_autotune)" % shape
     else:
@@ -686,7 +687,8 @@ def gpu_arm_cfg5(args, dist):
                        "l2": "working set %.1f GB > 126 MB L2, no flush" % (cells * 6 * 4 / 1e9),
                        "loop": "omx_batch_run: one k_fused3_batch launch per step over every grid's tiles "
                                "(largest grid first), the steps captured in CUDA graphs; tile %s from "
-                               "omx_batch_autotune" % ("32 x %d, %d planes per block" % (shape // 1000, shape % 1000)
+                               "omx_batch_autotune" % ("32 x %d, %d planes per block, ring of %d planes" % (shape // 1000 % 100, shape % 1000,
+                                                                               shape // 100000 or 4)
                                                        if shape >= 1000 else "depth %d" % shape),
                        "timing": "wall clock around omx_batch_run + omx_batch_synchronize"},
             "one_at_a_time": {"value": solo_value, "unit": "Gcell-updates/s",

@@ -313,8 +313,9 @@ int omx_set_step_form(omx_ctx *ctx, int form);
  * the fused FP32 TMz kernel's form (0 register prefetch, 4/5/6/8 bulk-copy ring depth, 14/15/16
  * ring depth 4/5/6 filled by a dedicated copy warp, 24/25 the same with depth 4/5 and two 4-cell
  * chunks per thread, 34/36 register tiles of 4/6 rows, 44/45 depth 4/5 with eight compute warps
- * per block -- 44 is the default), the fused FP32 3D pass's tile (rows x 1000 + planes per block:
- * rows 8 or 16; 8064 is the default) or the planes / rows each thread marches in the unfused
+ * per block -- 44 is the default), the fused FP32 3D pass's shape (ring depth x 100000 + tile rows
+ * x 1000 + planes per block: ring depth 0 (the default, 4) or 2..16 staged planes, rows 8 or 16,
+ * 1..128 planes; 8064 is the default) or the planes / rows each thread marches in the unfused
  * kernels.  The candidates run on the initial
  * all-zero fields, which every kernel maps to zero, so the simulation state is unchanged: call it
  * after the grid is configured and before the first step or omx_write_field (OMX_ERR_STATE

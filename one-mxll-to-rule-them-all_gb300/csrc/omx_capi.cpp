@@ -1633,7 +1633,8 @@ template <class R> void run_impl(omx_ctx *c, int tt0, int nsteps, int n_skip, in
     if (!prepare_only) c->rec_count += nrec;
 }
 
-// A launch shape as omx_autotune reports it: fused 3D pass: tile rows x 1000 + planes per block;
+// A launch shape as omx_autotune reports it: fused 3D pass: (ring depth x 100 + tile rows) x 1000
+// + planes per block;
 // fused TMz pass: the kernel form; unfused kernels: planes (3D) or rows (2D) per thread.
 void apply_shape(omx_ctx *c, int v)
 {
@@ -1656,10 +1657,15 @@ template <class R> int autotune_impl(omx_ctx *c, int reps)
     const bool fused = std::is_same<R, float>::value && c->fused_ok;
     std::vector<int> cand;
     if (fused && c->dims == 3) {
-        // fused 3D pass: tile rows x 1000 + planes per block
-        for (int ty : {8, 16})
-            for (int kch : {16, 32, 64, 128})
-                if (kch <= c->n[2] * 2) cand.push_back(ty * 1000 + kch);
+        // fused 3D pass: (ring depth x 100 + tile rows) x 1000 + planes per block
+        int dev = 0, optin = 0;
+        ck(cudaGetDevice(&dev), "device");
+        ck(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev), "device");
+        for (int ring : {0, 6, 8})
+            for (int ty : {8, 16})
+                for (int kch : {8, 16, 32, 64, 128})
+                    if (kch <= c->n[2] * 2 && f3t_smem_bytes(ring * 100 + ty) <= optin)
+                        cand.push_back((ring * 100 + ty) * 1000 + kch);
     } else if (fused) {
         cand = {0, 4, 5, 6, 8, 14, 15, 16, 24, 25, 34, 36, 44, 45};
     } else if (c->dims == 3) {
@@ -2848,9 +2854,16 @@ int omx_set_launch_shape(omx_ctx *c, int shape)
     OMX_API_BEGIN
     join_side(c);
     req(c && shape >= 1, "bad argument");
-    if (c->dims == 3 && c->fp32 && fused_eligible(c))
-        req((shape / 1000 == 8 || shape / 1000 == 16) && shape % 1000 >= 1, "fused 3D shape: (8 | 16) * 1000 + planes");
-    else
+    if (c->dims == 3 && c->fp32 && fused_eligible(c)) {
+        const int form = shape / 1000, rows = form % 100, ring = form / 100;
+        req((rows == 8 || rows == 16) && (ring == 0 || (ring >= 2 && ring <= F3T_RING_MAX)) && shape % 1000 >= 1 &&
+                shape % 1000 <= F3T_KMAX,
+            "fused 3D shape: ring depth (0 or 2..16) * 100000 + (8 | 16) * 1000 + planes (1..128)");
+        int dev = 0, optin = 0;
+        ck(cudaGetDevice(&dev), "device");
+        ck(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev), "device");
+        req(f3t_smem_bytes(form) <= optin, "fused 3D shape: the ring does not fit in a block's shared memory");
+    } else
         req(shape < 1000, "fused 3D shape for a grid that steps with two passes");
     apply_shape(c, shape);
     c->epoch++;
@@ -3098,7 +3111,7 @@ BatchTables<R> batch_tables(omx_batch *b, const std::vector<RunPlan> *plans, int
                 }
                 if (!encode_f3t_maps(reinterpret_cast<F3tMaps *>(e.m), e.A.in, c->L, TY))
                     throw Fail{OMX_ERR_CUDA, "cuTensorMapEncodeTiled failed for the batched fused pass"};
-                e.kch = b->f3kch;
+                e.kch = std::min(std::max(b->f3kch, 1), F3T_KMAX);
                 e.tx = (c->L.nx + 31) / 32;
                 e.ty = (c->L.ny + TY - 1) / TY;
                 e.tz = (c->L.nz + e.kch - 1) / e.kch;
@@ -3320,35 +3333,42 @@ template <class R> int batch_autotune_impl(omx_batch *b, int reps)
     if (b->blocks == 0) b->blocks = batch3_blocks<R>();
     const int n = (int)b->ctx.size();
     if (b->fused == 1) {
-        // fused batched pass: tile rows x 1000 + planes per block, each candidate timed over
-        // `reps` launches on the zero initial fields (the pass maps them to zero)
+        // fused batched pass: (ring depth x 100 + tile rows) x 1000 + planes per block, each
+        // candidate timed over `reps` launches on the zero initial fields (the pass maps them to zero)
         cudaEvent_t e0, e1;
         ck(cudaEventCreate(&e0), "event");
         ck(cudaEventCreate(&e1), "event");
         float best = 0.f;
         int pick = 8064;
         bool first = true;
-        for (int ty : {8, 16})
-            for (int kch : {16, 32, 64, 128}) {
-                b->f3form = ty;
-                b->f3kch = kch;
-                const BatchTables<R> T = batch_tables<R>(b, nullptr, kch, 0);
-                auto once = [&]() {
-                    ck(launch_fused3t_batch(T.f3, n, T.f3_blocks, ty, b->ctx[0]->d_err.p, b->stream), "autotune");
-                };
-                once();
-                ck(cudaEventRecord(e0, b->stream), "event");
-                for (int r = 0; r < reps; ++r) once();
-                ck(cudaEventRecord(e1, b->stream), "event");
-                ck(cudaEventSynchronize(e1), "batch autotune");
-                float ms = 0.f;
-                ck(cudaEventElapsedTime(&ms, e0, e1), "batch autotune");
-                if (first || ms < best) {
-                    best = ms;
-                    pick = ty * 1000 + kch;
-                    first = false;
+        int dev = 0, optin = 0;
+        ck(cudaGetDevice(&dev), "device");
+        ck(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev), "device");
+        for (int ring : {0, 6, 8})
+            for (int ty : {8, 16})
+                for (int kch : {16, 32, 64, 128}) {
+                    const int form = ring * 100 + ty;
+                    if (f3t_smem_bytes(form) > optin) continue;
+                    b->f3form = form;
+                    b->f3kch = kch;
+                    const BatchTables<R> T = batch_tables<R>(b, nullptr, kch, 0);
+                    auto once = [&]() {
+                        ck(launch_fused3t_batch(T.f3, n, T.f3_blocks, form, b->ctx[0]->d_err.p, b->stream),
+                           "autotune");
+                    };
+                    once();
+                    ck(cudaEventRecord(e0, b->stream), "event");
+                    for (int r = 0; r < reps; ++r) once();
+                    ck(cudaEventRecord(e1, b->stream), "event");
+                    ck(cudaEventSynchronize(e1), "batch autotune");
+                    float ms = 0.f;
+                    ck(cudaEventElapsedTime(&ms, e0, e1), "batch autotune");
+                    if (first || ms < best) {
+                        best = ms;
+                        pick = form * 1000 + kch;
+                        first = false;
+                    }
                 }
-            }
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         b->f3form = pick / 1000;

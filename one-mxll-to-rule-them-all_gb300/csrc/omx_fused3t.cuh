@@ -41,23 +41,30 @@
 namespace omx {
 
 constexpr int F3T_BX = 40;    // staged box width: x from i0-4 (16-byte aligned) to i0+35
-constexpr int F3T_D = 4;      // ring depth in planes
 constexpr long long F3T_WAIT_CYCLES = 2000000000LL;   // about one second at the SM clock
 
-// bytes reserved for a grid's GridArgs copy in the batched kernel's shared memory
+// bytes reserved for the copy of a grid's GridArgs in the kernels' shared memory
 constexpr int F3T_ARGB = (int)((sizeof(GridArgs<float>) + 15) / 16 * 16);
 
+// Shared memory of a block, for a ring of nd plane slots: the copies of the grid's arguments
+// (GridArgs, Fused3Args), the ring (1024-byte aligned), the new-H tiles, the per-plane z
+// coefficients (2 float4 a plane) and the 2 nd mbarriers.  TY tile rows, RPT rows per compute
+// thread (1 for 8 rows, 2 for 16): TY / RPT compute warps, a halo warp, a copy warp.
 template <int TY> struct F3tShape {
+    static constexpr int RPT = TY / 8;
+    static constexpr int NCW = TY / RPT;                       // compute warps
     static constexpr int BY = TY + 2;                          // staged rows j0-1 .. j0+TY
     static constexpr int BOXF = F3T_BX * BY;                   // floats per staged box
     static constexpr int BOXB = (BOXF * 4 + 127) / 128 * 128;  // bytes per box slot (128-byte aligned)
     static constexpr int SLOTB = 6 * BOXB;                     // one plane: Ex, Ey, Ez, Hx, Hy, Hz
     static constexpr int HNF = (TY + 1) * 33;                  // new-H tile incl. column i0-1 and row j0-1
-    static constexpr int SMEM = F3T_D * SLOTB + 2 * 3 * HNF * 4 + 2 * F3T_D * 8;
-    // with the copy of the grid's arguments (GridArgs, Fused3Args) that the kernels read
-    // with the copy of the grid's arguments (GridArgs, Fused3Args) that the kernels read
-    static constexpr int SMEM_BATCH = SMEM + F3T_ARGB + (int)((sizeof(Fused3Args) + 15) / 16 * 16);
-    static constexpr int THREADS = 32 * (TY + 2);
+    static constexpr int ARGS = F3T_ARGB + (int)((sizeof(Fused3Args) + 15) / 16 * 16);
+    static constexpr int RING = (ARGS + 1023) / 1024 * 1024;
+    static constexpr int THREADS = 32 * (NCW + 2);
+    __host__ __device__ static constexpr int hn_off(int nd) { return RING + nd * SLOTB; }
+    __host__ __device__ static constexpr int z_off(int nd) { return (hn_off(nd) + 2 * 3 * HNF * 4 + 15) / 16 * 16; }
+    __host__ __device__ static constexpr int bar_off(int nd) { return z_off(nd) + (F3T_KMAX + 2) * 32; }
+    __host__ __device__ static constexpr int smem(int nd) { return bar_off(nd) + 2 * nd * 8; }
 };
 
 __device__ __forceinline__ void tma_load_3d(void *dst, const void *tmap, int x, int y, int z, uint64_t *bar)
@@ -157,9 +164,10 @@ __device__ __forceinline__ float f3t_hz(float hz, float ey_c, float ey_ip, float
     return h;
 }
 
-// The ADE of one dispersive component-cell: ade_update's arithmetic in the same order, with the
-// pole state read again in the second loop instead of held in register arrays (which would take
-// registers from the whole pass).  st: the cell's state at slot 0 (PD), V: the slot stride, P:
+// The ADE of one dispersive component-cell: ade_update's terms in the same order, each product
+// added by an explicitly rounded FMA (so that no tile shape or code path contracts differently),
+// with the pole state read again in the second loop instead of held in register arrays (which
+// would take registers from the whole pass).  st: the cell's state at slot 0 (PD), V: the slot stride, P:
 // poles per cell in the state.
 __device__ __forceinline__ float f3t_ade(float e, float rot, int type, const MedR<float> *mp, float *st, long long V,
                                          int P)
@@ -167,21 +175,23 @@ __device__ __forceinline__ float f3t_ade(float e, float rot, int type, const Med
     const MedR<float> &m = *mp;
     const float PD = st[0];
     if (type == CLS_DRUDE) {
-        const float t = m.C1 * e + m.C3 * rot - m.C4 * PD;
-        st[0] = m.A1 * PD + m.A2 * (t + e);
+        const float t = __fmaf_rn(-m.C4, PD, __fmaf_rn(m.C3, rot, __fmul_rn(m.C1, e)));
+        st[0] = __fmaf_rn(m.A1, PD, __fmul_rn(m.A2, __fadd_rn(t, e)));
         return t;
     }
     const float eo = st[V];
-    float t = m.C1 * e + m.C2 * eo + m.C3 * rot - m.C4 * PD;
+    float t = __fmaf_rn(-m.C4, PD, __fmaf_rn(m.C3, rot, __fmaf_rn(m.C2, eo, __fmul_rn(m.C1, e))));
     const int np = m.np;
 #pragma unroll 1
-    for (int p = 0; p < np; ++p) t = t - m.B1[p] * st[(2 + p) * V] - m.B2[p] * st[(2 + P + p) * V];
-    st[0] = m.A1 * PD + m.A2 * (t + e);
+    for (int p = 0; p < np; ++p)
+        t = __fmaf_rn(-m.B2[p], st[(2 + P + p) * V], __fmaf_rn(-m.B1[p], st[(2 + p) * V], t));
+    st[0] = __fmaf_rn(m.A1, PD, __fmul_rn(m.A2, __fadd_rn(t, e)));
+    const float dte = __fsub_rn(t, eo);
 #pragma unroll 1
     for (int p = 0; p < np; ++p) {
         const float pl = st[(2 + p) * V], plo = st[(2 + P + p) * V];
         st[(2 + P + p) * V] = pl;
-        st[(2 + p) * V] = m.al[p] * pl + m.be[p] * plo + m.ga[p] * (t - eo);
+        st[(2 + p) * V] = __fmaf_rn(m.al[p], pl, __fmaf_rn(m.be[p], plo, __fmul_rn(m.ga[p], dte)));
     }
     st[V] = e;
     return t;
@@ -191,27 +201,42 @@ __device__ __forceinline__ float f3t_ade(float e, float rot, int type, const Med
 __device__ __forceinline__ float f3t_media(float e, float rot, int c, int b, const GridArgs<float> &G)
 {
     const ClsR<float> cl = G.cls[G.mat[c][b]];
-    if (cl.type == CLS_PLAIN) return e + cl.coef * rot;
+    if (cl.type == CLS_PLAIN) return __fmaf_rn(cl.coef, rot, e);
     return f3t_ade(e, rot, cl.type, G.med + cl.medium, G.ade + (long long)c * (2 + 2 * G.P) * G.bbV + b, G.bbV, G.P);
 }
 
 template <int TY> constexpr int f3t_min_blocks() { return TY == 8 ? 3 : 2; }
 
+// the form a plane is computed in: lean (no CPML psi, media or plane source at the block's cells
+// of the plane) or general
+template <bool B> struct F3tForm {
+    static constexpr bool value = B;
+};
+
+// prefetch the 128-byte line of p into L1 (the next plane's CPML and media words)
+__device__ __forceinline__ void f3t_prefetch(const void *p)
+{
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+}
+
 // One block's work: tile (bx, by) of 32 x TY columns over plane chunk bz of one grid.  maps: the
-// in set's tensor maps (kernel parameter or global memory); nblk: the blocks of this grid's pass
-// (the last of them to finish advances the grid's device-loop step counter); smem: the dynamic
-// shared memory (F3tShape<TY>::SMEM bytes, 1024-byte aligned).
+// in set's tensor maps (kernel parameter or global memory); A, G: the grid's arguments (in
+// shared memory); nblk: the blocks of this grid's pass (the last of them to finish advances the
+// grid's device-loop step counter); smem: the dynamic shared memory (1024-byte aligned).
 template <int TY>
 __device__ __forceinline__ void f3t_tile(const CUtensorMap *maps, const Fused3Args &A, const GridArgs<float> &G,
-                                         int bx, int by, int bz, int kch, unsigned nblk, int *err,
+                                         int bx, int by, int bz, int kch, int nd, unsigned nblk, int *err,
                                          unsigned char *f3_smem)
 {
     using S = F3tShape<TY>;
-    constexpr int NC = TY + 1;                 // warps that read the ring: compute + halo
-    float *ring = reinterpret_cast<float *>(f3_smem);
-    float *hn = reinterpret_cast<float *>(f3_smem + F3T_D * S::SLOTB);   // [2][3][TY+1][33]
-    uint64_t *full = reinterpret_cast<uint64_t *>(f3_smem + F3T_D * S::SLOTB + 2 * 3 * S::HNF * 4);
-    uint64_t *empty = full + F3T_D;
+    constexpr int RPT = S::RPT, NCW = S::NCW;
+    constexpr int NC = NCW + 1;                // warps that read the ring: compute + halo
+    constexpr int CB = S::BOXB / 4;
+    float *ring = reinterpret_cast<float *>(f3_smem + S::RING);           // [nd][6][box]
+    float *hn = reinterpret_cast<float *>(f3_smem + S::hn_off(nd));      // [2][3][TY+1][33]
+    float4 *zc = reinterpret_cast<float4 *>(f3_smem + S::z_off(nd));     // [plane - pa][2]
+    uint64_t *full = reinterpret_cast<uint64_t *>(f3_smem + S::bar_off(nd));
+    uint64_t *empty = full + nd;
     const Lay &L = G.L;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int i0 = 1 + bx * 32, j0 = 1 + by * TY;
@@ -222,22 +247,40 @@ __device__ __forceinline__ void f3t_tile(const CUtensorMap *maps, const Fused3Ar
     const int pa = (k0 > 1 || perz) ? k0 - 1 : k0;
     const int nq = k1 + 2 - pa;
     if (threadIdx.x == 0) {
-        for (int s = 0; s < F3T_D; ++s) {
+        for (int s = 0; s < nd; ++s) {
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], NC);
         }
         mbar_fence_init();
     }
-    __syncthreads();
+    // per-plane z coefficients of the planes pa .. k1 (index of plane 0 of a periodic axis: nz):
+    // (den_h, den_e, bH, cH) and (bE, cE, H psi layer, E psi layer)
+    for (int t = threadIdx.x; t < nq - 1; t += blockDim.x) {
+        const int p = pa + t, kk = p == 0 ? L.nz : p;
+        const int lh = G.lH[2][kk], le = G.lE[2][kk];
+        zc[2 * t] = make_float4(G.den_h[2][kk], G.den_e[2][kk], G.bH[2][kk], G.cH[2][kk]);
+        zc[2 * t + 1] = make_float4(G.bE[2][kk], G.cE[2][kk], __int_as_float(lh), __int_as_float(le));
+    }
+    // does a CPML slab of x or y reach a cell this block updates (own or halo)?  Then every plane
+    // takes the general form; else a plane without z CPML, media or plane source takes the lean one
+    bool slab = false;
+    if (threadIdx.x < 33) {
+        const int ih = i0 - 1 + (int)threadIdx.x;
+        if (ih >= 1 && ih <= L.nx) slab = G.lH[0][ih] >= 0 || G.lE[0][ih] >= 0;
+    } else if (threadIdx.x < 34 + TY) {
+        const int jh = j0 - 34 + (int)threadIdx.x;
+        if (jh >= 1 && jh <= L.ny) slab = G.lH[1][jh] >= 0 || G.lE[1][jh] >= 0;
+    }
+    const bool xy_slab = __syncthreads_or(slab) != 0;
 
-    if (warp == TY + 1) {
+    if (warp == NCW + 1) {
         // ---- copy warp: lane 0 stages plane pa + q into slot q % D
         if (lane != 0) return;
         int q = 0;
         bool ok = true;
         for (; q < nq; ++q) {
-            const int s = q % F3T_D;
-            if (q >= F3T_D && !mbar_wait_bounded(&empty[s], (uint32_t)(((q / F3T_D) - 1) & 1), F3T_WAIT_CYCLES)) {
+            const int s = q % nd;
+            if (q >= nd && !mbar_wait_bounded(&empty[s], (uint32_t)(((q / nd) - 1) & 1), F3T_WAIT_CYCLES)) {
                 ok = false;
                 break;
             }
@@ -247,38 +290,50 @@ __device__ __forceinline__ void f3t_tile(const CUtensorMap *maps, const Fused3Ar
             float *dst = ring + (size_t)s * (S::SLOTB / 4);
 #pragma unroll
             for (int c = 0; c < 6; ++c)
-                tma_load_3d(dst + c * (S::BOXB / 4), &maps[c], 32 * bx, j0 - 1, z, &full[s]);
+                tma_load_3d(dst + c * CB, &maps[c], 32 * bx, j0 - 1, z, &full[s]);
         }
         if (!ok) {
             atomicOr(err, 1);
-            for (int p = max(0, q - F3T_D); p < q; ++p)
-                mbar_wait_bounded(&full[p % F3T_D], (uint32_t)((p / F3T_D) & 1), F3T_WAIT_CYCLES);
+            for (int p = max(0, q - nd); p < q; ++p)
+                mbar_wait_bounded(&full[p % nd], (uint32_t)((p / nd) & 1), F3T_WAIT_CYCLES);
         }
         return;
     }
 
-    // ---- compute warps (warp < TY: row j0 + warp) and the halo warp (warp == TY)
-    const bool cw = warp < TY;
+    // ---- compute warps (warp < NCW: rows j0 + RPT warp + r) and the halo warp (warp == NCW)
+    const bool cw = warp < NCW;
     const float dt_mu0 = G.dt_mu0, dt_eps0 = G.dt_eps0;
-    // this thread's cell: compute warps own (i0 + lane, j0 + warp); the halo warp takes the row
-    // halo cell (i0 + lane, j0 - 1) and, for lane < TY, the column halo cell (i0 - 1, j0 + lane)
     const int i = i0 + lane;
-    const int j = cw ? j0 + warp : j0 - 1;
-    const bool own = cw && i <= L.nx && j <= L.ny;
-    const int ic = min(i, L.nx), jc = max(1, min(j, L.ny));
-    const float dhx = G.den_h[0][ic], dhy = G.den_h[1][jc], dex = G.den_e[0][ic], dey = G.den_e[1][jc];
-    const int lhx = G.lH[0][ic], lhy = G.lH[1][jc], lex = G.lE[0][ic], ley = G.lE[1][jc];
-    // halo cells: row (i, j0 - 1) valid when j0 > 1 and i <= nx; column (i0 - 1, jh) when i0 > 1,
-    // lane < TY and jh <= ny (a non-periodic index 0 is the PEC ghost: new H = 0)
+    const int ic = min(i, L.nx);
+    const float dhx = G.den_h[0][ic], dex = G.den_e[0][ic];
+    const int lhx = G.lH[0][ic], lex = G.lE[0][ic];
+    const int cc = lane + 4;                   // staged column of i
+    // compute warps: cells (i, j_r), j_r = j0 + RPT warp + r, staged row rr_r = j_r - j0 + 1.  The
+    // halo warp: the row halo cell (i, j0 - 1) and, for lane < TY, the column halo cell
+    // (i0 - 1, j0 + lane) (a non-periodic index 0 is the PEC ghost: new H = 0)
+    const int jb = cw ? j0 + RPT * warp : j0 - 1;
+    float dhy[RPT], dey[RPT];
+    int lhy[RPT], ley[RPT];
+    bool own[RPT], bbc[RPT];
+#pragma unroll
+    for (int r = 0; r < RPT; ++r) {
+        const int j = jb + r, jc = max(1, min(j, L.ny));
+        dhy[r] = G.den_h[1][jc];
+        dey[r] = G.den_e[1][jc];
+        lhy[r] = G.lH[1][jc];
+        ley[r] = G.lE[1][jc];
+        own[r] = cw && i <= L.nx && j <= L.ny;
+        bbc[r] = own[r] && i >= G.bb0[0] && i <= G.bb1[0] && j >= G.bb0[1] && j <= G.bb1[1];
+    }
     const bool row_h = !cw && j0 > 1 && i <= L.nx;
     const bool col_h = !cw && i0 > 1 && lane < TY && j0 + lane <= L.ny;
-    const bool bb_ij = own && i >= G.bb0[0] && i <= G.bb1[0] && j >= G.bb0[1] && j <= G.bb1[1];
-    const int col = (int)L.off + i + L.px * j;   // element offsets < 2^31 (checked by the host)
-    const int cc = lane + 4;                   // staged column of i; row of j: warp + 1 (row halo: 0)
-    const int rr = cw ? warp + 1 : 0;
+    const int col0 = (int)L.off + i + L.px * jb;   // element offsets < 2^31 (checked by the host)
+    const int rr0 = cw ? RPT * warp + 1 : 0;
 
     bool fail = false;
-    float hxm = 0.f, hym = 0.f;                // new Hx, Hy of this cell at plane k - 1
+    float hxm[RPT], hym[RPT];                  // new Hx, Hy of the own cells at plane k - 1
+#pragma unroll
+    for (int r = 0; r < RPT; ++r) hxm[r] = hym[r] = 0.f;
     if (pa < k0) {
         // new H of plane pa = k0 - 1 (or the image of plane 0) for the owned cells, no writes
         fail |= !mbar_wait_bounded(&full[0], 0u, F3T_WAIT_CYCLES);
@@ -286,59 +341,89 @@ __device__ __forceinline__ void f3t_tile(const CUtensorMap *maps, const Fused3Ar
         if (cw) {
             const int kk = (pa == 0) ? L.nz : pa;
             const float *B0 = ring, *B1 = ring + S::SLOTB / 4;
-            const int o = rr * F3T_BX + cc;
-            const float ex_c = B0[o], ey_c = B0[S::BOXB / 4 + o], ez_c = B0[2 * (S::BOXB / 4) + o];
-            const float ez_jp = B0[2 * (S::BOXB / 4) + o + F3T_BX], ez_ip = B0[2 * (S::BOXB / 4) + o + 1];
-            const float ex_kp = B1[o], ey_kp = B1[S::BOXB / 4 + o];
-            const float dhz = G.den_h[2][kk];
-            const int lhz = G.lH[2][kk];
-            hxm = f3t_hx(B0[3 * (S::BOXB / 4) + o], ez_c, ez_jp, ey_c, ey_kp, dhy, dhz, dt_mu0, lhy, lhz, G, A, ic, jc,
-                         kk, own ? 1 : 0);
-            hym = f3t_hy(B0[4 * (S::BOXB / 4) + o], ez_c, ez_ip, ex_c, ex_kp, dhx, dhz, dt_mu0, lhx, lhz, G, A, ic, jc,
-                         kk, own ? 1 : 0);
+            const float4 z0 = zc[0], z1 = zc[1];
+            const int lhz = __float_as_int(z1.z);
+#pragma unroll
+            for (int r = 0; r < RPT; ++r) {
+                const int o = (rr0 + r) * F3T_BX + cc;
+                const float ex_c = B0[o], ey_c = B0[CB + o], ez_c = B0[2 * CB + o];
+                const float ez_jp = B0[2 * CB + o + F3T_BX], ez_ip = B0[2 * CB + o + 1];
+                const float ex_kp = B1[o], ey_kp = B1[CB + o];
+                const int jc = max(1, min(jb + r, L.ny));
+                hxm[r] = f3t_hx(B0[3 * CB + o], ez_c, ez_jp, ey_c, ey_kp, dhy[r], z0.x, dt_mu0, lhy[r], lhz, G, A, ic,
+                                jc, kk, own[r] ? 1 : 0);
+                hym[r] = f3t_hy(B0[4 * CB + o], ez_c, ez_ip, ex_c, ex_kp, dhx, z0.x, dt_mu0, lhx, lhz, G, A, ic, jc,
+                                kk, own[r] ? 1 : 0);
+            }
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(&empty[0]);
+    } else {
+        fail |= !mbar_wait_bounded(&full[0], 0u, F3T_WAIT_CYCLES);
     }
 
-    for (int k = k0; k <= k1; ++k) {
-        const int q = k - pa, sc = q % F3T_D, sn = (q + 1) % F3T_D;
-        fail |= !mbar_wait_bounded(&full[sc], (uint32_t)((q / F3T_D) & 1), F3T_WAIT_CYCLES);
-        fail |= !mbar_wait_bounded(&full[sn], (uint32_t)(((q + 1) / F3T_D) & 1), F3T_WAIT_CYCLES);
+    // Planes that need none of the CPML psi, the media box or the plane source take the lean
+    // form (the same expressions with those branches left out): no x / y slab at the block's
+    // cells, no z slab at the plane, no media-box cell in the tile's part of the plane, no
+    // source plane through the tile.
+    const bool mb_xy = G.bb1[0] >= G.bb0[0] && G.bb1[1] >= G.bb0[1] && G.bb1[2] >= G.bb0[2] &&
+                       G.bb0[0] <= i0 + 31 && G.bb1[0] >= i0 && G.bb0[1] <= j0 + TY - 1 && G.bb1[1] >= j0;
+    const int mbk0 = mb_xy ? G.bb0[2] : 1, mbk1 = mb_xy ? G.bb1[2] : 0;
+    const bool pl_xy = G.pl_on && ((G.pl_axis == 0 && G.pl_index >= i0 && G.pl_index <= i0 + 31) ||
+                                   (G.pl_axis == 1 && G.pl_index >= j0 && G.pl_index <= j0 + TY - 1));
+    const int plk = (G.pl_on && G.pl_axis == 2) ? G.pl_index : -1;
+    auto lean_at = [&](int k, float4 z1) {
+        return !xy_slab && !pl_xy && __float_as_int(z1.z) < 0 && __float_as_int(z1.w) < 0 && k != plk &&
+               (k < mbk0 || k > mbk1);
+    };
+
+    // One plane: new H of the tile (+ halo) into shared memory and HBM, the barrier, then new E.
+    // Returns true when a wait ran out somewhere in the block (every consumer warp then leaves).
+    auto plane = [&](auto form, int k, int sc, int sn, float4 z0, float4 z1) -> bool {
+        constexpr bool LEAN = decltype(form)::value;
         const float *Bc = ring + (size_t)sc * (S::SLOTB / 4);
         const float *Bn = ring + (size_t)sn * (S::SLOTB / 4);
-        constexpr int CB = S::BOXB / 4;
         const float *Exc = Bc, *Eyc = Bc + CB, *Ezc = Bc + 2 * CB, *Hxc = Bc + 3 * CB, *Hyc = Bc + 4 * CB,
                     *Hzc = Bc + 5 * CB;
-        const float dhz = G.den_h[2][k], dez = G.den_e[2][k];
-        const int lhz = G.lH[2][k], lez = G.lE[2][k];
+        const float dhz = z0.x;
+        const int lhz = __float_as_int(z1.z);
         float *hp = hn + (k & 1) * 3 * S::HNF;   // [Hx, Hy, Hz][TY+1][33]
+        float eo[RPT][3];                        // lean form: old E of the own cells across the barrier
         if (cw) {
-            // new H of the own cell: into the tile in shared memory and out to HBM (nothing of it
-            // stays in registers across the barrier; the E half reads it back)
-            const int o = rr * F3T_BX + cc;
-            const float ex_c = Exc[o], ey_c = Eyc[o], ez_c = Ezc[o];
-            const float ez_jp = Ezc[o + F3T_BX], ez_ip = Ezc[o + 1];
-            const float ey_ip = Eyc[o + 1], ex_jp = Exc[o + F3T_BX];
-            const float ex_kp = Bn[o], ey_kp = Bn[CB + o];
-            const float hx = f3t_hx(Hxc[o], ez_c, ez_jp, ey_c, ey_kp, dhy, dhz, dt_mu0, lhy, lhz, G, A, ic, jc, k,
-                                    own ? 2 : 0);
-            const float hy = f3t_hy(Hyc[o], ez_c, ez_ip, ex_c, ex_kp, dhx, dhz, dt_mu0, lhx, lhz, G, A, ic, jc, k,
-                                    own ? 2 : 0);
-            const float hz = f3t_hz(Hzc[o], ey_c, ey_ip, ex_c, ex_jp, dhx, dhy, dt_mu0, lhx, lhy, G, A, ic, jc, k,
-                                    own ? 2 : 0);
-            const int h = rr * 33 + lane + 1;
-            hp[h] = hx;
-            hp[S::HNF + h] = hy;
-            hp[2 * S::HNF + h] = hz;
-            if (own) {
-                const int idx = col + (int)L.pz * k;
-                __stcs(A.out.f[3] + idx, hx);
-                __stcs(A.out.f[4] + idx, hy);
-                __stcs(A.out.f[5] + idx, hz);
-                if (perz && k == L.nz) {   // periodic ghost plane H(0) = H(nz) (mxll_3D_mod.f90:725-738)
-                    A.out.f[3][idx - L.nz * (int)L.pz] = hx;
-                    A.out.f[4][idx - L.nz * (int)L.pz] = hy;
+            // new H of the own cells: into the tile in shared memory and out to HBM
+#pragma unroll
+            for (int r = 0; r < RPT; ++r) {
+                const int o = (rr0 + r) * F3T_BX + cc;
+                const int jc = max(1, min(jb + r, L.ny));
+                const float ex_c = Exc[o], ey_c = Eyc[o], ez_c = Ezc[o];
+                const float ez_jp = Ezc[o + F3T_BX], ez_ip = Ezc[o + 1];
+                const float ey_ip = Eyc[o + 1], ex_jp = Exc[o + F3T_BX];
+                const float ex_kp = Bn[o], ey_kp = Bn[CB + o];
+                if constexpr (LEAN) {
+                    eo[r][0] = ex_c;
+                    eo[r][1] = ey_c;
+                    eo[r][2] = ez_c;
+                }
+                const int pm = (LEAN || !own[r]) ? 0 : 2;
+                const float hx = f3t_hx(Hxc[o], ez_c, ez_jp, ey_c, ey_kp, dhy[r], dhz, dt_mu0, lhy[r], lhz, G, A, ic,
+                                        jc, k, pm);
+                const float hy = f3t_hy(Hyc[o], ez_c, ez_ip, ex_c, ex_kp, dhx, dhz, dt_mu0, lhx, lhz, G, A, ic, jc, k,
+                                        pm);
+                const float hz = f3t_hz(Hzc[o], ey_c, ey_ip, ex_c, ex_jp, dhx, dhy[r], dt_mu0, lhx, lhy[r], G, A, ic,
+                                        jc, k, pm);
+                const int h = (rr0 + r) * 33 + lane + 1;
+                hp[h] = hx;
+                hp[S::HNF + h] = hy;
+                hp[2 * S::HNF + h] = hz;
+                if (own[r]) {
+                    const int idx = col0 + L.px * r + (int)L.pz * k;
+                    __stcs(A.out.f[3] + idx, hx);
+                    __stcs(A.out.f[4] + idx, hy);
+                    __stcs(A.out.f[5] + idx, hz);
+                    if (perz && k == L.nz) {   // periodic ghost plane H(0) = H(nz) (mxll_3D_mod.f90:725-738)
+                        A.out.f[3][idx - L.nz * (int)L.pz] = hx;
+                        A.out.f[4][idx - L.nz * (int)L.pz] = hy;
+                    }
                 }
             }
         } else {
@@ -347,14 +432,14 @@ __device__ __forceinline__ void f3t_tile(const CUtensorMap *maps, const Fused3Ar
             if (row_h) {
                 const int o = cc;                      // staged row 0
                 const float e_x = Exc[o], e_y = Eyc[o], e_z = Ezc[o];
-                rx = f3t_hx(Hxc[o], e_z, Ezc[o + F3T_BX], e_y, Bn[CB + o], dhy, dhz, dt_mu0, lhy, lhz, G, A, ic,
-                            j0 - 1, k, 1);
-                rz = f3t_hz(Hzc[o], e_y, Eyc[o + 1], e_x, Exc[o + F3T_BX], dhx, dhy, dt_mu0, lhx, lhy, G, A, ic,
-                            j0 - 1, k, 1);
+                rx = f3t_hx(Hxc[o], e_z, Ezc[o + F3T_BX], e_y, Bn[CB + o], dhy[0], dhz, dt_mu0, lhy[0], lhz, G, A, ic,
+                            j0 - 1, k, LEAN ? 0 : 1);
+                rz = f3t_hz(Hzc[o], e_y, Eyc[o + 1], e_x, Exc[o + F3T_BX], dhx, dhy[0], dt_mu0, lhx, lhy[0], G, A, ic,
+                            j0 - 1, k, LEAN ? 0 : 1);
             }
             hp[lane + 1] = rx;
             hp[2 * S::HNF + lane + 1] = rz;
-            // column halo (i0 - 1, jh): Hz and Hy
+            // column halo (i0 - 1, j0 + lane): Hz and Hy
             if (lane < TY) {
                 float cy = 0.f, cz = 0.f;
                 if (col_h) {
@@ -363,91 +448,168 @@ __device__ __forceinline__ void f3t_tile(const CUtensorMap *maps, const Fused3Ar
                     const int lhx_h = G.lH[0][ih], lhy_h = G.lH[1][jhc];
                     const int o = (lane + 1) * F3T_BX + 3;
                     const float e_x = Exc[o], e_y = Eyc[o], e_z = Ezc[o];
-                    cy = f3t_hy(Hyc[o], e_z, Ezc[o + 1], e_x, Bn[o], dhx_h, dhz, dt_mu0, lhx_h, lhz, G, A, ih, jhc, k, 1);
+                    cy = f3t_hy(Hyc[o], e_z, Ezc[o + 1], e_x, Bn[o], dhx_h, dhz, dt_mu0, lhx_h, lhz, G, A, ih, jhc, k,
+                                LEAN ? 0 : 1);
                     cz = f3t_hz(Hzc[o], e_y, Eyc[o + 1], e_x, Exc[o + F3T_BX], dhx_h, dhy_h, dt_mu0, lhx_h, lhy_h, G,
-                                A, ih, jhc, k, 1);
+                                A, ih, jhc, k, LEAN ? 0 : 1);
                 }
                 hp[S::HNF + (lane + 1) * 33] = cy;
                 hp[2 * S::HNF + (lane + 1) * 33] = cz;
             }
         }
         // the new-H tile is complete; every consumer warp learns whether any wait ran out
-        if (bar_any(1, 32 * NC, fail)) {
-            if (threadIdx.x == 0) atomicOr(err, 1);
-            break;
-        }
+        if (bar_any(1, 32 * NC, fail)) return true;
         if (cw) {
-            const int idx = col + (int)L.pz * k;
-            const int h = rr * 33 + lane + 1;
-            const float hx = hp[h], hy = hp[S::HNF + h], hz = hp[2 * S::HNF + h];
-            const int o = rr * F3T_BX + cc;
-            const float ex_c = Exc[o], ey_c = Eyc[o], ez_c = Ezc[o];
-            const float hz_im = hp[2 * S::HNF + h - 1], hy_im = hp[S::HNF + h - 1];
-            const float hz_jm = hp[2 * S::HNF + h - 33], hx_jm = hp[h - 33];
-            const float rx = (hz - hz_jm) * dey + (hym - hy) * dez;
-            const float ry = (hz_im - hz) * dex + (hx - hxm) * dez;
-            const float rz = (hy - hy_im) * dex + (hx_jm - hx) * dey;
-            float ex = ex_c, ey = ey_c, ez = ez_c;
-            if (G.pl_on && (G.pl_axis == 0 ? i : (G.pl_axis == 1 ? j : k)) == G.pl_index) {
-                // the plane source of this step (source_interactions before the E update)
-                const double a = sp_get(G.pl_amp);
-                if (a != 0.0) {
-                    const double add = __dmul_rn(G.pl_c_src, a);
-                    if (G.pl_comp == 0) ex = (float)__dadd_rn((double)ex, add);
-                    else if (G.pl_comp == 1) ey = (float)__dadd_rn((double)ey, add);
-                    else ez = (float)__dadd_rn((double)ez, add);
+            const float dez = z0.y;
+            const int lez = __float_as_int(z1.w);
+#pragma unroll
+            for (int r = 0; r < RPT; ++r) {
+                const int j = jb + r;
+                const int h = (rr0 + r) * 33 + lane + 1;
+                const float hx = hp[h], hy = hp[S::HNF + h], hz = hp[2 * S::HNF + h];
+                const float hz_im = hp[2 * S::HNF + h - 1], hy_im = hp[S::HNF + h - 1];
+                const float hz_jm = hp[2 * S::HNF + h - 33], hx_jm = hp[h - 33];
+                // curl of the new H, every operation rounded explicitly (the lean and the general
+                // form, and every tile shape, give a cell the same bits)
+                const float dhyk = __fsub_rn(hym[r], hy), dhxk = __fsub_rn(hx, hxm[r]);   // planes k-1, k
+                const float rx = __fmaf_rn(dhyk, dez, __fmul_rn(__fsub_rn(hz, hz_jm), dey[r]));
+                const float ry = __fmaf_rn(dhxk, dez, __fmul_rn(__fsub_rn(hz_im, hz), dex));
+                const float rz = __fmaf_rn(__fsub_rn(hx_jm, hx), dey[r], __fmul_rn(__fsub_rn(hy, hy_im), dex));
+                hxm[r] = hx;
+                hym[r] = hy;
+                if (!own[r]) continue;
+                float ex, ey, ez;
+                if constexpr (LEAN) {
+                    ex = __fmaf_rn(dt_eps0, rx, eo[r][0]);
+                    ey = __fmaf_rn(dt_eps0, ry, eo[r][1]);
+                    ez = __fmaf_rn(dt_eps0, rz, eo[r][2]);
+                } else {
+                    const int o = (rr0 + r) * F3T_BX + cc;
+                    ex = Exc[o];
+                    ey = Eyc[o];
+                    ez = Ezc[o];
+                    if (G.pl_on && (G.pl_axis == 0 ? i : (G.pl_axis == 1 ? j : k)) == G.pl_index) {
+                        // the plane source of this step (source_interactions before the E update)
+                        const double a = sp_get(G.pl_amp);
+                        if (a != 0.0) {
+                            const double add = __dmul_rn(G.pl_c_src, a);
+                            if (G.pl_comp == 0) ex = (float)__dadd_rn((double)ex, add);
+                            else if (G.pl_comp == 1) ey = (float)__dadd_rn((double)ey, add);
+                            else ez = (float)__dadd_rn((double)ez, add);
+                        }
+                    }
+                    if (bbc[r] && k >= G.bb0[2] && k <= G.bb1[2]) {
+                        const int b = (i - G.bb0[0]) + G.bbd[0] * ((j - G.bb0[1]) + G.bbd[1] * (k - G.bb0[2]));
+                        ex = f3t_media(ex, rx, 0, b, G);
+                        ey = f3t_media(ey, ry, 1, b, G);
+                        ez = f3t_media(ez, rz, 2, b, G);
+                    } else {
+                        ex = __fmaf_rn(dt_eps0, rx, ex);
+                        ey = __fmaf_rn(dt_eps0, ry, ey);
+                        ez = __fmaf_rn(dt_eps0, rz, ez);
+                    }
+                    if (lex >= 0) {   // mxll_3D_mod.f90:817-849
+                        const int p = lex + G.L2 * ((j - 1) + L.ny * (k - 1));
+                        const float b = G.bE[0][i], c = G.cE[0][i];
+                        const float v0 = f3t_psi(b, G.psiE[0][0][p], c, __fsub_rn(hz_im, hz));
+                        const float v1 = f3t_psi(b, G.psiE[0][1][p], c, __fsub_rn(hy, hy_im));
+                        G.psiE[0][0][p] = v0;
+                        G.psiE[0][1][p] = v1;
+                        ey = __fmaf_rn(dt_eps0, v0, ey);
+                        ez = __fmaf_rn(dt_eps0, v1, ez);
+                    }
+                    if (ley[r] >= 0) {   // :851-885
+                        const int p = (i - 1) + L.nx * (ley[r] + G.L2 * (k - 1));
+                        const float b = G.bE[1][j], c = G.cE[1][j];
+                        const float v0 = f3t_psi(b, G.psiE[1][0][p], c, __fsub_rn(hz, hz_jm));
+                        const float v1 = f3t_psi(b, G.psiE[1][1][p], c, __fsub_rn(hx_jm, hx));
+                        G.psiE[1][0][p] = v0;
+                        G.psiE[1][1][p] = v1;
+                        ex = __fmaf_rn(dt_eps0, v0, ex);
+                        ez = __fmaf_rn(dt_eps0, v1, ez);
+                    }
+                    if (lez >= 0) {   // :887-921
+                        const int p = (i - 1) + L.nx * ((j - 1) + L.ny * lez);
+                        const float b = z1.x, c = z1.y;
+                        const float v0 = f3t_psi(b, G.psiE[2][0][p], c, dhyk);
+                        const float v1 = f3t_psi(b, G.psiE[2][1][p], c, dhxk);
+                        G.psiE[2][0][p] = v0;
+                        G.psiE[2][1][p] = v1;
+                        ex = __fmaf_rn(dt_eps0, v0, ex);
+                        ey = __fmaf_rn(dt_eps0, v1, ey);
+                    }
                 }
-            }
-            if (bb_ij && k >= G.bb0[2] && k <= G.bb1[2]) {
-                const int b = (i - G.bb0[0]) + G.bbd[0] * ((j - G.bb0[1]) + G.bbd[1] * (k - G.bb0[2]));
-                ex = f3t_media(ex, rx, 0, b, G);
-                ey = f3t_media(ey, ry, 1, b, G);
-                ez = f3t_media(ez, rz, 2, b, G);
-            } else {
-                ex = ex + dt_eps0 * rx;
-                ey = ey + dt_eps0 * ry;
-                ez = ez + dt_eps0 * rz;
-            }
-            if (own) {
-                if (lex >= 0) {   // mxll_3D_mod.f90:817-849
-                    const int p = lex + G.L2 * ((j - 1) + L.ny * (k - 1));
-                    const float b = G.bE[0][i], c = G.cE[0][i];
-                    const float v0 = b * G.psiE[0][0][p] + c * (hz_im - hz);
-                    const float v1 = b * G.psiE[0][1][p] + c * (hy - hy_im);
-                    G.psiE[0][0][p] = v0;
-                    G.psiE[0][1][p] = v1;
-                    ey = ey + dt_eps0 * v0;
-                    ez = ez + dt_eps0 * v1;
-                }
-                if (ley >= 0) {   // :851-885
-                    const int p = (i - 1) + L.nx * (ley + G.L2 * (k - 1));
-                    const float b = G.bE[1][j], c = G.cE[1][j];
-                    const float v0 = b * G.psiE[1][0][p] + c * (hz - hz_jm);
-                    const float v1 = b * G.psiE[1][1][p] + c * (hx_jm - hx);
-                    G.psiE[1][0][p] = v0;
-                    G.psiE[1][1][p] = v1;
-                    ex = ex + dt_eps0 * v0;
-                    ez = ez + dt_eps0 * v1;
-                }
-                if (lez >= 0) {   // :887-921
-                    const int p = (i - 1) + L.nx * ((j - 1) + L.ny * lez);
-                    const float b = G.bE[2][k], c = G.cE[2][k];
-                    const float v0 = b * G.psiE[2][0][p] + c * (hym - hy);
-                    const float v1 = b * G.psiE[2][1][p] + c * (hx - hxm);
-                    G.psiE[2][0][p] = v0;
-                    G.psiE[2][1][p] = v1;
-                    ex = ex + dt_eps0 * v0;
-                    ey = ey + dt_eps0 * v1;
-                }
+                const int idx = col0 + L.px * r + (int)L.pz * k;
                 __stcs(A.out.f[0] + idx, ex);
                 __stcs(A.out.f[1] + idx, ey);
                 __stcs(A.out.f[2] + idx, ez);
             }
-            hxm = hx;
-            hym = hy;
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(&empty[sc]);   // plane k's slot is read
+        return false;
+    };
+
+    for (int k = k0; k <= k1; ++k) {
+        const int q = k - pa, sc = q % nd, sn = sc + 1 == nd ? 0 : sc + 1;
+        const float4 z0 = zc[2 * q], z1 = zc[2 * q + 1];
+        // the words of the next plane that come from HBM outside the staging (CPML psi, media
+        // bytes) are pulled into L1 now, so that their loads there do not stall the block
+        if (cw && k < k1) {
+            const float4 zn = zc[2 * (q + 1) + 1];
+            if (!lean_at(k + 1, zn)) {
+                const int lhzn = __float_as_int(zn.z), lezn = __float_as_int(zn.w);
+#pragma unroll
+                for (int r = 0; r < RPT; ++r) {
+                    if (!own[r]) continue;
+                    const int j = jb + r;
+                    if (lhx >= 0) {
+                        const int p = lhx + G.L2 * ((j - 1) + L.ny * k);
+                        f3t_prefetch(G.psiH[0][0] + p);
+                        f3t_prefetch(G.psiH[0][1] + p);
+                    }
+                    if (lex >= 0) {
+                        const int p = lex + G.L2 * ((j - 1) + L.ny * k);
+                        f3t_prefetch(G.psiE[0][0] + p);
+                        f3t_prefetch(G.psiE[0][1] + p);
+                    }
+                    if (lhy[r] >= 0) {
+                        const int p = (i - 1) + L.nx * (lhy[r] + G.L2 * k);
+                        f3t_prefetch(G.psiH[1][0] + p);
+                        f3t_prefetch(G.psiH[1][1] + p);
+                    }
+                    if (ley[r] >= 0) {
+                        const int p = (i - 1) + L.nx * (ley[r] + G.L2 * k);
+                        f3t_prefetch(G.psiE[1][0] + p);
+                        f3t_prefetch(G.psiE[1][1] + p);
+                    }
+                    if (lhzn >= 0) {
+                        const int p = (i - 1) + L.nx * ((j - 1) + L.ny * lhzn);
+                        f3t_prefetch(G.psiH[2][0] + p);
+                        f3t_prefetch(G.psiH[2][1] + p);
+                    }
+                    if (lezn >= 0) {
+                        const int p = (i - 1) + L.nx * ((j - 1) + L.ny * lezn);
+                        f3t_prefetch(G.psiE[2][0] + p);
+                        f3t_prefetch(G.psiE[2][1] + p);
+                    }
+                    if (bbc[r] && k + 1 >= G.bb0[2] && k + 1 <= G.bb1[2]) {
+                        const int b = (i - G.bb0[0]) + G.bbd[0] * ((j - G.bb0[1]) + G.bbd[1] * (k + 1 - G.bb0[2]));
+                        f3t_prefetch(G.mat[0] + b);
+                        f3t_prefetch(G.mat[1] + b);
+                        f3t_prefetch(G.mat[2] + b);
+                    }
+                }
+            }
+        }
+        // plane k's slot completed in the previous iteration (or before the loop); wait for k+1
+        fail |= !mbar_wait_bounded(&full[sn], (uint32_t)(((q + 1) / nd) & 1), F3T_WAIT_CYCLES);
+        const bool bad = lean_at(k, z1) ? plane(F3tForm<true>{}, k, sc, sn, z0, z1)
+                                        : plane(F3tForm<false>{}, k, sc, sn, z0, z1);
+        if (bad) {
+            if (threadIdx.x == 0) atomicOr(err, 1);
+            break;
+        }
     }
     // device loop: the last block to finish advances the step counter, so every block of this
     // pass reads the step's scalars (the plane source amplitude) before the counter moves; the
@@ -465,31 +627,29 @@ __device__ __forceinline__ void f3t_tile(const CUtensorMap *maps, const Fused3Ar
     }
 }
 
-// The grid's arguments in shared memory, after the pass's own layout: read from there, the
-// compiler does not hold the many pointers of the argument block in registers (which spilled).
-template <int TY>
+// The grid's arguments in shared memory, at the start of the block's layout: read from there,
+// the compiler does not hold the many pointers of the argument block in registers (which spilled).
 __device__ __forceinline__ void f3t_args_to_smem(const GridArgs<float> &G, const Fused3Args &A, unsigned char *smem)
 {
-    using S = F3tShape<TY>;
     const int *src = reinterpret_cast<const int *>(&G);
-    int *dst = reinterpret_cast<int *>(smem + S::SMEM);
+    int *dst = reinterpret_cast<int *>(smem);
     for (int w = threadIdx.x; w < (int)(sizeof(GridArgs<float>) / 4); w += blockDim.x) dst[w] = src[w];
     src = reinterpret_cast<const int *>(&A);
-    dst = reinterpret_cast<int *>(smem + S::SMEM + F3T_ARGB);
+    dst = reinterpret_cast<int *>(smem + F3T_ARGB);
     for (int w = threadIdx.x; w < (int)(sizeof(Fused3Args) / 4); w += blockDim.x) dst[w] = src[w];
     __syncthreads();
 }
 
+// nd: ring depth (the dynamic shared memory holds F3tShape<TY>::smem(nd) bytes)
 template <int TY>
-__global__ void __launch_bounds__(32 * (TY + 2), f3t_min_blocks<TY>())
-    k_fused3_tma(const __grid_constant__ F3tMaps M, Fused3Args A, GridArgs<float> G, int kch, int *err)
+__global__ void __launch_bounds__(F3tShape<TY>::THREADS, f3t_min_blocks<TY>())
+    k_fused3_tma(const __grid_constant__ F3tMaps M, Fused3Args A, GridArgs<float> G, int kch, int nd, int *err)
 {
-    using S = F3tShape<TY>;
     extern __shared__ __align__(1024) unsigned char f3_smem[];
-    f3t_args_to_smem<TY>(G, A, f3_smem);
-    f3t_tile<TY>(M.m, *reinterpret_cast<const Fused3Args *>(f3_smem + S::SMEM + F3T_ARGB),
-                 *reinterpret_cast<const GridArgs<float> *>(f3_smem + S::SMEM), (int)blockIdx.x, (int)blockIdx.y,
-                 (int)blockIdx.z, kch, gridDim.x * gridDim.y * gridDim.z, err, f3_smem);
+    f3t_args_to_smem(G, A, f3_smem);
+    f3t_tile<TY>(M.m, *reinterpret_cast<const Fused3Args *>(f3_smem + F3T_ARGB),
+                 *reinterpret_cast<const GridArgs<float> *>(f3_smem), (int)blockIdx.x, (int)blockIdx.y,
+                 (int)blockIdx.z, kch, nd, gridDim.x * gridDim.y * gridDim.z, err, f3_smem);
 }
 
 // ---- batched: the fused pass of several grids in one launch ----------------------------------
@@ -498,10 +658,9 @@ __global__ void __launch_bounds__(32 * (TY + 2), f3t_min_blocks<TY>())
 // copied into shared memory first.  Each grid computes exactly what its own k_fused3_tma does
 // (same f3t_tile arithmetic; every tile shape gives the same bits).
 template <int TY>
-__global__ void __launch_bounds__(32 * (TY + 2), f3t_min_blocks<TY>())
-    k_fused3_batch(const F3tBatchGrid *__restrict__ grids, int n, int *err)
+__global__ void __launch_bounds__(F3tShape<TY>::THREADS, f3t_min_blocks<TY>())
+    k_fused3_batch(const F3tBatchGrid *__restrict__ grids, int n, int nd, int *err)
 {
-    using S = F3tShape<TY>;
     extern __shared__ __align__(1024) unsigned char f3_smem[];
     const long long b = blockIdx.x;
     int lo = 0, hi = n - 1;                    // last grid with item0 <= b
@@ -511,12 +670,12 @@ __global__ void __launch_bounds__(32 * (TY + 2), f3t_min_blocks<TY>())
         else hi = mid - 1;
     }
     const F3tBatchGrid &B = grids[lo];
-    f3t_args_to_smem<TY>(B.G, B.A, f3_smem);
-    const GridArgs<float> *sG = reinterpret_cast<const GridArgs<float> *>(f3_smem + S::SMEM);
-    const Fused3Args *sA = reinterpret_cast<const Fused3Args *>(f3_smem + S::SMEM + F3T_ARGB);
+    f3t_args_to_smem(B.G, B.A, f3_smem);
+    const GridArgs<float> *sG = reinterpret_cast<const GridArgs<float> *>(f3_smem);
+    const Fused3Args *sA = reinterpret_cast<const Fused3Args *>(f3_smem + F3T_ARGB);
     const long long t = b - B.item0;
     const int bx = (int)(t % B.tx), by = (int)((t / B.tx) % B.ty), bz = (int)(t / ((long long)B.tx * B.ty));
-    f3t_tile<TY>(B.m, *sA, *sG, bx, by, bz, B.kch, (unsigned)((long long)B.tx * B.ty * B.tz), err, f3_smem);
+    f3t_tile<TY>(B.m, *sA, *sG, bx, by, bz, B.kch, nd, (unsigned)((long long)B.tx * B.ty * B.tz), err, f3_smem);
 }
 
 }  // namespace omx

@@ -203,8 +203,14 @@ struct F3tBatchGrid {
     long long item0;         // first block of this grid in the launch
     int tx, ty, tz, kch;     // tiles along x (32 cells), y (tile rows), z (kch planes)
 };
-// tile rows of a fused 3D form (form <= 0: the default, 8)
-inline int f3t_rows(int form) { return form == 16 ? 16 : 8; }
+constexpr int F3T_KMAX = 128;   // planes per block of the fused 3D pass at most
+// a fused 3D form is ring depth x 100 + tile rows (8 or 16); depth 0 and form <= 0 are defaults
+constexpr int F3T_RING_DEFAULT = 4;   // plane slots in a block's ring
+constexpr int F3T_RING_MAX = 16;
+inline int f3t_rows(int form) { return form > 0 && form % 100 == 16 ? 16 : 8; }
+inline int f3t_ring(int form) { return form >= 200 ? form / 100 : F3T_RING_DEFAULT; }
+// dynamic shared memory of a fused 3D block of this form (bytes)
+int f3t_smem_bytes(int form);
 bool encode_f3t_maps(F3tMaps *M, const FieldPtrs<float> &in, const Lay &L, int ty);
 // form: tile rows (8 or 16); kch: planes per block (0 = default); err: the device error word
 cudaError_t launch_fused3t(const F3tMaps &M, const Fused3Args &A, const GridArgs<float> &G, int form, int kch,

@@ -182,58 +182,67 @@ bool encode_f3t_maps(F3tMaps *M, const FieldPtrs<float> &in, const Lay &L, int t
     return true;
 }
 
-template <int TY>
-static cudaError_t launch_f3t(const F3tMaps &M, const Fused3Args &A, const GridArgs<float> &G, int kch, int *err,
-                              cudaStream_t s)
+// the largest dynamic shared memory set so far for a fused 3D kernel on this device (the
+// attribute grows with the ring depth a launch asks for)
+template <class K> static cudaError_t f3t_smem_attr(K kernel, int *have, int bytes)
 {
-    using S = F3tShape<TY>;
-    static bool attr[FZ_MAX_DEV] = {};
     int dev = 0;
     cudaGetDevice(&dev);
-    bool &a = attr[dev < FZ_MAX_DEV ? dev : 0];
-    if (!a) {
-        const cudaError_t e =
-            cudaFuncSetAttribute(k_fused3_tma<TY>, cudaFuncAttributeMaxDynamicSharedMemorySize, S::SMEM_BATCH);
-        if (e != cudaSuccess) return e;
-        a = true;
-    }
-    const int m = kch > 0 ? kch : 64;
+    int &h = have[dev < FZ_MAX_DEV ? dev : 0];
+    if (h >= bytes) return cudaSuccess;
+    const cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess) h = bytes;
+    return e;
+}
+
+template <int TY>
+static cudaError_t launch_f3t(const F3tMaps &M, const Fused3Args &A, const GridArgs<float> &G, int kch, int nd,
+                              int *err, cudaStream_t s)
+{
+    using S = F3tShape<TY>;
+    static int have[FZ_MAX_DEV] = {};
+    const int bytes = S::smem(nd);
+    const cudaError_t e = f3t_smem_attr(k_fused3_tma<TY>, have, bytes);
+    if (e != cudaSuccess) return e;
+    const int m = kch > 0 ? std::min(kch, F3T_KMAX) : 64;
     const dim3 g((unsigned)((G.L.nx + 31) / 32), (unsigned)((G.L.ny + TY - 1) / TY), (unsigned)((G.L.nz + m - 1) / m));
-    k_fused3_tma<TY><<<g, S::THREADS, S::SMEM_BATCH, s>>>(M, A, G, m, err);
+    k_fused3_tma<TY><<<g, S::THREADS, bytes, s>>>(M, A, G, m, nd, err);
     return cudaGetLastError();
+}
+
+int f3t_smem_bytes(int form)
+{
+    return f3t_rows(form) == 16 ? F3tShape<16>::smem(f3t_ring(form)) : F3tShape<8>::smem(f3t_ring(form));
 }
 
 cudaError_t launch_fused3t(const F3tMaps &M, const Fused3Args &A, const GridArgs<float> &G, int form, int kch,
                            int *err, void *s)
 {
-    if (f3t_rows(form) == 16) return launch_f3t<16>(M, A, G, kch, err, (cudaStream_t)s);
-    return launch_f3t<8>(M, A, G, kch, err, (cudaStream_t)s);
+    const int nd = f3t_ring(form);
+    if (f3t_rows(form) == 16) return launch_f3t<16>(M, A, G, kch, nd, err, (cudaStream_t)s);
+    return launch_f3t<8>(M, A, G, kch, nd, err, (cudaStream_t)s);
 }
 
 template <int TY>
-static cudaError_t launch_f3t_batch(const F3tBatchGrid *grids, int n, long long blocks, int *err, cudaStream_t s)
+static cudaError_t launch_f3t_batch(const F3tBatchGrid *grids, int n, long long blocks, int nd, int *err,
+                                    cudaStream_t s)
 {
     using S = F3tShape<TY>;
-    static bool attr[FZ_MAX_DEV] = {};
-    int dev = 0;
-    cudaGetDevice(&dev);
-    bool &a = attr[dev < FZ_MAX_DEV ? dev : 0];
-    if (!a) {
-        const cudaError_t e =
-            cudaFuncSetAttribute(k_fused3_batch<TY>, cudaFuncAttributeMaxDynamicSharedMemorySize, S::SMEM_BATCH);
-        if (e != cudaSuccess) return e;
-        a = true;
-    }
+    static int have[FZ_MAX_DEV] = {};
+    const int bytes = S::smem(nd);
+    const cudaError_t e = f3t_smem_attr(k_fused3_batch<TY>, have, bytes);
+    if (e != cudaSuccess) return e;
     if (n <= 0 || blocks <= 0) return cudaSuccess;
     if (blocks > 0x7fffffffLL) return cudaErrorInvalidValue;
-    k_fused3_batch<TY><<<(unsigned)blocks, S::THREADS, S::SMEM_BATCH, s>>>(grids, n, err);
+    k_fused3_batch<TY><<<(unsigned)blocks, S::THREADS, bytes, s>>>(grids, n, nd, err);
     return cudaGetLastError();
 }
 
 cudaError_t launch_fused3t_batch(const F3tBatchGrid *grids, int n, long long blocks, int form, int *err, void *s)
 {
-    if (f3t_rows(form) == 16) return launch_f3t_batch<16>(grids, n, blocks, err, (cudaStream_t)s);
-    return launch_f3t_batch<8>(grids, n, blocks, err, (cudaStream_t)s);
+    const int nd = f3t_ring(form);
+    if (f3t_rows(form) == 16) return launch_f3t_batch<16>(grids, n, blocks, nd, err, (cudaStream_t)s);
+    return launch_f3t_batch<8>(grids, n, blocks, nd, err, (cudaStream_t)s);
 }
 
 template <> void launch_batch3<float>(int pass, const BatchGrid<float> *g, int n, long long total, int kch,

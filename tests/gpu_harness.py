@@ -125,6 +125,28 @@ def trace_error(trace_g, trace_c):
     return float(np.max(np.abs(trace_g - trace_c) / scale))
 
 
+def point_trace_error(trace_g, trace_c, deck):
+    """Max detector-field error relative to the field at the detector's point: each detector's
+    max |gpu - oracle| over the run, divided by the largest |value| that any detector of the same
+    point and the same field kind (E: codes 1-3, H: codes 4-6) records.  A component that nearly
+    vanishes at its point (for example Hx beside a uniform Ex sheet, 1e-5 of the point's H) holds
+    only FP32 rounding of the point's field, which the per-component normalisation of
+    trace_error would amplify by that factor in any FP32 implementation."""
+    cols = []
+    for det in deck["detectors"]:
+        kind = 0 if det["field"] <= 3 else 1
+        for p in np.asarray(det["idx"]).reshape(-1, np.asarray(det["idx"]).shape[-1]):
+            cols.append((tuple(int(v) for v in p), kind))
+    assert len(cols) == trace_c.shape[1]
+    m = np.max(np.abs(trace_c), axis=0)
+    e = np.max(np.abs(trace_g - trace_c), axis=0)
+    scale = {}
+    for key, v in zip(cols, m):
+        scale[key] = max(scale.get(key, 0.0), float(v))
+    floor = max(FLOOR * float(np.max(m)), 1e-300)
+    return float(max(e[c] / max(scale[key], floor) for c, key in enumerate(cols)))
+
+
 def tmz_variant_deck(nx, ny, bx, by, with_media=True, src="plane"):
     """2D TMz scene for the FP32 fused step: Drude disc + dielectric block away from CPML,
     a plane or radial Ez source, a material q-group, point detectors."""

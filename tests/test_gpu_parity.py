@@ -16,7 +16,8 @@ import pytest
 
 import omx
 from omx import decks
-from gpu_harness import compare_fields, make_pair, run_both, step_loop, tmz_variant_deck, trace_error
+from gpu_harness import (compare_fields, make_pair, point_trace_error, run_both, step_loop, tmz_variant_deck,
+                         trace_error)
 
 pytestmark = pytest.mark.gpu
 
@@ -252,12 +253,19 @@ def _fused3_ran(g, deck):
 def test_fp32_fused3d(orc_mod, n, boundaries, src, steps):
     """The FP32 single-pass 3D step (k_fused3_tma, the default 3D FP32 form when x and y are not
     periodic): detector traces and fields within the FP32 bar of the FP64 oracle, through the
-    device loop and through the per-call sequence (omx_step_H deferred into the fused pass)."""
+    device loop and through the per-call sequence (omx_step_H deferred into the fused pass).
+
+    The detector bar is relative to the field at each detector's point (point_trace_error): the
+    scene puts E and H detectors of every component at each point, and some components vanish
+    there by symmetry (Hx beside the Ex sheet reaches 1e-5 of the point's H), so their own
+    maximum is no scale for an FP32 rounding error -- the plain two-pass FP32 step shows the same
+    per-component figure (2.7e-3 at such a detector) as this pass (3.0e-3)."""
     deck = fused3_deck(n, boundaries, src=src)
     for mode in ("run", "calls"):
         gpu, cpu, gg, cg, tc, tg = run_both(orc_mod, deck, steps, "fp32", mode, use_graph=True)
         assert np.max(np.abs(tc)) > 0
-        assert trace_error(tg, tc) <= FP32_TOL, (mode, trace_error(tg, tc))
+        err = point_trace_error(tg, tc, deck)
+        assert err <= FP32_TOL, (mode, err)
         assert compare_fields(gpu, cpu, deck) <= 10 * FP32_TOL
         for a, b in zip(gg, cg):
             ga, cb = a.read(), cpu.q_group_read(b)
