@@ -251,13 +251,16 @@ def rel_err(a, b):
     return float(np.max(np.abs(a - b) / scale))
 
 
-def error_statement(deck, nsteps):
-    """FP32 fused vs FP64 plain on the same deck over nsteps (every detector sampled every step)."""
+def error_statement(deck, nsteps, shape=None):
+    """The FP32 path (launch shape `shape`, as timed) vs FP64 plain on the same deck over nsteps
+    (every detector sampled every step)."""
     import numpy as np
 
     out = {}
     for prec in ("fp32", "fp64"):
         g, groups = build_gpu(deck, prec)
+        if prec == "fp32" and shape is not None:
+            g.set_launch_shape(shape)
         g.run(1, nsteps, deck["n_skip"], 1, use_graph=True)
         _, rec = g.drain_detectors(max_records=nsteps)
         dip = groups[0].read()["dipole"] if groups else None
@@ -506,7 +509,7 @@ def measure(args, dist, config, grid, K, W, err_steps, cpu_seconds):
         g64.drain_detectors()
         v64 = dist.world * cells * K / (ms64 / 1e3) / 1e9
         g64.kill()
-        field_err, dip_err = error_statement(deck, err_steps)
+        field_err, dip_err = error_statement(deck, err_steps, shape)
         plain = {"value": v64, "unit": "Gcell-updates/s", "ms_per_step": ms64 / K,
                  "emitter_steps_per_s": dist.world * ne * K / (ms64 / 1e3),
                  "speedup_fp32_over_fp64": value / v64,
@@ -530,6 +533,9 @@ def measure(args, dist, config, grid, K, W, err_steps, cpu_seconds):
             shape // 1000 % 100, shape % 1000, shape // 100000 or 4)
     elif dims == 2:
         shape_desc = "fused-kernel form %d (omx_autotune)" % shape
+    elif dims == 3:
+        shape_desc = "two half-step passes, %d planes marched per thread (omx_autotune: faster than the " \
+                     "fused pass at this size)" % shape
     else:
         shape_desc = "planes marched per thread %d (omx_autotune)" % shape
     return {

@@ -316,14 +316,18 @@ int omx_set_step_form(omx_ctx *ctx, int form);
  * per block -- 44 is the default), the fused FP32 3D pass's shape (ring depth x 100000 + tile rows
  * x 1000 + planes per block: ring depth 0 (the default, 4) or 2..16 staged planes, rows 8 or 16,
  * 1..128 planes; 8064 is the default) or the planes / rows each thread marches in the unfused
- * kernels.  The candidates run on the initial
+ * kernels.  For a 3D FP32 grid on OMX_STEP_DEFAULT the two half-step passes compete as well
+ * (reported as planes per thread, below 1000); when they win, the grid steps with them from then
+ * on, as after omx_set_step_form(OMX_STEP_TWO_PASS).  The candidates run on the initial
  * all-zero fields, which every kernel maps to zero, so the simulation state is unchanged: call it
  * after the grid is configured and before the first step or omx_write_field (OMX_ERR_STATE
  * otherwise); configuration calls are closed afterwards, as after a first step.  *choice (may
  * be NULL) receives the chosen shape. */
 int omx_autotune(omx_ctx *ctx, int reps, int *choice);
 /* Sets the launch shape directly (a value omx_autotune reported, e.g. for a grid of the same shape
- * tuned earlier); no counterpart in the reference.  Every shape gives the same results bit for bit. */
+ * tuned earlier); no counterpart in the reference.  Every shape of one step form gives the same
+ * results bit for bit; on a 3D FP32 grid a shape below 1000 switches to the two half-step passes,
+ * whose FP32 results differ from the single pass's by rounding. */
 int omx_set_launch_shape(omx_ctx *ctx, int shape);
 
 /* ---- batched multi-grid runs (no counterpart in the reference: it runs one grid per process) -

@@ -212,6 +212,7 @@ struct omx_ctx {
     // and the fused-kernel form (-1 = default)
     int march = 0;
     int fused_form = -1;
+    int march_two_pass = 0;   // autotune: the two-pass candidate of a 3D FP32 fused-eligible grid is selected
     int tq_step_old = 0;
     double t_skip = 0.0;
     // run tables
@@ -222,6 +223,10 @@ struct omx_ctx {
     // stream's kernels read their step's scalars through their own counter
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    // the fused 3D pass's general runs (latency-bound) run on f3aux beside the lean runs
+    // (bandwidth-bound) of the same step; ev_f3a / ev_f3b fork and join them
+    cudaStream_t f3aux = nullptr;
+    cudaEvent_t ev_f3a = nullptr, ev_f3b = nullptr;
     DevBuf<int> d_step2;
     // a one-step omx_run leaves its side-stream work running (ev_join marks its end) so that the
     // next call's fused pass overlaps it; every other entry point first orders the main stream
@@ -290,6 +295,12 @@ struct omx_ctx {
     bool fold3 = false;         // the fused 3D pass adds the single plane source (fold3_of)
     F3tMaps f3maps[2][2];       // tensor maps of the fused 3D pass: [in set][tile rows 8 / 16]
     const void *f3key[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};   // Ex buffer they were made for
+    // runs {bx, by, k0, k1} of the fused 3D pass (general runs first, then lean ones) for the
+    // tile rows / planes per block / plane-source setting in f3plan_key
+    DevBuf<int4> f3items;
+    int f3n_gen = 0, f3n_lean = 0;
+    long long f3plan_key = -1;
+    std::vector<short> hl[3][2];   // host copies of the CPML layer tables (lE, lH per axis)
     int step_form = OMX_STEP_DEFAULT;   // omx_set_step_form; a batch sets TWO_PASS on its members
     int *run_step = nullptr;    // device step counter while omx_run issues a step sequence
     std::string err;
@@ -460,6 +471,8 @@ template <class R> void upload_axis_tables(omx_ctx *c)
         tb[5].upload(cH);
         c->tl[a][0].upload(lE);
         c->tl[a][1].upload(lH);
+        c->hl[a][0] = lE;
+        c->hl[a][1] = lH;
         if (!exact && a == 1) {
             // packed y coefficients of the fused FP32 TMz kernel: (den_h, den_e, bH, cH) and
             // (bE, cE, H layer, E layer) per row, the layers as int bit patterns
@@ -971,6 +984,8 @@ bool plane_fold_eligible(const omx_ctx *c)
     return true;
 }
 
+void f3t_plan(omx_ctx *c);
+
 void prepare(omx_ctx *c)
 {
     const bool recheck = c->j_dirty || c->fused_dirty;
@@ -987,6 +1002,7 @@ void prepare(omx_ctx *c)
         c->plane_fold = plane_fold_eligible(c);
         c->fold3 = c->fused_ok && fold3_of(c);
     }
+    if (c->fused_ok && c->fp32 && c->dims == 3) f3t_plan(c);
     if (c->fused_ok && !c->ff2[2].p) {
         for (int q = 0; q < 6; ++q)
             if (c->field_used[q]) c->ff2[q].alloc(c->felems);
@@ -1138,6 +1154,60 @@ template <class R> void do_sample(omx_ctx *c, StepParam slot, StepParam time)
     c->launches++;
 }
 
+// The runs of the fused 3D pass: each tile's planes 1..nz split where the plane form changes
+// (the device's test, restated: a CPML slab of x or y at the tile's own or halo cells, a z slab at
+// the plane, a media-box cell of the tile's part of the plane, the folded plane source), then
+// into pieces of at most kch planes.  General runs come first in the list.
+void f3t_plan(omx_ctx *c)
+{
+    const int ty = f3t_rows(c->fused_form);
+    const int kch = c->march > 0 ? std::min(c->march, F3T_KMAX) : 64;
+    const bool pl = c->fold3 && !c->sources.empty();
+    const long long key = ((long long)ty * 1000 + kch) * 2 + (pl ? 1 : 0);
+    if (c->f3plan_key == key) return;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    ck(cudaStreamIsCapturing(c->stream, &cs), "capture status");
+    if (cs != cudaStreamCaptureStatusNone)
+        throw Fail{OMX_ERR_STATE, "fused 3D pass: its run list changed during a stream capture"};
+    const int nx = c->n[0], ny = c->n[1], nz = c->n[2];
+    int pl_axis = -1, pl_index = -1;
+    if (pl) {
+        const SourceRec &S = *c->sources[0];
+        pl_axis = S.pd.plane_axis - 1;
+        pl_index = S.pd.plane_index;
+    }
+    auto slab = [&](int a, int p) { return c->hl[a][0][p] >= 0 || c->hl[a][1][p] >= 0; };
+    const bool box = c->bb1[0] >= c->bb0[0] && c->bb1[1] >= c->bb0[1] && c->bb1[2] >= c->bb0[2];
+    std::vector<int4> gen, lean;
+    std::vector<char> lk(nz + 1);
+    for (int by = 0; by * ty < ny; ++by)
+        for (int bx = 0; bx * 32 < nx; ++bx) {
+            const int i0 = 1 + 32 * bx, j0 = 1 + ty * by;
+            bool xy = false;
+            for (int i = std::max(1, i0 - 1); i <= std::min(nx, i0 + 31); ++i) xy = xy || slab(0, i);
+            for (int j = std::max(1, j0 - 1); j <= std::min(ny, j0 + ty - 1); ++j) xy = xy || slab(1, j);
+            const bool mb = box && c->bb0[0] <= i0 + 31 && c->bb1[0] >= i0 && c->bb0[1] <= j0 + ty - 1 &&
+                            c->bb1[1] >= j0;
+            const bool plxy = (pl_axis == 0 && pl_index >= i0 && pl_index <= i0 + 31) ||
+                              (pl_axis == 1 && pl_index >= j0 && pl_index <= j0 + ty - 1);
+            for (int k = 1; k <= nz; ++k)
+                lk[k] = !xy && !plxy && !slab(2, k) && !(pl_axis == 2 && k == pl_index) &&
+                        !(mb && k >= c->bb0[2] && k <= c->bb1[2]);
+            for (int k = 1; k <= nz;) {
+                int e = k;
+                while (e < nz && lk[e + 1] == lk[k] && e - k + 1 < kch) ++e;
+                (lk[k] ? lean : gen).push_back(make_int4(bx, by, k, e));
+                k = e + 1;
+            }
+        }
+    std::vector<int4> all(gen);
+    all.insert(all.end(), lean.begin(), lean.end());
+    c->f3items.upload(all);
+    c->f3n_gen = (int)gen.size();
+    c->f3n_lean = (int)lean.size();
+    c->f3plan_key = key;
+}
+
 // One FP32 fused step: the H+E pass from the current buffer set into the other.  2D TMz: then
 // the dispersive cells (ade); 3D: the dispersive cells are inside the pass, and so is the single
 // plane source when fold3 holds (`plane`: its amplitude).  The caller adds the other sources and
@@ -1176,8 +1246,30 @@ template <> void fused_step<float>(omx_ctx *c, bool ade, const StepParam *plane)
                 throw Fail{OMX_ERR_CUDA, "cuTensorMapEncodeTiled failed for the fused 3D pass"};
             c->f3key[in][t] = Fin.f[0];
         }
-        ck(launch_fused3t(c->f3maps[in][t], A, G, c->fused_form, c->march, c->d_err.p, c->stream), "fused 3D launch");
-        c->launches += 1;
+        f3t_plan(c);
+        const int4 *items = c->f3items.p;
+        // general runs (CPML, media, plane source): new H on f3aux beside the lean runs' fused
+        // launch on the stream, then new E on the stream once both have written their new H; the E
+        // launch (the pass's only reader of the step's scalars) advances the device-loop step
+        // counter, or the lean launch when there are no general runs
+        const int ng = c->f3n_gen, nl = c->f3n_lean;
+        GridArgs<float> Gq = G;
+        Gq.step_inc = nullptr;
+        Gq.step_done = nullptr;
+        if (ng > 0) {
+            ck(cudaEventRecord(c->ev_f3a, c->stream), "fork");
+            ck(cudaStreamWaitEvent(c->f3aux, c->ev_f3a, 0), "fork");
+            ck(launch_fused3t_general(A, Gq, c->fused_form, items, ng, false, c->f3aux), "fused 3D launch");
+            ck(cudaEventRecord(c->ev_f3b, c->f3aux), "join");
+        }
+        ck(launch_fused3t_lean(c->f3maps[in][t], A, ng > 0 ? Gq : G, c->fused_form, items + ng, nl, c->d_err.p,
+                               c->stream),
+           "fused 3D launch");
+        if (ng > 0) {
+            ck(cudaStreamWaitEvent(c->stream, c->ev_f3b, 0), "join");
+            ck(launch_fused3t_general(A, G, c->fused_form, items, ng, true, c->stream), "fused 3D launch");
+        }
+        c->launches += (ng > 0 ? 2 : 0) + (nl > 0 ? 1 : 0);
         c->cur = out;
         return;
     }
@@ -1293,9 +1385,13 @@ void sync_checked(omx_ctx *c, const char *what)
     ck(cudaMemcpyAsync(c->h_err, c->d_err.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream), what);
     ck(cudaStreamSynchronize(c->stream), what);
     if (*c->h_err) {
+        const int e = *c->h_err;
         *c->h_err = 0;
         ck(cudaMemsetAsync(c->d_err.p, 0, sizeof(int), c->stream), what);
-        throw Fail{OMX_ERR_CUDA, "fused TMz kernel: a bulk-copy wait ran out; the fields of that step are invalid"};
+        if (e & 4)
+            throw Fail{OMX_ERR_CUDA, "fused 3D pass: a plane planned as lean needed CPML, media or a source; the "
+                                     "fields of that step are invalid"};
+        throw Fail{OMX_ERR_CUDA, "fused kernel: a bulk-copy wait ran out; the fields of that step are invalid"};
     }
 }
 
@@ -1639,9 +1735,13 @@ template <class R> void run_impl(omx_ctx *c, int tt0, int nsteps, int n_skip, in
 void apply_shape(omx_ctx *c, int v)
 {
     const bool fused = c->fp32 && fused_eligible(c);
+    c->march_two_pass = 0;
     if (v >= 1000) {
         c->fused_form = v / 1000;
         c->march = v % 1000;
+    } else if (fused && c->dims == 3) {
+        c->march = v;                 // the two half-step passes, v planes per thread
+        c->march_two_pass = 1;
     } else if (fused) {
         c->fused_form = v;
     } else {
@@ -1655,17 +1755,23 @@ void apply_shape(omx_ctx *c, int v)
 template <class R> int autotune_impl(omx_ctx *c, int reps)
 {
     const bool fused = std::is_same<R, float>::value && c->fused_ok;
+    // 3D FP32 with the fused pass eligible: the two half-step passes compete too (shapes below
+    // 1000: planes marched per thread); where their in-place buffers fit in L2 (small grids) they
+    // can beat the single pass, whose ping-pong sets take twice the room
+    const bool both = fused && c->dims == 3 && c->step_form == OMX_STEP_DEFAULT;
     std::vector<int> cand;
     if (fused && c->dims == 3) {
         // fused 3D pass: (ring depth x 100 + tile rows) x 1000 + planes per block
         int dev = 0, optin = 0;
         ck(cudaGetDevice(&dev), "device");
         ck(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev), "device");
-        for (int ring : {0, 6, 8})
+        for (int ring : {0, 3, 6})
             for (int ty : {8, 16})
                 for (int kch : {8, 16, 32, 64, 128})
                     if (kch <= c->n[2] * 2 && f3t_smem_bytes(ring * 100 + ty) <= optin)
                         cand.push_back((ring * 100 + ty) * 1000 + kch);
+        if (both)
+            for (int m : {4, 8, 16, 32}) cand.push_back(m);
     } else if (fused) {
         cand = {0, 4, 5, 6, 8, 14, 15, 16, 24, 25, 34, 36, 44, 45};
     } else if (c->dims == 3) {
@@ -1677,7 +1783,7 @@ template <class R> int autotune_impl(omx_ctx *c, int reps)
     }
     auto select = [&](int v) { apply_shape(c, v); };
     auto once = [&]() {
-        if (fused) {
+        if (fused && c->march_two_pass == 0) {
             fused_step<R>(c);
         } else {
             do_H<R>(c);
@@ -1712,6 +1818,14 @@ template <class R> int autotune_impl(omx_ctx *c, int reps)
         }
     select(pick);
     ck(cudaPeekAtLastError(), "autotune");
+    if (both && pick < 1000) {
+        // the two half-step passes won: the grid steps with them from now on
+        c->step_form = OMX_STEP_TWO_PASS;
+        c->fused_dirty = true;
+        c->march_two_pass = 0;
+        c->march = pick;
+        prepare(c);
+    }
     return pick;
 }
 
@@ -1838,6 +1952,9 @@ int omx_create(const omx_grid_desc *d, omx_ctx **out)
         ck(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking), "stream");
         ck(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming), "event");
         ck(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming), "event");
+        ck(cudaStreamCreateWithFlags(&c->f3aux, cudaStreamNonBlocking), "stream");
+        ck(cudaEventCreateWithFlags(&c->ev_f3a, cudaEventDisableTiming), "event");
+        ck(cudaEventCreateWithFlags(&c->ev_f3b, cudaEventDisableTiming), "event");
         // layout
         const int align = c->fp32 ? 32 : 16;
         Lay &L = c->L;
@@ -1851,7 +1968,11 @@ int omx_create(const omx_grid_desc *d, omx_ctx **out)
             L.pz = 0;
             c->felems = (size_t)(L.off + L.nx + 2 + align);
         } else {
-            L.px = ((L.nx + 2 + align - 1) / align) * align;
+            // FP32 3D: the fused pass's tensor maps view each row from 3 elements before cell 0
+            // (its tiles' boxes start on 16-byte boundaries) and must reach the ghost cell nx+1,
+            // so the row holds nx + 5 elements at least
+            const int row = (c->dims == 3 && c->fp32) ? L.nx + 5 : L.nx + 2;
+            L.px = ((row + align - 1) / align) * align;
             L.pz = (c->dims == 3) ? (long long)L.px * (L.ny + 2) : 0;
             const long long rows = (long long)(L.ny + 2) * (c->dims == 3 ? (L.nz + 2) : 1);
             c->felems = (size_t)(L.off + (long long)L.px * rows + align);
@@ -1921,6 +2042,12 @@ int omx_destroy(omx_ctx *c)
         cudaStreamSynchronize(c->side);
         cudaStreamDestroy(c->side);
     }
+    if (c->f3aux) {
+        cudaStreamSynchronize(c->f3aux);
+        cudaStreamDestroy(c->f3aux);
+    }
+    if (c->ev_f3a) cudaEventDestroy(c->ev_f3a);
+    if (c->ev_f3b) cudaEventDestroy(c->ev_f3b);
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     if (c->ev_join) cudaEventDestroy(c->ev_join);
     if (c->ev_drain) cudaEventDestroy(c->ev_drain);
@@ -2854,7 +2981,12 @@ int omx_set_launch_shape(omx_ctx *c, int shape)
     OMX_API_BEGIN
     join_side(c);
     req(c && shape >= 1, "bad argument");
-    if (c->dims == 3 && c->fp32 && fused_eligible(c)) {
+    if (c->dims == 3 && c->fp32 && fused_eligible(c) && shape < 1000) {
+        // 3D FP32: a shape below 1000 selects the two half-step passes (v planes per thread)
+        c->step_form = OMX_STEP_TWO_PASS;
+        c->fused_dirty = true;
+        c->march = shape;
+    } else if (c->dims == 3 && c->fp32 && fused_eligible(c)) {
         const int form = shape / 1000, rows = form % 100, ring = form / 100;
         req((rows == 8 || rows == 16) && (ring == 0 || (ring >= 2 && ring <= F3T_RING_MAX)) && shape % 1000 >= 1 &&
                 shape % 1000 <= F3T_KMAX,

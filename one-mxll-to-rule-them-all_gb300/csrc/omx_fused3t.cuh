@@ -42,6 +42,7 @@ namespace omx {
 
 constexpr int F3T_BX = 40;    // staged box width: x from i0-4 (16-byte aligned) to i0+35
 constexpr long long F3T_WAIT_CYCLES = 2000000000LL;   // about one second at the SM clock
+constexpr int F3T_PF = 2;     // planes ahead whose CPML psi and media words are prefetched into L1
 
 // bytes reserved for the copy of a grid's GridArgs in the kernels' shared memory
 constexpr int F3T_ARGB = (int)((sizeof(GridArgs<float>) + 15) / 16 * 16);
@@ -99,66 +100,85 @@ __device__ __forceinline__ float f3t_psi(float b, float psi, float c, float d)
     return __fmaf_rn(b, psi, __fmul_rn(c, d));
 }
 
+// The in-set H psi of one cell at its psi indices px, py, pz (-1: the cell lies in no slab of that
+// axis; all zero when on = false): every load is issued before any of them is used, so that a cell
+// in two or three slabs waits for memory once.  The in set is read-only during the pass (the
+// owner writes the out set).
+struct F3tPsiH {
+    float x0, x1, y0, y1, z0, z1;
+};
+__device__ __forceinline__ F3tPsiH f3t_load_psiH(const GridArgs<float> &G, int px, int py, int pz, bool on)
+{
+    F3tPsiH q{0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (!on) return q;
+    if (px >= 0) {
+        q.x0 = __ldg(G.psiH[0][0] + px);
+        q.x1 = __ldg(G.psiH[0][1] + px);
+    }
+    if (py >= 0) {
+        q.y0 = __ldg(G.psiH[1][0] + py);
+        q.y1 = __ldg(G.psiH[1][1] + py);
+    }
+    if (pz >= 0) {
+        q.z0 = __ldg(G.psiH[2][0] + pz);
+        q.z1 = __ldg(G.psiH[2][1] + pz);
+    }
+    return q;
+}
+
 // New H components (h3_tile's expressions, the CPML faces in the reference's order) from the
-// staged neighbourhood.  pm: 0 no psi access (a cell past the grid edge, whose value nobody
-// uses), 1 read the in set's psi (a halo cell, or the plane before the first), 2 read and write
-// the out set's psi (the owner).
+// staged neighbourhood and the cell's in-set psi (f3t_load_psiH) at psi indices px / py / pz (-1:
+// no slab).  i, j, kk: the cell's indices for the CPML coefficients of the faces it uses.  pm: 0
+// no psi (a cell past the grid edge, whose value nobody uses, or a plane of the lean form), 1
+// psi read only (a halo cell, or the plane before the first), 2 the new psi written to the out
+// set (the owner).
 __device__ __forceinline__ float f3t_hx(float hx, float ez_c, float ez_jp, float ey_c, float ey_kp, float dhy,
-                                        float dhz, float dt_mu0, int ly, int lz, const GridArgs<float> &G,
-                                        const Fused3Args &A, int i, int j, int kk, int pm)
+                                        float dhz, float dt_mu0, const GridArgs<float> &G, const Fused3Args &A,
+                                        int j, int kk, int pm, int py, int pz, float psy, float psz)
 {
     float h = __fmaf_rn(dt_mu0, __fmaf_rn(ey_kp - ey_c, dhz, __fmul_rn(ez_c - ez_jp, dhy)), hx);
-    const Lay &L = G.L;
-    if (ly >= 0 && pm) {   // mxll_3D_mod.f90:622-657
-        const int p = (i - 1) + L.nx * (ly + G.L2 * (kk - 1));
-        const float v = f3t_psi(G.bH[1][j], G.psiH[1][0][p], G.cH[1][j], ez_c - ez_jp);
-        if (pm == 2) A.psiH_out[1][0][p] = v;
+    if (py >= 0 && pm) {   // mxll_3D_mod.f90:622-657
+        const float v = f3t_psi(__ldg(G.bH[1] + j), psy, __ldg(G.cH[1] + j), ez_c - ez_jp);
+        if (pm == 2) A.psiH_out[1][0][py] = v;
         h = __fmaf_rn(dt_mu0, v, h);
     }
-    if (lz >= 0 && pm) {   // :659-694
-        const int p = (i - 1) + L.nx * ((j - 1) + L.ny * lz);
-        const float v = f3t_psi(G.bH[2][kk], G.psiH[2][0][p], G.cH[2][kk], ey_kp - ey_c);
-        if (pm == 2) A.psiH_out[2][0][p] = v;
+    if (pz >= 0 && pm) {   // :659-694
+        const float v = f3t_psi(__ldg(G.bH[2] + kk), psz, __ldg(G.cH[2] + kk), ey_kp - ey_c);
+        if (pm == 2) A.psiH_out[2][0][pz] = v;
         h = __fmaf_rn(dt_mu0, v, h);
     }
     return h;
 }
 __device__ __forceinline__ float f3t_hy(float hy, float ez_c, float ez_ip, float ex_c, float ex_kp, float dhx,
-                                        float dhz, float dt_mu0, int lx, int lz, const GridArgs<float> &G,
-                                        const Fused3Args &A, int i, int j, int kk, int pm)
+                                        float dhz, float dt_mu0, const GridArgs<float> &G, const Fused3Args &A,
+                                        int i, int kk, int pm, int px, int pz, float psx, float psz)
 {
     float h = __fmaf_rn(dt_mu0, __fmaf_rn(ex_c - ex_kp, dhz, __fmul_rn(ez_ip - ez_c, dhx)), hy);
-    const Lay &L = G.L;
-    if (lx >= 0 && pm) {   // mxll_3D_mod.f90:585-620
-        const int p = lx + G.L2 * ((j - 1) + L.ny * (kk - 1));
-        const float v = f3t_psi(G.bH[0][i], G.psiH[0][0][p], G.cH[0][i], ez_ip - ez_c);
-        if (pm == 2) A.psiH_out[0][0][p] = v;
+    if (px >= 0 && pm) {   // mxll_3D_mod.f90:585-620
+        const float v = f3t_psi(__ldg(G.bH[0] + i), psx, __ldg(G.cH[0] + i), ez_ip - ez_c);
+        if (pm == 2) A.psiH_out[0][0][px] = v;
         h = __fmaf_rn(dt_mu0, v, h);
     }
-    if (lz >= 0 && pm) {
-        const int p = (i - 1) + L.nx * ((j - 1) + L.ny * lz);
-        const float v = f3t_psi(G.bH[2][kk], G.psiH[2][1][p], G.cH[2][kk], ex_c - ex_kp);
-        if (pm == 2) A.psiH_out[2][1][p] = v;
+    if (pz >= 0 && pm) {
+        const float v = f3t_psi(__ldg(G.bH[2] + kk), psz, __ldg(G.cH[2] + kk), ex_c - ex_kp);
+        if (pm == 2) A.psiH_out[2][1][pz] = v;
         h = __fmaf_rn(dt_mu0, v, h);
     }
     return h;
 }
 __device__ __forceinline__ float f3t_hz(float hz, float ey_c, float ey_ip, float ex_c, float ex_jp, float dhx,
-                                        float dhy, float dt_mu0, int lx, int ly, const GridArgs<float> &G,
-                                        const Fused3Args &A, int i, int j, int kk, int pm)
+                                        float dhy, float dt_mu0, const GridArgs<float> &G, const Fused3Args &A,
+                                        int i, int j, int pm, int px, int py, float psx, float psy)
 {
     float h = __fmaf_rn(dt_mu0, __fmaf_rn(ex_jp - ex_c, dhy, __fmul_rn(ey_c - ey_ip, dhx)), hz);
-    const Lay &L = G.L;
-    if (lx >= 0 && pm) {
-        const int p = lx + G.L2 * ((j - 1) + L.ny * (kk - 1));
-        const float v = f3t_psi(G.bH[0][i], G.psiH[0][1][p], G.cH[0][i], ey_c - ey_ip);
-        if (pm == 2) A.psiH_out[0][1][p] = v;
+    if (px >= 0 && pm) {
+        const float v = f3t_psi(__ldg(G.bH[0] + i), psx, __ldg(G.cH[0] + i), ey_c - ey_ip);
+        if (pm == 2) A.psiH_out[0][1][px] = v;
         h = __fmaf_rn(dt_mu0, v, h);
     }
-    if (ly >= 0 && pm) {
-        const int p = (i - 1) + L.nx * (ly + G.L2 * (kk - 1));
-        const float v = f3t_psi(G.bH[1][j], G.psiH[1][1][p], G.cH[1][j], ex_jp - ex_c);
-        if (pm == 2) A.psiH_out[1][1][p] = v;
+    if (py >= 0 && pm) {
+        const float v = f3t_psi(__ldg(G.bH[1] + j), psy, __ldg(G.cH[1] + j), ex_jp - ex_c);
+        if (pm == 2) A.psiH_out[1][1][py] = v;
         h = __fmaf_rn(dt_mu0, v, h);
     }
     return h;
@@ -205,7 +225,93 @@ __device__ __forceinline__ float f3t_media(float e, float rot, int c, int b, con
     return f3t_ade(e, rot, cl.type, G.med + cl.medium, G.ade + (long long)c * (2 + 2 * G.P) * G.bbV + b, G.bbV, G.P);
 }
 
-template <int TY> constexpr int f3t_min_blocks() { return TY == 8 ? 3 : 2; }
+// The curl of the new H at an owned cell (the E update's right-hand side per unit dt_eps0), every
+// operation rounded explicitly so that every kernel and tile shape gives a cell the same bits.
+// hxm, hym: new Hx, Hy of plane k-1; dhxk, dhyk: their plane differences (the z-face psi's input).
+__device__ __forceinline__ void f3t_curl(float hx, float hy, float hz, float hz_im, float hy_im, float hz_jm,
+                                         float hx_jm, float hxm, float hym, float dex, float dey, float dez, float &rx,
+                                         float &ry, float &rz, float &dhxk, float &dhyk)
+{
+    dhyk = __fsub_rn(hym, hy);
+    dhxk = __fsub_rn(hx, hxm);
+    rx = __fmaf_rn(dhyk, dez, __fmul_rn(__fsub_rn(hz, hz_jm), dey));
+    ry = __fmaf_rn(dhxk, dez, __fmul_rn(__fsub_rn(hz_im, hz), dex));
+    rz = __fmaf_rn(__fsub_rn(hx_jm, hx), dey, __fmul_rn(__fsub_rn(hy, hy_im), dex));
+}
+
+// New E of an owned cell (i, j, k) in the general form, from its old E (in ex, ey, ez) and the
+// curl of the new H: the plane source of the step, the media-box update (plain classes or the
+// ADE) or the vacuum update, then the CPML E psi of the x, y and z faces in the reference's order
+// (mxll_3D_mod.f90:740-921).  pe0, pe1, pe2: the cell's E psi indices (-1: no slab; in place: each
+// word is read and written by this thread only, all of them requested first); bz, cz: the z
+// face's coefficients of plane k; bbc: (i, j) lies in the media box's x-y extent.
+__device__ __forceinline__ void f3t_e_general(float &ex, float &ey, float &ez, float rx, float ry, float rz, float dhxk,
+                                              float dhyk, float hx, float hy, float hz, float hz_im, float hy_im,
+                                              float hz_jm, float hx_jm, int i, int j, int k, int pe0, int pe1, int pe2,
+                                              float bz, float cz, bool bbc, float dt_eps0, const GridArgs<float> &G)
+{
+    float qe[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (pe0 >= 0) {
+        qe[0] = __ldg(G.psiE[0][0] + pe0);
+        qe[1] = __ldg(G.psiE[0][1] + pe0);
+    }
+    if (pe1 >= 0) {
+        qe[2] = __ldg(G.psiE[1][0] + pe1);
+        qe[3] = __ldg(G.psiE[1][1] + pe1);
+    }
+    if (pe2 >= 0) {
+        qe[4] = __ldg(G.psiE[2][0] + pe2);
+        qe[5] = __ldg(G.psiE[2][1] + pe2);
+    }
+    if (G.pl_on && (G.pl_axis == 0 ? i : (G.pl_axis == 1 ? j : k)) == G.pl_index) {
+        // the plane source of this step (source_interactions before the E update)
+        const double a = sp_get(G.pl_amp);
+        if (a != 0.0) {
+            const double add = __dmul_rn(G.pl_c_src, a);
+            if (G.pl_comp == 0) ex = (float)__dadd_rn((double)ex, add);
+            else if (G.pl_comp == 1) ey = (float)__dadd_rn((double)ey, add);
+            else ez = (float)__dadd_rn((double)ez, add);
+        }
+    }
+    if (bbc && k >= G.bb0[2] && k <= G.bb1[2]) {
+        const int b = (i - G.bb0[0]) + G.bbd[0] * ((j - G.bb0[1]) + G.bbd[1] * (k - G.bb0[2]));
+        ex = f3t_media(ex, rx, 0, b, G);
+        ey = f3t_media(ey, ry, 1, b, G);
+        ez = f3t_media(ez, rz, 2, b, G);
+    } else {
+        ex = __fmaf_rn(dt_eps0, rx, ex);
+        ey = __fmaf_rn(dt_eps0, ry, ey);
+        ez = __fmaf_rn(dt_eps0, rz, ez);
+    }
+    if (pe0 >= 0) {   // mxll_3D_mod.f90:817-849
+        const float b = __ldg(G.bE[0] + i), c = __ldg(G.cE[0] + i);
+        const float v0 = f3t_psi(b, qe[0], c, __fsub_rn(hz_im, hz));
+        const float v1 = f3t_psi(b, qe[1], c, __fsub_rn(hy, hy_im));
+        G.psiE[0][0][pe0] = v0;
+        G.psiE[0][1][pe0] = v1;
+        ey = __fmaf_rn(dt_eps0, v0, ey);
+        ez = __fmaf_rn(dt_eps0, v1, ez);
+    }
+    if (pe1 >= 0) {   // :851-885
+        const float b = __ldg(G.bE[1] + j), c = __ldg(G.cE[1] + j);
+        const float v0 = f3t_psi(b, qe[2], c, __fsub_rn(hz, hz_jm));
+        const float v1 = f3t_psi(b, qe[3], c, __fsub_rn(hx_jm, hx));
+        G.psiE[1][0][pe1] = v0;
+        G.psiE[1][1][pe1] = v1;
+        ex = __fmaf_rn(dt_eps0, v0, ex);
+        ez = __fmaf_rn(dt_eps0, v1, ez);
+    }
+    if (pe2 >= 0) {   // :887-921
+        const float v0 = f3t_psi(bz, qe[4], cz, dhyk);
+        const float v1 = f3t_psi(bz, qe[5], cz, dhxk);
+        G.psiE[2][0][pe2] = v0;
+        G.psiE[2][1][pe2] = v1;
+        ex = __fmaf_rn(dt_eps0, v0, ex);
+        ey = __fmaf_rn(dt_eps0, v1, ey);
+    }
+}
+
+template <int TY> constexpr int f3t_min_blocks() { return 2; }
 
 // the form a plane is computed in: lean (no CPML psi, media or plane source at the block's cells
 // of the plane) or general
@@ -219,13 +325,19 @@ __device__ __forceinline__ void f3t_prefetch(const void *p)
     asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
 }
 
-// One block's work: tile (bx, by) of 32 x TY columns over plane chunk bz of one grid.  maps: the
+// How a launch chooses the form of each plane: per plane (F3T_MIXED, the batched pass) or every
+// plane lean (F3T_LEAN_ONLY: the host gave this launch lean runs only; the general code is not
+// compiled in, which keeps the lean form's registers to itself).
+enum { F3T_MIXED = 0, F3T_LEAN_ONLY = 1 };
+
+// One block's work: tile (bx, by) of 32 x TY columns over planes k0 .. k1 of one grid.  maps: the
 // in set's tensor maps (kernel parameter or global memory); A, G: the grid's arguments (in
-// shared memory); nblk: the blocks of this grid's pass (the last of them to finish advances the
-// grid's device-loop step counter); smem: the dynamic shared memory (1024-byte aligned).
-template <int TY>
+// shared memory); nblk: the blocks of this launch (the last of them to finish advances the
+// grid's device-loop step counter, when G.step_inc is set); smem: the dynamic shared memory
+// (1024-byte aligned).
+template <int TY, int MODE>
 __device__ __forceinline__ void f3t_tile(const CUtensorMap *maps, const Fused3Args &A, const GridArgs<float> &G,
-                                         int bx, int by, int bz, int kch, int nd, unsigned nblk, int *err,
+                                         int bx, int by, int k0, int k1, int nd, unsigned nblk, int *err,
                                          unsigned char *f3_smem)
 {
     using S = F3tShape<TY>;
@@ -240,7 +352,6 @@ __device__ __forceinline__ void f3t_tile(const CUtensorMap *maps, const Fused3Ar
     const Lay &L = G.L;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int i0 = 1 + bx * 32, j0 = 1 + by * TY;
-    const int k0 = 1 + bz * kch, k1 = min(L.nz, k0 + kch - 1);
     const bool perz = G.per[2] != 0;
     // staged planes pa .. k1+1; pa = k0-1 when the new H of plane k0-1 is needed (k0 > 1, or the
     // periodic image of plane 0), else k0 (plane 0 is the PEC ghost: new H = 0)
@@ -276,11 +387,10 @@ __device__ __forceinline__ void f3t_tile(const CUtensorMap *maps, const Fused3Ar
     if (warp == NCW + 1) {
         // ---- copy warp: lane 0 stages plane pa + q into slot q % D
         if (lane != 0) return;
-        int q = 0;
+        int q = 0, s = 0, round = 0;           // plane q goes to slot s in its round-th use
         bool ok = true;
         for (; q < nq; ++q) {
-            const int s = q % nd;
-            if (q >= nd && !mbar_wait_bounded(&empty[s], (uint32_t)(((q / nd) - 1) & 1), F3T_WAIT_CYCLES)) {
+            if (round > 0 && !mbar_wait_bounded(&empty[s], (uint32_t)((round - 1) & 1), F3T_WAIT_CYCLES)) {
                 ok = false;
                 break;
             }
@@ -291,6 +401,10 @@ __device__ __forceinline__ void f3t_tile(const CUtensorMap *maps, const Fused3Ar
 #pragma unroll
             for (int c = 0; c < 6; ++c)
                 tma_load_3d(dst + c * CB, &maps[c], 32 * bx, j0 - 1, z, &full[s]);
+            if (++s == nd) {
+                s = 0;
+                ++round;
+            }
         }
         if (!ok) {
             atomicOr(err, 1);
@@ -306,29 +420,50 @@ __device__ __forceinline__ void f3t_tile(const CUtensorMap *maps, const Fused3Ar
     const int i = i0 + lane;
     const int ic = min(i, L.nx);
     const float dhx = G.den_h[0][ic], dex = G.den_e[0][ic];
-    const int lhx = G.lH[0][ic], lex = G.lE[0][ic];
     const int cc = lane + 4;                   // staged column of i
+    // CPML psi offsets of the planes: x and y faces grow by one plane of their array per k, the z
+    // face holds sZ words per layer
+    const int sX = G.L2 * L.ny, sY = L.nx * G.L2, sZ = L.nx * L.ny;
     // compute warps: cells (i, j_r), j_r = j0 + RPT warp + r, staged row rr_r = j_r - j0 + 1.  The
-    // halo warp: the row halo cell (i, j0 - 1) and, for lane < TY, the column halo cell
-    // (i0 - 1, j0 + lane) (a non-periodic index 0 is the PEC ghost: new H = 0)
+    // halo warp: the row halo cell (i, j0 - 1) as its row 0 and, for lane < TY, the column halo
+    // cell (i0 - 1, j0 + lane) (a non-periodic index 0 is the PEC ghost: new H = 0).  Per row, the
+    // psi index of each face at plane 1 (x, y) or layer 0 (z); -1 where the cell is in no slab.
     const int jb = cw ? j0 + RPT * warp : j0 - 1;
+    const int lhx = G.lH[0][ic], lex = G.lE[0][ic];
     float dhy[RPT], dey[RPT];
-    int lhy[RPT], ley[RPT];
+    int bxH[RPT], bxE[RPT], byH[RPT], byE[RPT], bz0[RPT];
     bool own[RPT], bbc[RPT];
 #pragma unroll
     for (int r = 0; r < RPT; ++r) {
         const int j = jb + r, jc = max(1, min(j, L.ny));
         dhy[r] = G.den_h[1][jc];
         dey[r] = G.den_e[1][jc];
-        lhy[r] = G.lH[1][jc];
-        ley[r] = G.lE[1][jc];
+        const int lhy = G.lH[1][jc], ley = G.lE[1][jc];
+        bxH[r] = lhx >= 0 ? lhx + G.L2 * (jc - 1) : -1;
+        bxE[r] = lex >= 0 ? lex + G.L2 * (jc - 1) : -1;
+        byH[r] = lhy >= 0 ? (ic - 1) + L.nx * lhy : -1;
+        byE[r] = ley >= 0 ? (ic - 1) + L.nx * ley : -1;
+        bz0[r] = (ic - 1) + L.nx * (jc - 1);
         own[r] = cw && i <= L.nx && j <= L.ny;
         bbc[r] = own[r] && i >= G.bb0[0] && i <= G.bb1[0] && j >= G.bb0[1] && j <= G.bb1[1];
     }
     const bool row_h = !cw && j0 > 1 && i <= L.nx;
     const bool col_h = !cw && i0 > 1 && lane < TY && j0 + lane <= L.ny;
+    // the column halo cell (i0 - 1, jhc) of this lane and its psi bases
+    const int ih = i0 - 1, jhc = min(j0 + lane, L.ny);
+    int cxH = -1, cyH = -1, cz0 = 0;
+    if (col_h) {
+        const int lx = G.lH[0][ih], ly = G.lH[1][jhc];
+        cxH = lx >= 0 ? lx + G.L2 * (jhc - 1) : -1;
+        cyH = ly >= 0 ? (ih - 1) + L.nx * ly : -1;
+        cz0 = (ih - 1) + L.nx * (jhc - 1);
+    }
     const int col0 = (int)L.off + i + L.px * jb;   // element offsets < 2^31 (checked by the host)
     const int rr0 = cw ? RPT * warp + 1 : 0;
+    // psi indices of a face at plane kk: x / y from a plane-1 base, z from the layer lz
+    auto at_x = [&](int b, int kk) { return b >= 0 ? b + sX * (kk - 1) : -1; };
+    auto at_y = [&](int b, int kk) { return b >= 0 ? b + sY * (kk - 1) : -1; };
+    auto at_z = [&](int b, int lz) { return lz >= 0 ? b + sZ * lz : -1; };
 
     bool fail = false;
     float hxm[RPT], hym[RPT];                  // new Hx, Hy of the own cells at plane k - 1
@@ -350,10 +485,12 @@ __device__ __forceinline__ void f3t_tile(const CUtensorMap *maps, const Fused3Ar
                 const float ez_jp = B0[2 * CB + o + F3T_BX], ez_ip = B0[2 * CB + o + 1];
                 const float ex_kp = B1[o], ey_kp = B1[CB + o];
                 const int jc = max(1, min(jb + r, L.ny));
-                hxm[r] = f3t_hx(B0[3 * CB + o], ez_c, ez_jp, ey_c, ey_kp, dhy[r], z0.x, dt_mu0, lhy[r], lhz, G, A, ic,
-                                jc, kk, own[r] ? 1 : 0);
-                hym[r] = f3t_hy(B0[4 * CB + o], ez_c, ez_ip, ex_c, ex_kp, dhx, z0.x, dt_mu0, lhx, lhz, G, A, ic, jc,
-                                kk, own[r] ? 1 : 0);
+                const int px = at_x(bxH[r], kk), py = at_y(byH[r], kk), pz = at_z(bz0[r], lhz);
+                const F3tPsiH q = f3t_load_psiH(G, px, py, pz, own[r]);
+                hxm[r] = f3t_hx(B0[3 * CB + o], ez_c, ez_jp, ey_c, ey_kp, dhy[r], z0.x, dt_mu0, G, A, jc, kk,
+                                own[r] ? 1 : 0, py, pz, q.y0, q.z0);
+                hym[r] = f3t_hy(B0[4 * CB + o], ez_c, ez_ip, ex_c, ex_kp, dhx, z0.x, dt_mu0, G, A, ic, kk,
+                                own[r] ? 1 : 0, px, pz, q.x0, q.z1);
             }
         }
         __syncwarp();
@@ -390,7 +527,17 @@ __device__ __forceinline__ void f3t_tile(const CUtensorMap *maps, const Fused3Ar
         float *hp = hn + (k & 1) * 3 * S::HNF;   // [Hx, Hy, Hz][TY+1][33]
         float eo[RPT][3];                        // lean form: old E of the own cells across the barrier
         if (cw) {
-            // new H of the own cells: into the tile in shared memory and out to HBM
+            // new H of the own cells: into the tile in shared memory and out to HBM; every row's
+            // psi is requested before any is used
+            int px[RPT], py[RPT], pz[RPT];
+            F3tPsiH q[RPT];
+#pragma unroll
+            for (int r = 0; r < RPT; ++r) {
+                px[r] = LEAN ? -1 : at_x(bxH[r], k);
+                py[r] = LEAN ? -1 : at_y(byH[r], k);
+                pz[r] = LEAN ? -1 : at_z(bz0[r], lhz);
+                q[r] = f3t_load_psiH(G, px[r], py[r], pz[r], !LEAN && own[r]);
+            }
 #pragma unroll
             for (int r = 0; r < RPT; ++r) {
                 const int o = (rr0 + r) * F3T_BX + cc;
@@ -405,12 +552,12 @@ __device__ __forceinline__ void f3t_tile(const CUtensorMap *maps, const Fused3Ar
                     eo[r][2] = ez_c;
                 }
                 const int pm = (LEAN || !own[r]) ? 0 : 2;
-                const float hx = f3t_hx(Hxc[o], ez_c, ez_jp, ey_c, ey_kp, dhy[r], dhz, dt_mu0, lhy[r], lhz, G, A, ic,
-                                        jc, k, pm);
-                const float hy = f3t_hy(Hyc[o], ez_c, ez_ip, ex_c, ex_kp, dhx, dhz, dt_mu0, lhx, lhz, G, A, ic, jc, k,
-                                        pm);
-                const float hz = f3t_hz(Hzc[o], ey_c, ey_ip, ex_c, ex_jp, dhx, dhy[r], dt_mu0, lhx, lhy[r], G, A, ic,
-                                        jc, k, pm);
+                const float hx = f3t_hx(Hxc[o], ez_c, ez_jp, ey_c, ey_kp, dhy[r], dhz, dt_mu0, G, A, jc, k, pm, py[r],
+                                        pz[r], q[r].y0, q[r].z0);
+                const float hy = f3t_hy(Hyc[o], ez_c, ez_ip, ex_c, ex_kp, dhx, dhz, dt_mu0, G, A, ic, k, pm, px[r],
+                                        pz[r], q[r].x0, q[r].z1);
+                const float hz = f3t_hz(Hzc[o], ey_c, ey_ip, ex_c, ex_jp, dhx, dhy[r], dt_mu0, G, A, ic, jc, pm,
+                                        px[r], py[r], q[r].x1, q[r].y1);
                 const int h = (rr0 + r) * 33 + lane + 1;
                 hp[h] = hx;
                 hp[S::HNF + h] = hy;
@@ -427,31 +574,35 @@ __device__ __forceinline__ void f3t_tile(const CUtensorMap *maps, const Fused3Ar
                 }
             }
         } else {
-            // row halo (i, j0 - 1): Hz and Hx
+            // row halo (i, j0 - 1): Hz and Hx; column halo (i0 - 1, j0 + lane): Hz and Hy (the psi of
+            // both requested first)
+            const int rxp = LEAN ? -1 : at_x(bxH[0], k), ryp = LEAN ? -1 : at_y(byH[0], k);
+            const int rzp = LEAN ? -1 : at_z(bz0[0], lhz);
+            const int cxp = LEAN ? -1 : at_x(cxH, k), cyp = LEAN ? -1 : at_y(cyH, k);
+            const int czp = LEAN ? -1 : at_z(cz0, lhz);
+            const F3tPsiH qr = f3t_load_psiH(G, rxp, ryp, rzp, !LEAN && row_h);
+            const F3tPsiH qc = f3t_load_psiH(G, cxp, cyp, czp, !LEAN && col_h);
             float rx = 0.f, rz = 0.f;
             if (row_h) {
                 const int o = cc;                      // staged row 0
                 const float e_x = Exc[o], e_y = Eyc[o], e_z = Ezc[o];
-                rx = f3t_hx(Hxc[o], e_z, Ezc[o + F3T_BX], e_y, Bn[CB + o], dhy[0], dhz, dt_mu0, lhy[0], lhz, G, A, ic,
-                            j0 - 1, k, LEAN ? 0 : 1);
-                rz = f3t_hz(Hzc[o], e_y, Eyc[o + 1], e_x, Exc[o + F3T_BX], dhx, dhy[0], dt_mu0, lhx, lhy[0], G, A, ic,
-                            j0 - 1, k, LEAN ? 0 : 1);
+                rx = f3t_hx(Hxc[o], e_z, Ezc[o + F3T_BX], e_y, Bn[CB + o], dhy[0], dhz, dt_mu0, G, A, j0 - 1, k,
+                            LEAN ? 0 : 1, ryp, rzp, qr.y0, qr.z0);
+                rz = f3t_hz(Hzc[o], e_y, Eyc[o + 1], e_x, Exc[o + F3T_BX], dhx, dhy[0], dt_mu0, G, A, ic, j0 - 1,
+                            LEAN ? 0 : 1, rxp, ryp, qr.x1, qr.y1);
             }
             hp[lane + 1] = rx;
             hp[2 * S::HNF + lane + 1] = rz;
-            // column halo (i0 - 1, j0 + lane): Hz and Hy
             if (lane < TY) {
                 float cy = 0.f, cz = 0.f;
                 if (col_h) {
-                    const int ih = i0 - 1, jhc = j0 + lane;
                     const float dhx_h = G.den_h[0][ih], dhy_h = G.den_h[1][jhc];
-                    const int lhx_h = G.lH[0][ih], lhy_h = G.lH[1][jhc];
                     const int o = (lane + 1) * F3T_BX + 3;
                     const float e_x = Exc[o], e_y = Eyc[o], e_z = Ezc[o];
-                    cy = f3t_hy(Hyc[o], e_z, Ezc[o + 1], e_x, Bn[o], dhx_h, dhz, dt_mu0, lhx_h, lhz, G, A, ih, jhc, k,
-                                LEAN ? 0 : 1);
-                    cz = f3t_hz(Hzc[o], e_y, Eyc[o + 1], e_x, Exc[o + F3T_BX], dhx_h, dhy_h, dt_mu0, lhx_h, lhy_h, G,
-                                A, ih, jhc, k, LEAN ? 0 : 1);
+                    cy = f3t_hy(Hyc[o], e_z, Ezc[o + 1], e_x, Bn[o], dhx_h, dhz, dt_mu0, G, A, ih, k, LEAN ? 0 : 1,
+                                cxp, czp, qc.x0, qc.z1);
+                    cz = f3t_hz(Hzc[o], e_y, Eyc[o + 1], e_x, Exc[o + F3T_BX], dhx_h, dhy_h, dt_mu0, G, A, ih, jhc,
+                                LEAN ? 0 : 1, cxp, cyp, qc.x1, qc.y1);
                 }
                 hp[S::HNF + (lane + 1) * 33] = cy;
                 hp[2 * S::HNF + (lane + 1) * 33] = cz;
@@ -464,17 +615,13 @@ __device__ __forceinline__ void f3t_tile(const CUtensorMap *maps, const Fused3Ar
             const int lez = __float_as_int(z1.w);
 #pragma unroll
             for (int r = 0; r < RPT; ++r) {
-                const int j = jb + r;
                 const int h = (rr0 + r) * 33 + lane + 1;
                 const float hx = hp[h], hy = hp[S::HNF + h], hz = hp[2 * S::HNF + h];
                 const float hz_im = hp[2 * S::HNF + h - 1], hy_im = hp[S::HNF + h - 1];
                 const float hz_jm = hp[2 * S::HNF + h - 33], hx_jm = hp[h - 33];
-                // curl of the new H, every operation rounded explicitly (the lean and the general
-                // form, and every tile shape, give a cell the same bits)
-                const float dhyk = __fsub_rn(hym[r], hy), dhxk = __fsub_rn(hx, hxm[r]);   // planes k-1, k
-                const float rx = __fmaf_rn(dhyk, dez, __fmul_rn(__fsub_rn(hz, hz_jm), dey[r]));
-                const float ry = __fmaf_rn(dhxk, dez, __fmul_rn(__fsub_rn(hz_im, hz), dex));
-                const float rz = __fmaf_rn(__fsub_rn(hx_jm, hx), dey[r], __fmul_rn(__fsub_rn(hy, hy_im), dex));
+                float rx, ry, rz, dhxk, dhyk;
+                f3t_curl(hx, hy, hz, hz_im, hy_im, hz_jm, hx_jm, hxm[r], hym[r], dex, dey[r], dez, rx, ry, rz, dhxk,
+                         dhyk);
                 hxm[r] = hx;
                 hym[r] = hy;
                 if (!own[r]) continue;
@@ -488,56 +635,8 @@ __device__ __forceinline__ void f3t_tile(const CUtensorMap *maps, const Fused3Ar
                     ex = Exc[o];
                     ey = Eyc[o];
                     ez = Ezc[o];
-                    if (G.pl_on && (G.pl_axis == 0 ? i : (G.pl_axis == 1 ? j : k)) == G.pl_index) {
-                        // the plane source of this step (source_interactions before the E update)
-                        const double a = sp_get(G.pl_amp);
-                        if (a != 0.0) {
-                            const double add = __dmul_rn(G.pl_c_src, a);
-                            if (G.pl_comp == 0) ex = (float)__dadd_rn((double)ex, add);
-                            else if (G.pl_comp == 1) ey = (float)__dadd_rn((double)ey, add);
-                            else ez = (float)__dadd_rn((double)ez, add);
-                        }
-                    }
-                    if (bbc[r] && k >= G.bb0[2] && k <= G.bb1[2]) {
-                        const int b = (i - G.bb0[0]) + G.bbd[0] * ((j - G.bb0[1]) + G.bbd[1] * (k - G.bb0[2]));
-                        ex = f3t_media(ex, rx, 0, b, G);
-                        ey = f3t_media(ey, ry, 1, b, G);
-                        ez = f3t_media(ez, rz, 2, b, G);
-                    } else {
-                        ex = __fmaf_rn(dt_eps0, rx, ex);
-                        ey = __fmaf_rn(dt_eps0, ry, ey);
-                        ez = __fmaf_rn(dt_eps0, rz, ez);
-                    }
-                    if (lex >= 0) {   // mxll_3D_mod.f90:817-849
-                        const int p = lex + G.L2 * ((j - 1) + L.ny * (k - 1));
-                        const float b = G.bE[0][i], c = G.cE[0][i];
-                        const float v0 = f3t_psi(b, G.psiE[0][0][p], c, __fsub_rn(hz_im, hz));
-                        const float v1 = f3t_psi(b, G.psiE[0][1][p], c, __fsub_rn(hy, hy_im));
-                        G.psiE[0][0][p] = v0;
-                        G.psiE[0][1][p] = v1;
-                        ey = __fmaf_rn(dt_eps0, v0, ey);
-                        ez = __fmaf_rn(dt_eps0, v1, ez);
-                    }
-                    if (ley[r] >= 0) {   // :851-885
-                        const int p = (i - 1) + L.nx * (ley[r] + G.L2 * (k - 1));
-                        const float b = G.bE[1][j], c = G.cE[1][j];
-                        const float v0 = f3t_psi(b, G.psiE[1][0][p], c, __fsub_rn(hz, hz_jm));
-                        const float v1 = f3t_psi(b, G.psiE[1][1][p], c, __fsub_rn(hx_jm, hx));
-                        G.psiE[1][0][p] = v0;
-                        G.psiE[1][1][p] = v1;
-                        ex = __fmaf_rn(dt_eps0, v0, ex);
-                        ez = __fmaf_rn(dt_eps0, v1, ez);
-                    }
-                    if (lez >= 0) {   // :887-921
-                        const int p = (i - 1) + L.nx * ((j - 1) + L.ny * lez);
-                        const float b = z1.x, c = z1.y;
-                        const float v0 = f3t_psi(b, G.psiE[2][0][p], c, dhyk);
-                        const float v1 = f3t_psi(b, G.psiE[2][1][p], c, dhxk);
-                        G.psiE[2][0][p] = v0;
-                        G.psiE[2][1][p] = v1;
-                        ex = __fmaf_rn(dt_eps0, v0, ex);
-                        ey = __fmaf_rn(dt_eps0, v1, ey);
-                    }
+                    f3t_e_general(ex, ey, ez, rx, ry, rz, dhxk, dhyk, hx, hy, hz, hz_im, hy_im, hz_jm, hx_jm, i, jb + r, k,
+                                  at_x(bxE[r], k), at_y(byE[r], k), at_z(bz0[r], lez), z1.x, z1.y, bbc[r], dt_eps0, G);
                 }
                 const int idx = col0 + L.px * r + (int)L.pz * k;
                 __stcs(A.out.f[0] + idx, ex);
@@ -550,66 +649,99 @@ __device__ __forceinline__ void f3t_tile(const CUtensorMap *maps, const Fused3Ar
         return false;
     };
 
+    // slot and round of plane k (kept as counters: the ring depth is a launch parameter)
+    int sc = k0 - pa, rc = 0;
     for (int k = k0; k <= k1; ++k) {
-        const int q = k - pa, sc = q % nd, sn = sc + 1 == nd ? 0 : sc + 1;
+        const int q = k - pa;
+        const int sn = sc + 1 == nd ? 0 : sc + 1, rn = sc + 1 == nd ? rc + 1 : rc;
         const float4 z0 = zc[2 * q], z1 = zc[2 * q + 1];
-        // the words of the next plane that come from HBM outside the staging (CPML psi, media
-        // bytes) are pulled into L1 now, so that their loads there do not stall the block
-        if (cw && k < k1) {
-            const float4 zn = zc[2 * (q + 1) + 1];
-            if (!lean_at(k + 1, zn)) {
+        // the words of plane kn = k + F3T_PF that come from HBM outside the staging (CPML psi,
+        // media bytes) are pulled into L1 now, so that their loads there do not stall the block
+        const int kn = k + F3T_PF;
+        if (MODE != F3T_LEAN_ONLY && kn <= k1) {
+            const float4 zn = zc[2 * (q + F3T_PF) + 1];
+            if (!lean_at(kn, zn)) {
                 const int lhzn = __float_as_int(zn.z), lezn = __float_as_int(zn.w);
+                if (cw) {
 #pragma unroll
-                for (int r = 0; r < RPT; ++r) {
-                    if (!own[r]) continue;
-                    const int j = jb + r;
-                    if (lhx >= 0) {
-                        const int p = lhx + G.L2 * ((j - 1) + L.ny * k);
-                        f3t_prefetch(G.psiH[0][0] + p);
-                        f3t_prefetch(G.psiH[0][1] + p);
+                    for (int r = 0; r < RPT; ++r) {
+                        if (!own[r]) continue;
+                        const int pxh = at_x(bxH[r], kn), pxe = at_x(bxE[r], kn);
+                        const int pyh = at_y(byH[r], kn), pye = at_y(byE[r], kn);
+                        const int pzh = at_z(bz0[r], lhzn), pze = at_z(bz0[r], lezn);
+                        if (pxh >= 0) {
+                            f3t_prefetch(G.psiH[0][0] + pxh);
+                            f3t_prefetch(G.psiH[0][1] + pxh);
+                        }
+                        if (pxe >= 0) {
+                            f3t_prefetch(G.psiE[0][0] + pxe);
+                            f3t_prefetch(G.psiE[0][1] + pxe);
+                        }
+                        if (pyh >= 0) {
+                            f3t_prefetch(G.psiH[1][0] + pyh);
+                            f3t_prefetch(G.psiH[1][1] + pyh);
+                        }
+                        if (pye >= 0) {
+                            f3t_prefetch(G.psiE[1][0] + pye);
+                            f3t_prefetch(G.psiE[1][1] + pye);
+                        }
+                        if (pzh >= 0) {
+                            f3t_prefetch(G.psiH[2][0] + pzh);
+                            f3t_prefetch(G.psiH[2][1] + pzh);
+                        }
+                        if (pze >= 0) {
+                            f3t_prefetch(G.psiE[2][0] + pze);
+                            f3t_prefetch(G.psiE[2][1] + pze);
+                        }
+                        const int j = jb + r;
+                        if (bbc[r] && kn >= G.bb0[2] && kn <= G.bb1[2]) {
+                            const int b = (i - G.bb0[0]) + G.bbd[0] * ((j - G.bb0[1]) + G.bbd[1] * (kn - G.bb0[2]));
+                            f3t_prefetch(G.mat[0] + b);
+                            f3t_prefetch(G.mat[1] + b);
+                            f3t_prefetch(G.mat[2] + b);
+                        }
                     }
-                    if (lex >= 0) {
-                        const int p = lex + G.L2 * ((j - 1) + L.ny * k);
-                        f3t_prefetch(G.psiE[0][0] + p);
-                        f3t_prefetch(G.psiE[0][1] + p);
+                } else {
+                    // the halo cells' in-set H psi (their loads would otherwise hold every
+                    // compute warp at the plane's barrier for a trip to memory)
+                    if (row_h) {
+                        const int px = at_x(bxH[0], kn), py = at_y(byH[0], kn), pz = at_z(bz0[0], lhzn);
+                        if (px >= 0) f3t_prefetch(G.psiH[0][1] + px);
+                        if (py >= 0) {
+                            f3t_prefetch(G.psiH[1][0] + py);
+                            f3t_prefetch(G.psiH[1][1] + py);
+                        }
+                        if (pz >= 0) f3t_prefetch(G.psiH[2][0] + pz);
                     }
-                    if (lhy[r] >= 0) {
-                        const int p = (i - 1) + L.nx * (lhy[r] + G.L2 * k);
-                        f3t_prefetch(G.psiH[1][0] + p);
-                        f3t_prefetch(G.psiH[1][1] + p);
-                    }
-                    if (ley[r] >= 0) {
-                        const int p = (i - 1) + L.nx * (ley[r] + G.L2 * k);
-                        f3t_prefetch(G.psiE[1][0] + p);
-                        f3t_prefetch(G.psiE[1][1] + p);
-                    }
-                    if (lhzn >= 0) {
-                        const int p = (i - 1) + L.nx * ((j - 1) + L.ny * lhzn);
-                        f3t_prefetch(G.psiH[2][0] + p);
-                        f3t_prefetch(G.psiH[2][1] + p);
-                    }
-                    if (lezn >= 0) {
-                        const int p = (i - 1) + L.nx * ((j - 1) + L.ny * lezn);
-                        f3t_prefetch(G.psiE[2][0] + p);
-                        f3t_prefetch(G.psiE[2][1] + p);
-                    }
-                    if (bbc[r] && k + 1 >= G.bb0[2] && k + 1 <= G.bb1[2]) {
-                        const int b = (i - G.bb0[0]) + G.bbd[0] * ((j - G.bb0[1]) + G.bbd[1] * (k + 1 - G.bb0[2]));
-                        f3t_prefetch(G.mat[0] + b);
-                        f3t_prefetch(G.mat[1] + b);
-                        f3t_prefetch(G.mat[2] + b);
+                    if (col_h) {
+                        const int px = at_x(cxH, kn), py = at_y(cyH, kn), pz = at_z(cz0, lhzn);
+                        if (px >= 0) {
+                            f3t_prefetch(G.psiH[0][0] + px);
+                            f3t_prefetch(G.psiH[0][1] + px);
+                        }
+                        if (py >= 0) f3t_prefetch(G.psiH[1][1] + py);
+                        if (pz >= 0) f3t_prefetch(G.psiH[2][1] + pz);
                     }
                 }
             }
         }
         // plane k's slot completed in the previous iteration (or before the loop); wait for k+1
-        fail |= !mbar_wait_bounded(&full[sn], (uint32_t)(((q + 1) / nd) & 1), F3T_WAIT_CYCLES);
-        const bool bad = lean_at(k, z1) ? plane(F3tForm<true>{}, k, sc, sn, z0, z1)
-                                        : plane(F3tForm<false>{}, k, sc, sn, z0, z1);
+        fail |= !mbar_wait_bounded(&full[sn], (uint32_t)(rn & 1), F3T_WAIT_CYCLES);
+        bool bad;
+        if constexpr (MODE == F3T_LEAN_ONLY) {
+            // the host's plan and this block's own test agree, or the error word says otherwise
+            if (!lean_at(k, z1) && threadIdx.x == 0) atomicOr(err, 4);
+            bad = plane(F3tForm<true>{}, k, sc, sn, z0, z1);
+        } else {
+            bad = lean_at(k, z1) ? plane(F3tForm<true>{}, k, sc, sn, z0, z1)
+                                 : plane(F3tForm<false>{}, k, sc, sn, z0, z1);
+        }
         if (bad) {
             if (threadIdx.x == 0) atomicOr(err, 1);
             break;
         }
+        sc = sn;
+        rc = rn;
     }
     // device loop: the last block to finish advances the step counter, so every block of this
     // pass reads the step's scalars (the plane source amplitude) before the counter moves; the
@@ -640,16 +772,121 @@ __device__ __forceinline__ void f3t_args_to_smem(const GridArgs<float> &G, const
     __syncthreads();
 }
 
-// nd: ring depth (the dynamic shared memory holds F3tShape<TY>::smem(nd) bytes)
-template <int TY>
+// One launch over a list of runs (tile, planes k0 .. k1): block b takes items[b].  nd: ring depth
+// (the dynamic shared memory holds F3tShape<TY>::smem(nd) bytes).
+template <int TY, int MODE>
 __global__ void __launch_bounds__(F3tShape<TY>::THREADS, f3t_min_blocks<TY>())
-    k_fused3_tma(const __grid_constant__ F3tMaps M, Fused3Args A, GridArgs<float> G, int kch, int nd, int *err)
+    k_fused3_tma(const __grid_constant__ F3tMaps M, Fused3Args A, GridArgs<float> G, const int4 *__restrict__ items,
+                 int nd, int *err)
 {
     extern __shared__ __align__(1024) unsigned char f3_smem[];
     f3t_args_to_smem(G, A, f3_smem);
-    f3t_tile<TY>(M.m, *reinterpret_cast<const Fused3Args *>(f3_smem + F3T_ARGB),
-                 *reinterpret_cast<const GridArgs<float> *>(f3_smem), (int)blockIdx.x, (int)blockIdx.y,
-                 (int)blockIdx.z, kch, nd, gridDim.x * gridDim.y * gridDim.z, err, f3_smem);
+    const int4 it = items[blockIdx.x];
+    f3t_tile<TY, MODE>(M.m, *reinterpret_cast<const Fused3Args *>(f3_smem + F3T_ARGB),
+                       *reinterpret_cast<const GridArgs<float> *>(f3_smem), it.x, it.y, it.z, it.w, nd, gridDim.x,
+                       err, f3_smem);
+}
+
+// ---- general runs: the two-kernel form -----------------------------------------------------
+// Runs whose planes need CPML psi, the media box or the plane source are updated by two plain
+// kernels, one thread per (i, j) column of the run's 32 x TY tile marching its planes: new H (from
+// the in set, psi in -> out) and then new E (from the out set's new H), with the same device
+// functions as the fused pass, so each cell gets the same bits whichever kernel updates it.  The
+// H kernel runs beside the lean fused launch; the E kernel after both (it reads the new H of
+// neighbouring cells that either of them wrote).
+template <int TY>
+__global__ void __launch_bounds__(32 * TY) k_f3g_h(Fused3Args A, GridArgs<float> G, const int4 *__restrict__ items)
+{
+    const int4 it = items[blockIdx.x];
+    const Lay L = G.L;
+    const int i = 1 + 32 * it.x + (int)threadIdx.x, j = 1 + TY * it.y + (int)threadIdx.y;
+    if (i > L.nx || j > L.ny) return;
+    const bool perz = G.per[2] != 0;
+    const float *__restrict__ Ex = A.in.f[0];
+    const float *__restrict__ Ey = A.in.f[1];
+    const float *__restrict__ Ez = A.in.f[2];
+    const float dt_mu0 = G.dt_mu0, dhx = G.den_h[0][i], dhy = G.den_h[1][j];
+    const int lhx = G.lH[0][i], lhy = G.lH[1][j];
+    const int bxH = lhx >= 0 ? lhx + G.L2 * (j - 1) : -1, byH = lhy >= 0 ? (i - 1) + L.nx * lhy : -1;
+    const int bz0 = (i - 1) + L.nx * (j - 1), sX = G.L2 * L.ny, sY = L.nx * G.L2, sZ = L.nx * L.ny;
+    const int px_ = L.px, pz_ = (int)L.pz;
+    int idx = (int)L.off + i + px_ * j + pz_ * it.z;   // element offsets < 2^31 (checked by the host)
+    for (int k = it.z; k <= it.w; ++k, idx += pz_) {
+        const int kp = (perz && k == L.nz) ? idx - (L.nz - 1) * pz_ : idx + pz_;   // E of plane k + 1
+        const float ex_c = Ex[idx], ey_c = Ey[idx], ez_c = Ez[idx];
+        const float ez_jp = Ez[idx + px_], ez_ip = Ez[idx + 1], ey_ip = Ey[idx + 1], ex_jp = Ex[idx + px_];
+        const float ex_kp = Ex[kp], ey_kp = Ey[kp];
+        const float dhz = G.den_h[2][k];
+        const int lhz = G.lH[2][k];
+        const int px = bxH >= 0 ? bxH + sX * (k - 1) : -1, py = byH >= 0 ? byH + sY * (k - 1) : -1;
+        const int pz = lhz >= 0 ? bz0 + sZ * lhz : -1;
+        const F3tPsiH q = f3t_load_psiH(G, px, py, pz, true);
+        const float hx = f3t_hx(__ldcs(A.in.f[3] + idx), ez_c, ez_jp, ey_c, ey_kp, dhy, dhz, dt_mu0, G, A, j, k, 2, py,
+                                pz, q.y0, q.z0);
+        const float hy = f3t_hy(__ldcs(A.in.f[4] + idx), ez_c, ez_ip, ex_c, ex_kp, dhx, dhz, dt_mu0, G, A, i, k, 2, px,
+                                pz, q.x0, q.z1);
+        const float hz = f3t_hz(__ldcs(A.in.f[5] + idx), ey_c, ey_ip, ex_c, ex_jp, dhx, dhy, dt_mu0, G, A, i, j, 2, px,
+                                py, q.x1, q.y1);
+        __stcs(A.out.f[3] + idx, hx);
+        __stcs(A.out.f[4] + idx, hy);
+        __stcs(A.out.f[5] + idx, hz);
+        if (perz && k == L.nz) {   // periodic ghost plane H(0) = H(nz) (mxll_3D_mod.f90:725-738)
+            A.out.f[3][idx - L.nz * pz_] = hx;
+            A.out.f[4][idx - L.nz * pz_] = hy;
+        }
+    }
+}
+
+template <int TY>
+__global__ void __launch_bounds__(32 * TY) k_f3g_e(Fused3Args A, GridArgs<float> G, const int4 *__restrict__ items)
+{
+    const int4 it = items[blockIdx.x];
+    const Lay L = G.L;
+    const int i = 1 + 32 * it.x + (int)threadIdx.x, j = 1 + TY * it.y + (int)threadIdx.y;
+    if (i <= L.nx && j <= L.ny) {
+        const float *__restrict__ Hx = A.out.f[3];
+        const float *__restrict__ Hy = A.out.f[4];
+        const float *__restrict__ Hz = A.out.f[5];
+        const float dt_eps0 = G.dt_eps0, dex = G.den_e[0][i], dey = G.den_e[1][j];
+        const int lex = G.lE[0][i], ley = G.lE[1][j];
+        const int bxE = lex >= 0 ? lex + G.L2 * (j - 1) : -1, byE = ley >= 0 ? (i - 1) + L.nx * ley : -1;
+        const int bz0 = (i - 1) + L.nx * (j - 1), sX = G.L2 * L.ny, sY = L.nx * G.L2, sZ = L.nx * L.ny;
+        const bool bbc = i >= G.bb0[0] && i <= G.bb1[0] && j >= G.bb0[1] && j <= G.bb1[1];
+        const int px_ = L.px, pz_ = (int)L.pz;
+        int idx = (int)L.off + i + px_ * j + pz_ * it.z;
+        // new Hx, Hy of plane k - 1 (plane 0: the periodic image written by the pass, or the zero ghost)
+        float hxm = Hx[idx - pz_], hym = Hy[idx - pz_];
+        for (int k = it.z; k <= it.w; ++k, idx += pz_) {
+            const float hx = Hx[idx], hy = Hy[idx], hz = Hz[idx];
+            const float hz_im = Hz[idx - 1], hy_im = Hy[idx - 1], hz_jm = Hz[idx - px_], hx_jm = Hx[idx - px_];
+            const float dez = G.den_e[2][k];
+            const int lez = G.lE[2][k];
+            float rx, ry, rz, dhxk, dhyk;
+            f3t_curl(hx, hy, hz, hz_im, hy_im, hz_jm, hx_jm, hxm, hym, dex, dey, dez, rx, ry, rz, dhxk, dhyk);
+            hxm = hx;
+            hym = hy;
+            float ex = __ldcs(A.in.f[0] + idx), ey = __ldcs(A.in.f[1] + idx), ez = __ldcs(A.in.f[2] + idx);
+            f3t_e_general(ex, ey, ez, rx, ry, rz, dhxk, dhyk, hx, hy, hz, hz_im, hy_im, hz_jm, hx_jm, i, j, k,
+                          bxE >= 0 ? bxE + sX * (k - 1) : -1, byE >= 0 ? byE + sY * (k - 1) : -1,
+                          lez >= 0 ? bz0 + sZ * lez : -1, __ldg(G.bE[2] + k), __ldg(G.cE[2] + k), bbc, dt_eps0, G);
+            __stcs(A.out.f[0] + idx, ex);
+            __stcs(A.out.f[1] + idx, ey);
+            __stcs(A.out.f[2] + idx, ez);
+        }
+    }
+    // device loop: the last block to finish advances the step counter (this launch ends the pass
+    // and holds its only reads of the step's scalars)
+    if (G.step_inc) {
+        __syncthreads();
+        if (threadIdx.x == 0 && threadIdx.y == 0) {
+            __threadfence();
+            if (atomicAdd((unsigned *)G.step_done, 1u) == gridDim.x - 1) {
+                *G.step_done = 0;
+                *G.step_inc += 1;
+                __threadfence();
+            }
+        }
+    }
 }
 
 // ---- batched: the fused pass of several grids in one launch ----------------------------------
@@ -675,7 +912,9 @@ __global__ void __launch_bounds__(F3tShape<TY>::THREADS, f3t_min_blocks<TY>())
     const Fused3Args *sA = reinterpret_cast<const Fused3Args *>(f3_smem + F3T_ARGB);
     const long long t = b - B.item0;
     const int bx = (int)(t % B.tx), by = (int)((t / B.tx) % B.ty), bz = (int)(t / ((long long)B.tx * B.ty));
-    f3t_tile<TY>(B.m, *sA, *sG, bx, by, bz, B.kch, nd, (unsigned)((long long)B.tx * B.ty * B.tz), err, f3_smem);
+    const int k0 = 1 + bz * B.kch, k1 = min(sG->L.nz, k0 + B.kch - 1);
+    f3t_tile<TY, F3T_MIXED>(B.m, *sA, *sG, bx, by, k0, k1, nd, (unsigned)((long long)B.tx * B.ty * B.tz), err,
+                            f3_smem);
 }
 
 }  // namespace omx

@@ -212,9 +212,17 @@ inline int f3t_ring(int form) { return form >= 200 ? form / 100 : F3T_RING_DEFAU
 // dynamic shared memory of a fused 3D block of this form (bytes)
 int f3t_smem_bytes(int form);
 bool encode_f3t_maps(F3tMaps *M, const FieldPtrs<float> &in, const Lay &L, int ty);
-// form: tile rows (8 or 16); kch: planes per block (0 = default); err: the device error word
-cudaError_t launch_fused3t(const F3tMaps &M, const Fused3Args &A, const GridArgs<float> &G, int form, int kch,
-                           int *err, void *stream);
+// The fused 3D pass's lean runs (no CPML, media or plane source at them) in one launch over n
+// runs {bx, by, k0, k1} (tile, planes k0..k1) of one grid.  form: ring depth x 100 + tile rows;
+// err: the device error word.  The launch advances the device-loop step counter when
+// G.step_inc is set.
+cudaError_t launch_fused3t_lean(const F3tMaps &M, const Fused3Args &A, const GridArgs<float> &G, int form,
+                                const int4 *items, int n, int *err, void *stream);
+// The general runs of the fused 3D pass through the two plain kernels: new H (e_half = false;
+// reads the in set only) or new E (e_half = true; after every new H of the step is written; it
+// advances the device-loop step counter when G.step_inc is set).
+cudaError_t launch_fused3t_general(const Fused3Args &A, const GridArgs<float> &G, int form, const int4 *items, int n,
+                                   bool e_half, void *stream);
 // the batched pass over n grids (device table, largest grid first) with `blocks` blocks in all
 cudaError_t launch_fused3t_batch(const F3tBatchGrid *grids, int n, long long blocks, int form, int *err,
                                  void *stream);

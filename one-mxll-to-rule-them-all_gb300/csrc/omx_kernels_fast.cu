@@ -166,7 +166,8 @@ static PFN_cuTensorMapEncodeTiled_v12000 f3t_encode_fn()
 bool encode_f3t_maps(F3tMaps *M, const FieldPtrs<float> &in, const Lay &L, int ty)
 {
     auto fn = f3t_encode_fn();
-    if (!fn || L.dims != 3 || L.off < 3) return false;
+    // a row must hold cells -3 .. nx+1 (the boxes start 3 cells before a tile; E of cell nx+1)
+    if (!fn || L.dims != 3 || L.off < 3 || L.px < L.nx + 5) return false;
     const cuuint64_t dims[3] = {(cuuint64_t)L.px, (cuuint64_t)(L.ny + 2), (cuuint64_t)(L.nz + 2)};
     const cuuint64_t strides[2] = {(cuuint64_t)L.px * 4u, (cuuint64_t)L.pz * 4u};
     const cuuint32_t box[3] = {(cuuint32_t)F3T_BX, (cuuint32_t)(ty + 2), 1u};
@@ -195,18 +196,34 @@ template <class K> static cudaError_t f3t_smem_attr(K kernel, int *have, int byt
     return e;
 }
 
-template <int TY>
-static cudaError_t launch_f3t(const F3tMaps &M, const Fused3Args &A, const GridArgs<float> &G, int kch, int nd,
-                              int *err, cudaStream_t s)
+template <int TY, int MODE>
+static cudaError_t launch_f3t(const F3tMaps &M, const Fused3Args &A, const GridArgs<float> &G, const int4 *items,
+                              int n, int nd, int *err, cudaStream_t s)
 {
     using S = F3tShape<TY>;
     static int have[FZ_MAX_DEV] = {};
     const int bytes = S::smem(nd);
-    const cudaError_t e = f3t_smem_attr(k_fused3_tma<TY>, have, bytes);
+    const cudaError_t e = f3t_smem_attr(k_fused3_tma<TY, MODE>, have, bytes);
     if (e != cudaSuccess) return e;
-    const int m = kch > 0 ? std::min(kch, F3T_KMAX) : 64;
-    const dim3 g((unsigned)((G.L.nx + 31) / 32), (unsigned)((G.L.ny + TY - 1) / TY), (unsigned)((G.L.nz + m - 1) / m));
-    k_fused3_tma<TY><<<g, S::THREADS, bytes, s>>>(M, A, G, m, nd, err);
+    if (n <= 0) return cudaSuccess;
+    k_fused3_tma<TY, MODE><<<(unsigned)n, S::THREADS, bytes, s>>>(M, A, G, items, nd, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fused3t_general(const Fused3Args &A, const GridArgs<float> &G, int form, const int4 *items, int n,
+                                   bool e_half, void *sv)
+{
+    if (n <= 0) return cudaSuccess;
+    const cudaStream_t s = (cudaStream_t)sv;
+    const int ty = f3t_rows(form);
+    const dim3 b(32, (unsigned)ty);
+    if (ty == 16) {
+        if (e_half) k_f3g_e<16><<<(unsigned)n, b, 0, s>>>(A, G, items);
+        else k_f3g_h<16><<<(unsigned)n, b, 0, s>>>(A, G, items);
+    } else {
+        if (e_half) k_f3g_e<8><<<(unsigned)n, b, 0, s>>>(A, G, items);
+        else k_f3g_h<8><<<(unsigned)n, b, 0, s>>>(A, G, items);
+    }
     return cudaGetLastError();
 }
 
@@ -215,12 +232,13 @@ int f3t_smem_bytes(int form)
     return f3t_rows(form) == 16 ? F3tShape<16>::smem(f3t_ring(form)) : F3tShape<8>::smem(f3t_ring(form));
 }
 
-cudaError_t launch_fused3t(const F3tMaps &M, const Fused3Args &A, const GridArgs<float> &G, int form, int kch,
-                           int *err, void *s)
+cudaError_t launch_fused3t_lean(const F3tMaps &M, const Fused3Args &A, const GridArgs<float> &G, int form,
+                                const int4 *items, int n, int *err, void *sv)
 {
     const int nd = f3t_ring(form);
-    if (f3t_rows(form) == 16) return launch_f3t<16>(M, A, G, kch, nd, err, (cudaStream_t)s);
-    return launch_f3t<8>(M, A, G, kch, nd, err, (cudaStream_t)s);
+    const cudaStream_t s = (cudaStream_t)sv;
+    if (f3t_rows(form) == 16) return launch_f3t<16, F3T_LEAN_ONLY>(M, A, G, items, n, nd, err, s);
+    return launch_f3t<8, F3T_LEAN_ONLY>(M, A, G, items, n, nd, err, s);
 }
 
 template <int TY>

@@ -249,6 +249,7 @@ def _fused3_ran(g, deck):
     ((64, 24, 20), (3, 3, 2), "plane", 90),    # periodic z: plane 0 is the image of plane nz
     ((33, 17, 19), (1, 1, 1), "both", 80),     # PEC box, odd sizes, a radial source after the pass
     ((48, 40, 70), (3, 1, 3), "plane", 100),   # several planes chunks along z
+    ((62, 20, 18), (1, 1, 3), "plane", 60),    # PEC x: the last tile's lean planes reach the row's end
 ])
 def test_fp32_fused3d(orc_mod, n, boundaries, src, steps):
     """The FP32 single-pass 3D step (k_fused3_tma, the default 3D FP32 form when x and y are not
