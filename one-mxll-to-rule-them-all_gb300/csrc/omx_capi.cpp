@@ -295,11 +295,15 @@ struct omx_ctx {
     bool fold3 = false;         // the fused 3D pass adds the single plane source (fold3_of)
     F3tMaps f3maps[2][2];       // tensor maps of the fused 3D pass: [in set][tile rows 8 / 16]
     const void *f3key[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};   // Ex buffer they were made for
-    // runs {bx, by, k0, k1} of the fused 3D pass (general runs first, then lean ones) for the
-    // tile rows / planes per block / plane-source setting in f3plan_key
-    DevBuf<int4> f3items;
-    int f3n_gen = 0, f3n_lean = 0;
-    long long f3plan_key = -1;
+    // runs {bx, by, k0, k1} of the fused 3D pass (general runs first, then lean ones), one list per
+    // tile rows / planes per block / plane-source setting (kept: the autotuner switches between
+    // them without uploading again); f3cur is the list of the current shape
+    struct F3Plan {
+        DevBuf<int4> items;
+        int n_gen = 0, n_lean = 0;
+    };
+    std::map<long long, std::unique_ptr<F3Plan>> f3plans;
+    F3Plan *f3cur = nullptr;
     std::vector<short> hl[3][2];   // host copies of the CPML layer tables (lE, lH per axis)
     int step_form = OMX_STEP_DEFAULT;   // omx_set_step_form; a batch sets TWO_PASS on its members
     int *run_step = nullptr;    // device step counter while omx_run issues a step sequence
@@ -1164,7 +1168,11 @@ void f3t_plan(omx_ctx *c)
     const int kch = c->march > 0 ? std::min(c->march, F3T_KMAX) : 64;
     const bool pl = c->fold3 && !c->sources.empty();
     const long long key = ((long long)ty * 1000 + kch) * 2 + (pl ? 1 : 0);
-    if (c->f3plan_key == key) return;
+    auto hit = c->f3plans.find(key);
+    if (hit != c->f3plans.end()) {
+        c->f3cur = hit->second.get();
+        return;
+    }
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     ck(cudaStreamIsCapturing(c->stream, &cs), "capture status");
     if (cs != cudaStreamCaptureStatusNone)
@@ -1194,18 +1202,23 @@ void f3t_plan(omx_ctx *c)
                 lk[k] = !xy && !plxy && !slab(2, k) && !(pl_axis == 2 && k == pl_index) &&
                         !(mb && k >= c->bb0[2] && k <= c->bb1[2]);
             for (int k = 1; k <= nz;) {
+                // general runs in short pieces: their plain kernels march a thread per column,
+                // so more pieces are more threads in flight
+                const int cap = lk[k] ? kch : std::min(kch, F3T_GEN_KCH);
                 int e = k;
-                while (e < nz && lk[e + 1] == lk[k] && e - k + 1 < kch) ++e;
+                while (e < nz && lk[e + 1] == lk[k] && e - k + 1 < cap) ++e;
                 (lk[k] ? lean : gen).push_back(make_int4(bx, by, k, e));
                 k = e + 1;
             }
         }
     std::vector<int4> all(gen);
     all.insert(all.end(), lean.begin(), lean.end());
-    c->f3items.upload(all);
-    c->f3n_gen = (int)gen.size();
-    c->f3n_lean = (int)lean.size();
-    c->f3plan_key = key;
+    std::unique_ptr<omx_ctx::F3Plan> P(new omx_ctx::F3Plan);
+    P->items.upload(all);
+    P->n_gen = (int)gen.size();
+    P->n_lean = (int)lean.size();
+    c->f3cur = P.get();
+    c->f3plans[key] = std::move(P);
 }
 
 // One FP32 fused step: the H+E pass from the current buffer set into the other.  2D TMz: then
@@ -1247,12 +1260,12 @@ template <> void fused_step<float>(omx_ctx *c, bool ade, const StepParam *plane)
             c->f3key[in][t] = Fin.f[0];
         }
         f3t_plan(c);
-        const int4 *items = c->f3items.p;
+        const int4 *items = c->f3cur->items.p;
         // general runs (CPML, media, plane source): new H on f3aux beside the lean runs' fused
         // launch on the stream, then new E on the stream once both have written their new H; the E
         // launch (the pass's only reader of the step's scalars) advances the device-loop step
         // counter, or the lean launch when there are no general runs
-        const int ng = c->f3n_gen, nl = c->f3n_lean;
+        const int ng = c->f3cur->n_gen, nl = c->f3cur->n_lean;
         GridArgs<float> Gq = G;
         Gq.step_inc = nullptr;
         Gq.step_done = nullptr;

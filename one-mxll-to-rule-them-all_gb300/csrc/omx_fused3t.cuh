@@ -811,6 +811,7 @@ __global__ void __launch_bounds__(32 * TY) k_f3g_h(Fused3Args A, GridArgs<float>
     const int bz0 = (i - 1) + L.nx * (j - 1), sX = G.L2 * L.ny, sY = L.nx * G.L2, sZ = L.nx * L.ny;
     const int px_ = L.px, pz_ = (int)L.pz;
     int idx = (int)L.off + i + px_ * j + pz_ * it.z;   // element offsets < 2^31 (checked by the host)
+#pragma unroll 2
     for (int k = it.z; k <= it.w; ++k, idx += pz_) {
         const int kp = (perz && k == L.nz) ? idx - (L.nz - 1) * pz_ : idx + pz_;   // E of plane k + 1
         const float ex_c = Ex[idx], ey_c = Ey[idx], ez_c = Ez[idx];
