@@ -1725,14 +1725,22 @@ template <class R> void run_impl(omx_ctx *c, int tt0, int nsteps, int n_skip, in
     };
     // the fused path alternates buffer sets, so its graphs cover an even number of steps; long
     // graphs keep the side stream's work overlapped across all but one step boundary per graph.
-    // A run of up to 64 steps is one graph (an odd fused run: one graph of the even part and a
-    // one-step graph), a longer run repeats a 16-step graph.
-    const int per_graph = (fused || split) ? (nsteps > 64 ? 16 : (fused ? (nsteps & ~1) : nsteps)) : 1;
+    // A run of 8 steps or more starts with a two-step graph, which the host submits quickly and
+    // the device runs while the host submits the long one (a long graph's submission takes tens
+    // of microseconds, during which the device would otherwise wait); then up to 64 steps are one
+    // graph (an odd fused run: one graph of the even part and a one-step graph), a longer run
+    // repeats a 16-step graph.
     if (use_graph && !c->prof) {
-        const int ngraph = per_graph > 0 ? nsteps / per_graph : 0;
         const int k = prepare_only ? 0 : 1;
+        int left = nsteps;
+        if ((fused || split) && left >= 8) {
+            launch_graph(2, k);
+            left -= 2;
+        }
+        const int per_graph = (fused || split) ? (left > 64 ? 16 : (fused ? (left & ~1) : left)) : 1;
+        const int ngraph = per_graph > 0 ? left / per_graph : 0;
         if (ngraph > 0) launch_graph(per_graph, k * ngraph);
-        int left = nsteps - ngraph * per_graph;
+        left -= ngraph * per_graph;
         if (left >= 2) launch_graph(2, k * (left / 2));
         if (left % 2) launch_graph(1, k);
     } else if (!prepare_only) {

@@ -77,6 +77,40 @@ def train(closure, e, d, steps, B=1024, T=16, lr=1e-3, skip=4, seed=0, log=None)
     return losses
 
 
+def trajectory_batches(e, d, B, rng):
+    """Whole trajectories from the ground state: inputs e[B][L], targets [L - W + 1][B] (the dipole
+    after each step from the W-th on).  The network's state starts at zero with the emitter's,
+    as in a simulation, so back-propagation runs through the whole history it must remember."""
+    n = e.shape[0]
+    while True:
+        rows = rng.integers(0, n, B)
+        yield np.ascontiguousarray(e[rows], np.float32), np.ascontiguousarray(d[rows][:, W - 1:].T, np.float32)
+
+
+def train_trajectories(closure, e, d, steps, B=256, lr=3e-4, skip=4, seed=0, log=None):
+    """Adam steps of the tensor-core training step on whole trajectories; returns the losses."""
+    rng = np.random.default_rng(seed)
+    gen = trajectory_batches(e, d, B, rng)
+    losses = []
+    for k in range(steps):
+        eb, db = next(gen)
+        losses.append(closure.train_step(eb, db, lr, skip))
+        if log and (k % 100 == 0 or k == steps - 1):
+            log(k, losses[-1])
+    return losses
+
+
+def trajectory_errors(predict, e, d, skip=4):
+    """Errors of a dipole predictor on whole trajectories e, d [n][L]: predict(e) -> [L - W + 1][n].
+    Returns (rms, max): root-mean-square and largest |prediction - target|, both relative to the
+    targets' root-mean-square / largest |value| (steps after the first `skip` scored)."""
+    t = d[:, W - 1:].T[skip:]
+    y = predict(np.ascontiguousarray(e, np.float32))[skip:]
+    rms = float(np.sqrt(np.mean((y - t) ** 2)) / max(np.sqrt(np.mean(t ** 2)), 1e-30))
+    mx = float(np.max(np.abs(y - t)) / max(np.max(np.abs(t)), 1e-30))
+    return rms, mx
+
+
 def new_closure(seed=0):
     """A closure with the oracle's initialisation rule (uniform +-1/sqrt(fan_in), update gate biased
     to keep its state) and the training data's scales."""
