@@ -1158,10 +1158,14 @@ template <class R> void do_sample(omx_ctx *c, StepParam slot, StepParam time)
     c->launches++;
 }
 
-// The runs of the fused 3D pass: each tile's planes 1..nz split where the plane form changes
-// (the device's test, restated: a CPML slab of x or y at the tile's own or halo cells, a z slab at
-// the plane, a media-box cell of the tile's part of the plane, the folded plane source), then
-// into pieces of at most kch planes.  General runs come first in the list.
+// The runs of the fused 3D pass.  Lean tiles (32 x ty columns, i0 = 1 mod 32) cover the columns
+// and rows away from the x / y CPML slabs (own and halo cells);
+// each of them is split along k where the plane form changes (the device's test, restated: a z
+// slab at the plane, a media-box cell of the tile's part of the plane, the folded plane source)
+// into lean and general runs of at most kch / F3T_GEN_KCH planes.  The columns and rows left at
+// the edges (the slabs and what the alignment leaves beside them) are general on every plane, in
+// pieces of at most 32 x ty columns.  General runs come first in the list; a general run packs
+// its width and height as {i0 | w << 20, j0 | h << 20, k0, k1}, a lean run is {i0, j0, k0, k1}.
 void f3t_plan(omx_ctx *c)
 {
     const int ty = f3t_rows(c->fused_form);
@@ -1185,21 +1189,63 @@ void f3t_plan(omx_ctx *c)
         pl_index = S.pd.plane_index;
     }
     auto slab = [&](int a, int p) { return c->hl[a][0][p] >= 0 || c->hl[a][1][p] >= 0; };
+    // clear(a, p0, p1): no slab of axis a at cells p0..p1 (clipped to the grid)
+    auto clear = [&](int a, int p0, int p1) {
+        for (int p = std::max(1, p0); p <= std::min(c->n[a], p1); ++p)
+            if (slab(a, p)) return false;
+        return true;
+    };
+    // lean tile origins along one axis: width w, origins = 1 mod align, own and halo cells clear
+    auto lean_origins = [&](int a, int w, int align) {
+        std::vector<int> o;
+        int p = 1;
+        while (p <= c->n[a]) {
+            if ((p - 1) % align == 0 && clear(a, p - 1, p + w - 1)) {
+                o.push_back(p);
+                p += w;
+            } else {
+                ++p;
+            }
+        }
+        return o;
+    };
+    // x origins at 1 mod 32: the new fields' rows then go out in whole 128-byte lines (a tile
+    // shifted off them writes partial 32-byte sectors, which measured 30 % slower at 512^3)
+    const std::vector<int> ox = lean_origins(0, 32, 32), oy = lean_origins(1, ty, 1);
+    // the other cells of an axis as pieces of at most w: [start, length]
+    auto rest = [&](const std::vector<int> &o, int n, int w) {
+        std::vector<std::pair<int, int>> r;
+        int p = 1;
+        size_t t = 0;
+        while (p <= n) {
+            if (t < o.size() && o[t] == p) {
+                p += w;
+                ++t;
+                continue;
+            }
+            const int end = t < o.size() ? o[t] - 1 : n;
+            for (int q = p; q <= end; q += w) r.push_back({q, std::min(w, end - q + 1)});
+            p = end + 1;
+        }
+        return r;
+    };
+    const auto rx = rest(ox, nx, 32), ry = rest(oy, ny, ty);
     const bool box = c->bb1[0] >= c->bb0[0] && c->bb1[1] >= c->bb0[1] && c->bb1[2] >= c->bb0[2];
     std::vector<int4> gen, lean;
+    const int gk = std::min(kch, F3T_GEN_KCH);
+    auto general_column = [&](int i0, int w, int j0, int h) {
+        for (int k = 1; k <= nz; k += gk) gen.push_back(make_int4(i0 | (w << 20), j0 | (h << 20), k, std::min(nz, k + gk - 1)));
+    };
     std::vector<char> lk(nz + 1);
-    for (int by = 0; by * ty < ny; ++by)
-        for (int bx = 0; bx * 32 < nx; ++bx) {
-            const int i0 = 1 + 32 * bx, j0 = 1 + ty * by;
-            bool xy = false;
-            for (int i = std::max(1, i0 - 1); i <= std::min(nx, i0 + 31); ++i) xy = xy || slab(0, i);
-            for (int j = std::max(1, j0 - 1); j <= std::min(ny, j0 + ty - 1); ++j) xy = xy || slab(1, j);
+    for (int j0 : oy)
+        for (int i0 : ox) {
+            const int h = std::min(ty, ny - j0 + 1), w = std::min(32, nx - i0 + 1);
             const bool mb = box && c->bb0[0] <= i0 + 31 && c->bb1[0] >= i0 && c->bb0[1] <= j0 + ty - 1 &&
                             c->bb1[1] >= j0;
             const bool plxy = (pl_axis == 0 && pl_index >= i0 && pl_index <= i0 + 31) ||
                               (pl_axis == 1 && pl_index >= j0 && pl_index <= j0 + ty - 1);
             for (int k = 1; k <= nz; ++k)
-                lk[k] = !xy && !plxy && !slab(2, k) && !(pl_axis == 2 && k == pl_index) &&
+                lk[k] = !plxy && !slab(2, k) && !(pl_axis == 2 && k == pl_index) &&
                         !(mb && k >= c->bb0[2] && k <= c->bb1[2]);
             for (int k = 1; k <= nz;) {
                 // general runs in short pieces: their plain kernels march a thread per column,
@@ -1207,10 +1253,21 @@ void f3t_plan(omx_ctx *c)
                 const int cap = lk[k] ? kch : std::min(kch, F3T_GEN_KCH);
                 int e = k;
                 while (e < nz && lk[e + 1] == lk[k] && e - k + 1 < cap) ++e;
-                (lk[k] ? lean : gen).push_back(make_int4(bx, by, k, e));
+                if (lk[k]) lean.push_back(make_int4(i0, j0, k, e));
+                else gen.push_back(make_int4(i0 | (w << 20), j0 | (h << 20), k, e));
                 k = e + 1;
             }
         }
+    // the edges: every (x piece, y piece) pair with at least one piece outside the lean tiles
+    std::vector<std::pair<int, int>> px, py;
+    for (int i0 : ox) px.push_back({i0, std::min(32, nx - i0 + 1)});
+    for (int j0 : oy) py.push_back({j0, std::min(ty, ny - j0 + 1)});
+    for (const auto &x : rx)
+        for (const auto &y : py) general_column(x.first, x.second, y.first, y.second);
+    for (const auto &y : ry) {
+        for (const auto &x : px) general_column(x.first, x.second, y.first, y.second);
+        for (const auto &x : rx) general_column(x.first, x.second, y.first, y.second);
+    }
     std::vector<int4> all(gen);
     all.insert(all.end(), lean.begin(), lean.end());
     std::unique_ptr<omx_ctx::F3Plan> P(new omx_ctx::F3Plan);

@@ -330,14 +330,15 @@ __device__ __forceinline__ void f3t_prefetch(const void *p)
 // compiled in, which keeps the lean form's registers to itself).
 enum { F3T_MIXED = 0, F3T_LEAN_ONLY = 1 };
 
-// One block's work: tile (bx, by) of 32 x TY columns over planes k0 .. k1 of one grid.  maps: the
+// One block's work: the tile of 32 x TY columns from (i0, j0) over planes k0 .. k1 of one grid
+// (i0 = 1 mod 4: the staged box starts at i0 - 4 on a 16-byte boundary).  maps: the
 // in set's tensor maps (kernel parameter or global memory); A, G: the grid's arguments (in
 // shared memory); nblk: the blocks of this launch (the last of them to finish advances the
 // grid's device-loop step counter, when G.step_inc is set); smem: the dynamic shared memory
 // (1024-byte aligned).
 template <int TY, int MODE>
 __device__ __forceinline__ void f3t_tile(const CUtensorMap *maps, const Fused3Args &A, const GridArgs<float> &G,
-                                         int bx, int by, int k0, int k1, int nd, unsigned nblk, int *err,
+                                         int i0, int j0, int k0, int k1, int nd, unsigned nblk, int *err,
                                          unsigned char *f3_smem)
 {
     using S = F3tShape<TY>;
@@ -351,7 +352,6 @@ __device__ __forceinline__ void f3t_tile(const CUtensorMap *maps, const Fused3Ar
     uint64_t *empty = full + nd;
     const Lay &L = G.L;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int i0 = 1 + bx * 32, j0 = 1 + by * TY;
     const bool perz = G.per[2] != 0;
     // staged planes pa .. k1+1; pa = k0-1 when the new H of plane k0-1 is needed (k0 > 1, or the
     // periodic image of plane 0), else k0 (plane 0 is the PEC ghost: new H = 0)
@@ -400,7 +400,7 @@ __device__ __forceinline__ void f3t_tile(const CUtensorMap *maps, const Fused3Ar
             float *dst = ring + (size_t)s * (S::SLOTB / 4);
 #pragma unroll
             for (int c = 0; c < 6; ++c)
-                tma_load_3d(dst + c * CB, &maps[c], 32 * bx, j0 - 1, z, &full[s]);
+                tma_load_3d(dst + c * CB, &maps[c], i0 - 1, j0 - 1, z, &full[s]);
             if (++s == nd) {
                 s = 0;
                 ++round;
@@ -772,7 +772,7 @@ __device__ __forceinline__ void f3t_args_to_smem(const GridArgs<float> &G, const
     __syncthreads();
 }
 
-// One launch over a list of runs (tile, planes k0 .. k1): block b takes items[b].  nd: ring depth
+// One launch over a list of runs {i0, j0, k0, k1} (tile origin, planes): block b takes items[b].  nd: ring depth
 // (the dynamic shared memory holds F3tShape<TY>::smem(nd) bytes).
 template <int TY, int MODE>
 __global__ void __launch_bounds__(F3tShape<TY>::THREADS, f3t_min_blocks<TY>())
@@ -789,7 +789,8 @@ __global__ void __launch_bounds__(F3tShape<TY>::THREADS, f3t_min_blocks<TY>())
 
 // ---- general runs: the two-kernel form -----------------------------------------------------
 // Runs whose planes need CPML psi, the media box or the plane source are updated by two plain
-// kernels, one thread per (i, j) column of the run's 32 x TY tile marching its planes: new H (from
+// kernels, one thread per (i, j) column of the run's tile marching its planes (a run {i0 | w << 20,
+// j0 | h << 20, k0, k1}: w <= 32 columns from i0, h <= TY rows from j0): new H (from
 // the in set, psi in -> out) and then new E (from the out set's new H), with the same device
 // functions as the fused pass, so each cell gets the same bits whichever kernel updates it.  The
 // H kernel runs beside the lean fused launch; the E kernel after both (it reads the new H of
@@ -799,8 +800,8 @@ __global__ void __launch_bounds__(32 * TY) k_f3g_h(Fused3Args A, GridArgs<float>
 {
     const int4 it = items[blockIdx.x];
     const Lay L = G.L;
-    const int i = 1 + 32 * it.x + (int)threadIdx.x, j = 1 + TY * it.y + (int)threadIdx.y;
-    if (i > L.nx || j > L.ny) return;
+    const int i = (it.x & 0xfffff) + (int)threadIdx.x, j = (it.y & 0xfffff) + (int)threadIdx.y;
+    if ((int)threadIdx.x >= (it.x >> 20) || (int)threadIdx.y >= (it.y >> 20) || i > L.nx || j > L.ny) return;
     const bool perz = G.per[2] != 0;
     const float *__restrict__ Ex = A.in.f[0];
     const float *__restrict__ Ey = A.in.f[1];
@@ -843,8 +844,8 @@ __global__ void __launch_bounds__(32 * TY) k_f3g_e(Fused3Args A, GridArgs<float>
 {
     const int4 it = items[blockIdx.x];
     const Lay L = G.L;
-    const int i = 1 + 32 * it.x + (int)threadIdx.x, j = 1 + TY * it.y + (int)threadIdx.y;
-    if (i <= L.nx && j <= L.ny) {
+    const int i = (it.x & 0xfffff) + (int)threadIdx.x, j = (it.y & 0xfffff) + (int)threadIdx.y;
+    if ((int)threadIdx.x < (it.x >> 20) && (int)threadIdx.y < (it.y >> 20) && i <= L.nx && j <= L.ny) {
         const float *__restrict__ Hx = A.out.f[3];
         const float *__restrict__ Hy = A.out.f[4];
         const float *__restrict__ Hz = A.out.f[5];
@@ -914,7 +915,8 @@ __global__ void __launch_bounds__(F3tShape<TY>::THREADS, f3t_min_blocks<TY>())
     const long long t = b - B.item0;
     const int bx = (int)(t % B.tx), by = (int)((t / B.tx) % B.ty), bz = (int)(t / ((long long)B.tx * B.ty));
     const int k0 = 1 + bz * B.kch, k1 = min(sG->L.nz, k0 + B.kch - 1);
-    f3t_tile<TY, F3T_MIXED>(B.m, *sA, *sG, bx, by, k0, k1, nd, (unsigned)((long long)B.tx * B.ty * B.tz), err,
+    f3t_tile<TY, F3T_MIXED>(B.m, *sA, *sG, 1 + 32 * bx, 1 + TY * by, k0, k1, nd,
+                            (unsigned)((long long)B.tx * B.ty * B.tz), err,
                             f3_smem);
 }
 
