@@ -614,6 +614,19 @@ def cfg5_decks(count, side_min=64, side_max=256):
     return [decks.deck_cfg5_instance(n, seed=CFG5_SEED + 1 + k) for k, n in enumerate(sides)], sides
 
 
+def batch_shape_text(shape):
+    """(the fused batched pass, its tile) from omx_batch_autotune's choice."""
+    if shape < 1000:
+        return "the two half-step passes of every grid (k_batch3)", "tile depth %d" % shape
+    form = shape // 1000 % 1000
+    tile = "tile 32 x %d, %d planes per block, ring of %d planes" % (form % 100, shape % 1000, form // 100 or 4)
+    if shape >= 1000000:
+        return ("the fused pass of every grid split by plane form: the general runs' new H (k_f3g_h_batch) "
+                "on a second stream beside one launch of every grid's lean runs (k_fused3_batch_lean), "
+                "then the general runs' new E (k_f3g_e_batch)"), tile
+    return "one k_fused3_batch launch per step over every grid's tiles (largest grid first)", tile
+
+
 def gpu_arm_cfg5(args, dist):
     import numpy as np
 
@@ -691,18 +704,15 @@ def gpu_arm_cfg5(args, dist):
                        "cells": cells, "sides": sides, "precision": "fp32",
                        "parallelism": f"replicas x{dist.world}" if dist.world > 1 else "single GPU",
                        "l2": "working set %.1f GB > 126 MB L2, no flush" % (cells * 6 * 4 / 1e9),
-                       "loop": "omx_batch_run: one k_fused3_batch launch per step over every grid's tiles "
-                               "(largest grid first), the steps captured in CUDA graphs; tile %s from "
-                               "omx_batch_autotune" % ("32 x %d, %d planes per block, ring of %d planes" % (shape // 1000 % 100, shape % 1000,
-                                                                               shape // 100000 or 4)
-                                                       if shape >= 1000 else "depth %d" % shape),
+                       "loop": "omx_batch_run: %s, the steps captured in CUDA graphs; shape from "
+                               "omx_batch_autotune: %s" % batch_shape_text(shape),
                        "timing": "wall clock around omx_batch_run + omx_batch_synchronize"},
             "one_at_a_time": {"value": solo_value, "unit": "Gcell-updates/s",
                               "how": "the same grids, each its own omx_run (CUDA graph), run one after another",
                               "batch_speedup": value / solo_value,
                               "detector_traces_bit_identical": same,
                               "arithmetic": "one fused pass per grid and step, as the batch"},
-            "roofline": {"bound": "hbm", "kernel": "k_fused3_batch (the fused pass of every grid in one launch)",
+            "roofline": {"bound": "hbm", "kernel": batch_shape_text(shape)[0],
                          "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": None, "peak_source": peak_kind,
                          "algorithmic_bytes_per_step": alg,

@@ -332,19 +332,30 @@ int omx_set_launch_shape(omx_ctx *ctx, int shape);
 
 /* ---- batched multi-grid runs (no counterpart in the reference: it runs one grid per process) -
  * A batch groups n configured 3D contexts of one precision on the current device (for example
- * the instances of a parameter sweep).  omx_batch_run advances all of them together: each step
- * runs ONE persistent launch for the H pass of every grid (its blocks walk a list of all grids'
- * tiles), one launch per round of radial sources (round r: source r of every grid), the
- * dispersive cells, ONE launch for the bulk E pass of every grid, the per-grid emitter work and
- * one launch for the detectors of every grid; use_graph != 0 captures that step once and
- * replays it.  Every grid computes exactly what omx_run computes for it alone (same kernels,
+ * the instances of a parameter sweep).  omx_batch_run advances all of them together.  When every
+ * member steps with the fused FP32 3D pass, each step runs that pass for every grid at once (one
+ * launch over all grids' tiles, or the pass split by plane form: the general runs' new H on a
+ * second stream beside one launch of every grid's lean runs, then the general runs' new E), one
+ * launch per round of the other sources, the per-grid emitter work and one launch for the
+ * detectors of every grid.  Otherwise each step runs ONE persistent launch for the H pass of
+ * every grid (its blocks walk a list of all grids' tiles), one launch per round of radial sources
+ * (round r: source r of every grid), the dispersive cells, ONE launch for the bulk E pass of every
+ * grid, the per-grid emitter work and the detectors.  use_graph != 0 captures that step once and
+ * replays it.  Every grid computes exactly what omx_run computes for it alone (same arithmetic,
  * same per-grid order).  The contexts stay owned by the caller and must outlive the batch; while
  * omx_batch_run executes, their launches go to the batch's stream. */
 typedef struct omx_batch omx_batch;
 int omx_batch_create(omx_ctx *const *ctxs, int n, omx_batch **out);
-/* Tile depth (z planes per tile: 4, 8, 16 or 32) of the batched passes, timed `reps` times each
- * on the initial zero fields; same preconditions as omx_autotune.  *choice may be NULL. */
+/* The launch shape of the batched passes, each candidate timed `reps` times on the initial zero
+ * fields; same preconditions as omx_autotune.  *choice (may be NULL) is the tile depth (z planes
+ * per tile: 4, 8, 16 or 32) of the two half-step passes, or for the fused pass
+ * split x 1000000 + (ring depth x 100 + tile rows) x 1000 + planes per block, split 1 for the pass
+ * split by plane form and ring depth 0 for the default of 4 planes. */
 int omx_batch_autotune(omx_batch *batch, int reps, int *choice);
+/* No counterpart in the reference: sets the launch shape of the batched passes, encoded as
+ * omx_batch_autotune's choice (a fused shape when every member steps with the fused FP32 pass,
+ * else a tile depth); OMX_ERR_ARG for a shape of the other kind or out of range. */
+int omx_batch_set_launch_shape(omx_batch *batch, int shape);
 int omx_batch_run(omx_batch *batch, int tt0, int nsteps, int n_skip_steps, int t_det_print,
                   int use_graph);
 /* No counterpart in the reference: builds the batch's tables and captures the step graphs that

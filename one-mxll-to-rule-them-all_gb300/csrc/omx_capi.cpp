@@ -1166,21 +1166,9 @@ template <class R> void do_sample(omx_ctx *c, StepParam slot, StepParam time)
 // the edges (the slabs and what the alignment leaves beside them) are general on every plane, in
 // pieces of at most 32 x ty columns.  General runs come first in the list; a general run packs
 // its width and height as {i0 | w << 20, j0 | h << 20, k0, k1}, a lean run is {i0, j0, k0, k1}.
-void f3t_plan(omx_ctx *c)
+void f3t_runs(const omx_ctx *c, int ty, int kch, std::vector<int4> &gen, std::vector<int4> &lean)
 {
-    const int ty = f3t_rows(c->fused_form);
-    const int kch = c->march > 0 ? std::min(c->march, F3T_KMAX) : 64;
     const bool pl = c->fold3 && !c->sources.empty();
-    const long long key = ((long long)ty * 1000 + kch) * 2 + (pl ? 1 : 0);
-    auto hit = c->f3plans.find(key);
-    if (hit != c->f3plans.end()) {
-        c->f3cur = hit->second.get();
-        return;
-    }
-    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-    ck(cudaStreamIsCapturing(c->stream, &cs), "capture status");
-    if (cs != cudaStreamCaptureStatusNone)
-        throw Fail{OMX_ERR_STATE, "fused 3D pass: its run list changed during a stream capture"};
     const int nx = c->n[0], ny = c->n[1], nz = c->n[2];
     int pl_axis = -1, pl_index = -1;
     if (pl) {
@@ -1231,10 +1219,10 @@ void f3t_plan(omx_ctx *c)
     };
     const auto rx = rest(ox, nx, 32), ry = rest(oy, ny, ty);
     const bool box = c->bb1[0] >= c->bb0[0] && c->bb1[1] >= c->bb0[1] && c->bb1[2] >= c->bb0[2];
-    std::vector<int4> gen, lean;
     const int gk = std::min(kch, F3T_GEN_KCH);
     auto general_column = [&](int i0, int w, int j0, int h) {
-        for (int k = 1; k <= nz; k += gk) gen.push_back(make_int4(i0 | (w << 20), j0 | (h << 20), k, std::min(nz, k + gk - 1)));
+        for (int k = 1; k <= nz; k += gk)
+            gen.push_back(make_int4(i0 | (w << 20), j0 | (h << 20), k, std::min(nz, k + gk - 1)));
     };
     std::vector<char> lk(nz + 1);
     for (int j0 : oy)
@@ -1268,6 +1256,26 @@ void f3t_plan(omx_ctx *c)
         for (const auto &x : px) general_column(x.first, x.second, y.first, y.second);
         for (const auto &x : rx) general_column(x.first, x.second, y.first, y.second);
     }
+}
+
+// The run list of the current launch shape, uploaded once per shape (f3cur).
+void f3t_plan(omx_ctx *c)
+{
+    const int ty = f3t_rows(c->fused_form);
+    const int kch = c->march > 0 ? std::min(c->march, F3T_KMAX) : 64;
+    const bool pl = c->fold3 && !c->sources.empty();
+    const long long key = ((long long)ty * 1000 + kch) * 2 + (pl ? 1 : 0);
+    auto hit = c->f3plans.find(key);
+    if (hit != c->f3plans.end()) {
+        c->f3cur = hit->second.get();
+        return;
+    }
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    ck(cudaStreamIsCapturing(c->stream, &cs), "capture status");
+    if (cs != cudaStreamCaptureStatusNone)
+        throw Fail{OMX_ERR_STATE, "fused 3D pass: its run list changed during a stream capture"};
+    std::vector<int4> gen, lean;
+    f3t_runs(c, ty, kch, gen, lean);
     std::vector<int4> all(gen);
     all.insert(all.end(), lean.begin(), lean.end());
     std::unique_ptr<omx_ctx::F3Plan> P(new omx_ctx::F3Plan);
@@ -3115,9 +3123,12 @@ template <class R> struct BatchTables {
     const BatchDet<R> *dets = nullptr;
     int ndet = 0;
     long long det_pts = 0;
-    // fused path: the grids of the batched pass (largest first) and its blocks
+    // fused path: the grids of the batched pass (largest first) and its blocks; the runs of the
+    // split pass (general runs, then lean runs, each with its grid's table index)
     const F3tBatchGrid *f3 = nullptr;
     long long f3_blocks = 0;
+    const int4 *f3gen = nullptr, *f3lean = nullptr;
+    int nf3gen = 0, nf3lean = 0;
 };
 
 struct omx_batch {
@@ -3130,11 +3141,17 @@ struct omx_batch {
     long long launches = 0;
     // device tables, one per step parity (the fused path alternates the members' buffer sets)
     DevBuf<unsigned char> dgrid[2], dsrc[2], ddet[2], df3[2];
+    DevBuf<int4> df3runs[2];
     cudaEvent_t done = nullptr;   // recorded after a batched call; member streams wait on it
     // 1: every member steps with one fused pass and the batch runs them in one k_fused3_batch
     // launch per step; 0: the two half-step passes (k_batch3); -1: not decided yet
     int fused = -1;
     int f3form = 8, f3kch = 64;   // tile rows and planes per block of the fused batched pass
+    // the fused batched pass split by plane form (general runs' H on `aux` beside the lean runs,
+    // then their E) instead of one k_fused3_batch launch
+    bool f3split = false;
+    cudaStream_t aux = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     // tables and captured step graphs, kept while the key (each member's configuration epoch,
     // buffer set, step table and the launch shapes) is unchanged
     std::vector<long long> key;
@@ -3286,6 +3303,7 @@ BatchTables<R> batch_tables(omx_batch *b, const std::vector<RunPlan> *plans, int
         T.dets = reinterpret_cast<const BatchDet<R> *>(b->ddet[q].p);
     }
     std::vector<F3tBatchGrid> f3g;
+    std::vector<int4> runs_gen, runs_lean;
     if constexpr (std::is_same<R, float>::value) {
         if (f3) {
             // the fused pass of every member in one launch, largest grid first
@@ -3327,6 +3345,16 @@ BatchTables<R> batch_tables(omx_batch *b, const std::vector<RunPlan> *plans, int
                 e.tz = (c->L.nz + e.kch - 1) / e.kch;
                 e.item0 = item;
                 item += (long long)e.tx * e.ty * e.tz;
+                // the grid's runs for the split pass, tagged with its place in the table
+                std::vector<int4> g0, l0;
+                f3t_runs(c, TY, e.kch, g0, l0);
+                const int gi = (int)f3g.size();
+                for (int4 &r : g0) r.w |= gi << 20;
+                for (int4 &r : l0) r.w |= gi << 20;
+                e.n_gen = (int)g0.size();
+                e.n_lean = (int)l0.size();
+                runs_gen.insert(runs_gen.end(), g0.begin(), g0.end());
+                runs_lean.insert(runs_lean.end(), l0.begin(), l0.end());
                 f3g.push_back(e);
             }
             b->df3[q].alloc(sizeof(F3tBatchGrid) * f3g.size(), false);
@@ -3335,6 +3363,13 @@ BatchTables<R> batch_tables(omx_batch *b, const std::vector<RunPlan> *plans, int
                "batch");
             T.f3 = reinterpret_cast<const F3tBatchGrid *>(b->df3[q].p);
             T.f3_blocks = item;
+            std::vector<int4> runs(runs_gen);
+            runs.insert(runs.end(), runs_lean.begin(), runs_lean.end());
+            b->df3runs[q].upload(runs);
+            T.f3gen = b->df3runs[q].p;
+            T.f3lean = b->df3runs[q].p + runs_gen.size();
+            T.nf3gen = (int)runs_gen.size();
+            T.nf3lean = (int)runs_lean.size();
         }
     }
     // the host vectors die here: wait for the copies that read them
@@ -3369,6 +3404,35 @@ struct BatchStreams {
     }
 };
 
+// The fused pass of every member: one k_fused3_batch launch, or the split pass (the general runs'
+// new H on the auxiliary stream while the lean runs go, then the general runs' new E).  Returns
+// the kernels launched.
+template <class R> long long batch_fused_pass(omx_batch *b, const BatchTables<R> &T, int form, bool split)
+{
+    const int n = (int)b->ctx.size();
+    int *err = b->ctx[0]->d_err.p;
+    if (!split) {
+        ck(launch_fused3t_batch(T.f3, n, T.f3_blocks, form, err, b->stream), "batched fused pass");
+        return 1;
+    }
+    if (T.nf3gen == 0) {
+        ck(launch_fused3t_batch_split(T.f3, T.f3gen, 0, T.f3lean, T.nf3lean, form, 2, err, b->stream),
+           "batched fused pass");
+        return T.nf3lean > 0 ? 1 : 0;
+    }
+    ck(cudaEventRecord(b->ev_fork, b->stream), "event");
+    ck(cudaStreamWaitEvent(b->aux, b->ev_fork, 0), "event");
+    ck(launch_fused3t_batch_split(T.f3, T.f3gen, T.nf3gen, T.f3lean, T.nf3lean, form, 1, err, b->aux),
+       "batched fused pass (general runs, H)");
+    ck(cudaEventRecord(b->ev_join, b->aux), "event");
+    ck(launch_fused3t_batch_split(T.f3, T.f3gen, T.nf3gen, T.f3lean, T.nf3lean, form, 2, err, b->stream),
+       "batched fused pass (lean runs)");
+    ck(cudaStreamWaitEvent(b->stream, b->ev_join, 0), "event");
+    ck(launch_fused3t_batch_split(T.f3, T.f3gen, T.nf3gen, T.f3lean, T.nf3lean, form, 4, err, b->stream),
+       "batched fused pass (general runs, E)");
+    return 2 + (T.nf3lean > 0 ? 1 : 0);
+}
+
 // One batched step: H of every grid in one launch, the sources, the dispersive cells and the
 // bulk E of every grid in one launch, the per-grid emitter work, the detectors in one launch.
 template <class R> long long batch_step(omx_batch *b, const BatchTables<R> &T, const std::vector<RunPlan> &plans,
@@ -3380,8 +3444,7 @@ template <class R> long long batch_step(omx_batch *b, const BatchTables<R> &T, c
         // the fused pass of every member (dispersive cells and folded plane sources inside), then
         // the work on the sets it wrote: the other sources, the emitter current and q-groups,
         // the detectors
-        ck(launch_fused3t_batch(T.f3, n, T.f3_blocks, b->f3form, b->ctx[0]->d_err.p, b->stream), "batched fused pass");
-        ++k;
+        k += batch_fused_pass(b, T, b->f3form, b->f3split);
         for (auto *c : b->ctx) c->cur ^= 1;
         for (size_t r = 0; r < T.src.size(); ++r) {
             if (T.nsrc[r] > 0) {
@@ -3477,7 +3540,7 @@ template <class R> void batch_run_impl(omx_batch *b, int tt0, int nsteps, int n_
     if (b->blocks == 0) b->blocks = batch3_blocks<R>();
     // the fused path alternates the members' buffer sets: step s of this call uses T[s & 1]
     const bool f3 = b->fused == 1;
-    std::vector<long long> key = {b->fused, kch, b->f3form, b->f3kch, b->blocks};
+    std::vector<long long> key = {b->fused, kch, b->f3form, b->f3kch, b->f3split, b->blocks};
     for (size_t i = 0; i < b->ctx.size(); ++i) {
         const omx_ctx *c = b->ctx[i];
         key.insert(key.end(), {(long long)c->epoch, c->cur, (long long)(uintptr_t)c->tab.p, plans[i].W,
@@ -3543,8 +3606,9 @@ template <class R> int batch_autotune_impl(omx_batch *b, int reps)
     if (b->blocks == 0) b->blocks = batch3_blocks<R>();
     const int n = (int)b->ctx.size();
     if (b->fused == 1) {
-        // fused batched pass: (ring depth x 100 + tile rows) x 1000 + planes per block, each
-        // candidate timed over `reps` launches on the zero initial fields (the pass maps them to zero)
+        // fused batched pass: split x 1000000 + (ring depth x 100 + tile rows) x 1000 + planes
+        // per block (split 1: the pass split by plane form, 0: one k_fused3_batch launch), each
+        // candidate timed over `reps` passes on the zero initial fields (the pass maps them to zero)
         cudaEvent_t e0, e1;
         ck(cudaEventCreate(&e0), "event");
         ck(cudaEventCreate(&e1), "event");
@@ -3554,34 +3618,33 @@ template <class R> int batch_autotune_impl(omx_batch *b, int reps)
         int dev = 0, optin = 0;
         ck(cudaGetDevice(&dev), "device");
         ck(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev), "device");
-        for (int ring : {0, 6, 8})
-            for (int ty : {8, 16})
-                for (int kch : {16, 32, 64, 128}) {
-                    const int form = ring * 100 + ty;
-                    if (f3t_smem_bytes(form) > optin) continue;
-                    b->f3form = form;
-                    b->f3kch = kch;
-                    const BatchTables<R> T = batch_tables<R>(b, nullptr, kch, 0);
-                    auto once = [&]() {
-                        ck(launch_fused3t_batch(T.f3, n, T.f3_blocks, form, b->ctx[0]->d_err.p, b->stream),
-                           "autotune");
-                    };
-                    once();
-                    ck(cudaEventRecord(e0, b->stream), "event");
-                    for (int r = 0; r < reps; ++r) once();
-                    ck(cudaEventRecord(e1, b->stream), "event");
-                    ck(cudaEventSynchronize(e1), "batch autotune");
-                    float ms = 0.f;
-                    ck(cudaEventElapsedTime(&ms, e0, e1), "batch autotune");
-                    if (first || ms < best) {
-                        best = ms;
-                        pick = form * 1000 + kch;
-                        first = false;
+        for (int split : {0, 1})
+            for (int ring : {0, 6, 8})
+                for (int ty : {8, 16})
+                    for (int kch : {16, 32, 64, 128}) {
+                        const int form = ring * 100 + ty;
+                        if (f3t_smem_bytes(form) > optin) continue;
+                        b->f3form = form;
+                        b->f3kch = kch;
+                        const BatchTables<R> T = batch_tables<R>(b, nullptr, kch, 0);
+                        auto once = [&]() { batch_fused_pass(b, T, form, split != 0); };
+                        once();
+                        ck(cudaEventRecord(e0, b->stream), "event");
+                        for (int r = 0; r < reps; ++r) once();
+                        ck(cudaEventRecord(e1, b->stream), "event");
+                        ck(cudaEventSynchronize(e1), "batch autotune");
+                        float ms = 0.f;
+                        ck(cudaEventElapsedTime(&ms, e0, e1), "batch autotune");
+                        if (first || ms < best) {
+                            best = ms;
+                            pick = split * 1000000 + form * 1000 + kch;
+                            first = false;
+                        }
                     }
-                }
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
-        b->f3form = pick / 1000;
+        b->f3split = pick >= 1000000;
+        b->f3form = pick / 1000 % 1000;
         b->f3kch = pick % 1000;
         return pick;
     }
@@ -3662,7 +3725,10 @@ int omx_batch_create(omx_ctx *const *ctxs, int n, omx_batch **out)
     for (auto *c : b->ctx) join_side(c);
     b->fp32 = ctxs[0]->fp32;
     ck(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "stream");
+    ck(cudaStreamCreateWithFlags(&b->aux, cudaStreamNonBlocking), "stream");
     ck(cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming), "event");
+    ck(cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming), "event");
+    ck(cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming), "event");
     *out = b.release();
     OMX_API_END(nullptr)
 }
@@ -3684,6 +3750,31 @@ int omx_batch_autotune(omx_batch *b, int reps, int *choice)
     b->key.clear();
     const int pick = b->fp32 ? batch_autotune_impl<float>(b, reps) : batch_autotune_impl<double>(b, reps);
     if (choice) *choice = pick;
+    OMX_API_END(nullptr)
+}
+
+int omx_batch_set_launch_shape(omx_batch *b, int shape)
+{
+    OMX_API_BEGIN
+    req(b && shape >= 1, "bad argument");
+    batch_decide(b);
+    if (b->fused == 1) {
+        const int form = shape / 1000 % 1000, rows = form % 100, ring = form / 100, kch = shape % 1000;
+        req(shape / 1000000 <= 1 && (rows == 8 || rows == 16) && (ring == 0 || (ring >= 2 && ring <= F3T_RING_MAX)) &&
+                kch >= 1 && kch <= F3T_KMAX,
+            "fused batched shape: split (0 | 1) * 1000000 + ring depth (0 or 2..16) * 100000 + (8 | 16) * 1000 + "
+            "planes (1..128)");
+        int dev = 0, optin = 0;
+        ck(cudaGetDevice(&dev), "device");
+        ck(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev), "device");
+        req(f3t_smem_bytes(form) <= optin, "fused batched shape: the ring does not fit in a block's shared memory");
+        b->f3split = shape >= 1000000;
+        b->f3form = form;
+        b->f3kch = kch;
+    } else {
+        req(shape == 4 || shape == 8 || shape == 16 || shape == 32, "batched two-pass shape: tile depth 4, 8, 16 or 32");
+        b->kch = shape;
+    }
     OMX_API_END(nullptr)
 }
 
@@ -3727,11 +3818,15 @@ int omx_batch_destroy(omx_batch *b)
 {
     if (!b) return OMX_OK;
     if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->aux) cudaStreamSynchronize(b->aux);
     b->drop_graphs();
     if (b->done) cudaEventDestroy(b->done);
-    cudaStream_t s = b->stream;
+    if (b->ev_fork) cudaEventDestroy(b->ev_fork);
+    if (b->ev_join) cudaEventDestroy(b->ev_join);
+    cudaStream_t s = b->stream, a = b->aux;
     delete b;
     if (s) cudaStreamDestroy(s);
+    if (a) cudaStreamDestroy(a);
     return OMX_OK;
 }
 

@@ -797,12 +797,14 @@ __global__ void __launch_bounds__(F3tShape<TY>::THREADS, f3t_min_blocks<TY>())
 // neighbouring cells that either of them wrote).  Both are bounded to 1536 threads' worth of
 // registers per SM (42 a thread): the extra resident warps hide more of their load latency
 // (512^3 dimer scene: 1.80 -> 1.71 ms per step with the H march not unrolled).
+// One general run's new H: the block's thread (tx, ty) takes column (i0 + tx, j0 + ty) when it
+// lies in the run's w x h tile and the grid.
 template <int TY>
-__global__ void __launch_bounds__(32 * TY, 1536 / (32 * TY)) k_f3g_h(Fused3Args A, GridArgs<float> G, const int4 *__restrict__ items)
+__device__ __forceinline__ void f3g_h_run(const Fused3Args &A, const GridArgs<float> &G, int4 it)
 {
-    const int4 it = items[blockIdx.x];
-    const Lay L = G.L;
+    const Lay &L = G.L;
     const int i = (it.x & 0xfffff) + (int)threadIdx.x, j = (it.y & 0xfffff) + (int)threadIdx.y;
+    const int k0 = it.z, k1 = it.w & 0xfffff;
     if ((int)threadIdx.x >= (it.x >> 20) || (int)threadIdx.y >= (it.y >> 20) || i > L.nx || j > L.ny) return;
     const bool perz = G.per[2] != 0;
     const float *__restrict__ Ex = A.in.f[0];
@@ -813,8 +815,8 @@ __global__ void __launch_bounds__(32 * TY, 1536 / (32 * TY)) k_f3g_h(Fused3Args 
     const int bxH = lhx >= 0 ? lhx + G.L2 * (j - 1) : -1, byH = lhy >= 0 ? (i - 1) + L.nx * lhy : -1;
     const int bz0 = (i - 1) + L.nx * (j - 1), sX = G.L2 * L.ny, sY = L.nx * G.L2, sZ = L.nx * L.ny;
     const int px_ = L.px, pz_ = (int)L.pz;
-    int idx = (int)L.off + i + px_ * j + pz_ * it.z;   // element offsets < 2^31 (checked by the host)
-    for (int k = it.z; k <= it.w; ++k, idx += pz_) {
+    int idx = (int)L.off + i + px_ * j + pz_ * k0;   // element offsets < 2^31 (checked by the host)
+    for (int k = k0; k <= k1; ++k, idx += pz_) {
         const int kp = (perz && k == L.nz) ? idx - (L.nz - 1) * pz_ : idx + pz_;   // E of plane k + 1
         const float ex_c = Ex[idx], ey_c = Ey[idx], ez_c = Ez[idx];
         const float ez_jp = Ez[idx + px_], ez_ip = Ez[idx + 1], ey_ip = Ey[idx + 1], ex_jp = Ex[idx + px_];
@@ -840,12 +842,15 @@ __global__ void __launch_bounds__(32 * TY, 1536 / (32 * TY)) k_f3g_h(Fused3Args 
     }
 }
 
+// One general run's new E; then, when G.step_inc is set, the last of the nblk blocks of this
+// grid's launch advances the grid's device-loop step counter (this launch ends the pass and holds
+// its only reads of the step's scalars).
 template <int TY>
-__global__ void __launch_bounds__(32 * TY, 1536 / (32 * TY)) k_f3g_e(Fused3Args A, GridArgs<float> G, const int4 *__restrict__ items)
+__device__ __forceinline__ void f3g_e_run(const Fused3Args &A, const GridArgs<float> &G, int4 it, unsigned nblk)
 {
-    const int4 it = items[blockIdx.x];
-    const Lay L = G.L;
+    const Lay &L = G.L;
     const int i = (it.x & 0xfffff) + (int)threadIdx.x, j = (it.y & 0xfffff) + (int)threadIdx.y;
+    const int k0 = it.z, k1 = it.w & 0xfffff;
     if ((int)threadIdx.x < (it.x >> 20) && (int)threadIdx.y < (it.y >> 20) && i <= L.nx && j <= L.ny) {
         const float *__restrict__ Hx = A.out.f[3];
         const float *__restrict__ Hy = A.out.f[4];
@@ -856,10 +861,10 @@ __global__ void __launch_bounds__(32 * TY, 1536 / (32 * TY)) k_f3g_e(Fused3Args 
         const int bz0 = (i - 1) + L.nx * (j - 1), sX = G.L2 * L.ny, sY = L.nx * G.L2, sZ = L.nx * L.ny;
         const bool bbc = i >= G.bb0[0] && i <= G.bb1[0] && j >= G.bb0[1] && j <= G.bb1[1];
         const int px_ = L.px, pz_ = (int)L.pz;
-        int idx = (int)L.off + i + px_ * j + pz_ * it.z;
+        int idx = (int)L.off + i + px_ * j + pz_ * k0;
         // new Hx, Hy of plane k - 1 (plane 0: the periodic image written by the pass, or the zero ghost)
         float hxm = Hx[idx - pz_], hym = Hy[idx - pz_];
-        for (int k = it.z; k <= it.w; ++k, idx += pz_) {
+        for (int k = k0; k <= k1; ++k, idx += pz_) {
             const float hx = Hx[idx], hy = Hy[idx], hz = Hz[idx];
             const float hz_im = Hz[idx - 1], hy_im = Hy[idx - 1], hz_jm = Hz[idx - px_], hx_jm = Hx[idx - px_];
             const float dez = G.den_e[2][k];
@@ -877,19 +882,49 @@ __global__ void __launch_bounds__(32 * TY, 1536 / (32 * TY)) k_f3g_e(Fused3Args 
             __stcs(A.out.f[2] + idx, ez);
         }
     }
-    // device loop: the last block to finish advances the step counter (this launch ends the pass
-    // and holds its only reads of the step's scalars)
     if (G.step_inc) {
         __syncthreads();
         if (threadIdx.x == 0 && threadIdx.y == 0) {
             __threadfence();
-            if (atomicAdd((unsigned *)G.step_done, 1u) == gridDim.x - 1) {
+            if (atomicAdd((unsigned *)G.step_done, 1u) == nblk - 1) {
                 *G.step_done = 0;
                 *G.step_inc += 1;
                 __threadfence();
             }
         }
     }
+}
+
+template <int TY>
+__global__ void __launch_bounds__(32 * TY, 1536 / (32 * TY)) k_f3g_h(Fused3Args A, GridArgs<float> G, const int4 *__restrict__ items)
+{
+    f3g_h_run<TY>(A, G, items[blockIdx.x]);
+}
+
+template <int TY>
+__global__ void __launch_bounds__(32 * TY, 1536 / (32 * TY)) k_f3g_e(Fused3Args A, GridArgs<float> G, const int4 *__restrict__ items)
+{
+    f3g_e_run<TY>(A, G, items[blockIdx.x], gridDim.x);
+}
+
+// Batched general runs of several grids: items[b].w carries the run's grid (k1 | g << 20); the
+// grid's arguments are read from its table entry.
+template <int TY>
+__global__ void __launch_bounds__(32 * TY, 1536 / (32 * TY)) k_f3g_h_batch(const F3tBatchGrid *__restrict__ grids,
+                                                                        const int4 *__restrict__ items)
+{
+    const int4 it = items[blockIdx.x];
+    const F3tBatchGrid &B = grids[it.w >> 20];
+    f3g_h_run<TY>(B.A, B.G, it);
+}
+
+template <int TY>
+__global__ void __launch_bounds__(32 * TY, 1536 / (32 * TY)) k_f3g_e_batch(const F3tBatchGrid *__restrict__ grids,
+                                                                        const int4 *__restrict__ items)
+{
+    const int4 it = items[blockIdx.x];
+    const F3tBatchGrid &B = grids[it.w >> 20];
+    f3g_e_run<TY>(B.A, B.G, it, (unsigned)B.n_gen);
 }
 
 // ---- batched: the fused pass of several grids in one launch ----------------------------------
@@ -919,6 +954,28 @@ __global__ void __launch_bounds__(F3tShape<TY>::THREADS, f3t_min_blocks<TY>())
     f3t_tile<TY, F3T_MIXED>(B.m, *sA, *sG, 1 + 32 * bx, 1 + TY * by, k0, k1, nd,
                             (unsigned)((long long)B.tx * B.ty * B.tz), err,
                             f3_smem);
+}
+
+// Batched lean runs of several grids (items[b] = {i0, j0, k0, k1 | g << 20}): the grid's
+// arguments are copied into shared memory; a grid that has general runs leaves its step counter
+// to their E launch.
+template <int TY>
+__global__ void __launch_bounds__(F3tShape<TY>::THREADS, f3t_min_blocks<TY>())
+    k_fused3_batch_lean(const F3tBatchGrid *__restrict__ grids, const int4 *__restrict__ items, int nd, int *err)
+{
+    extern __shared__ __align__(1024) unsigned char f3_smem[];
+    const int4 it = items[blockIdx.x];
+    const F3tBatchGrid &B = grids[it.w >> 20];
+    f3t_args_to_smem(B.G, B.A, f3_smem);
+    GridArgs<float> *sG = reinterpret_cast<GridArgs<float> *>(f3_smem);
+    if (B.n_gen > 0 && threadIdx.x == 0) {
+        sG->step_inc = nullptr;
+        sG->step_done = nullptr;
+    }
+    __syncthreads();
+    const Fused3Args *sA = reinterpret_cast<const Fused3Args *>(f3_smem + F3T_ARGB);
+    f3t_tile<TY, F3T_LEAN_ONLY>(B.m, *sA, *sG, it.x, it.y, it.z, it.w & 0xfffff, nd, (unsigned)B.n_lean, err,
+                                f3_smem);
 }
 
 }  // namespace omx

@@ -202,6 +202,7 @@ struct F3tBatchGrid {
     Fused3Args A;
     long long item0;         // first block of this grid in the launch
     int tx, ty, tz, kch;     // tiles along x (32 cells), y (tile rows), z (kch planes)
+    int n_gen, n_lean;       // the grid's general and lean runs in the run lists of a split launch
 };
 constexpr int F3T_KMAX = 128;   // planes per block of the fused 3D pass at most
 constexpr int F3T_GEN_KCH = 8;  // planes per run of the fused 3D pass's general runs at most
@@ -224,6 +225,13 @@ cudaError_t launch_fused3t_lean(const F3tMaps &M, const Fused3Args &A, const Gri
 // advances the device-loop step counter when G.step_inc is set).
 cudaError_t launch_fused3t_general(const Fused3Args &A, const GridArgs<float> &G, int form, const int4 *items, int n,
                                    bool e_half, void *stream);
+// The batched fused pass split by plane form: every grid's general runs through the two plain
+// kernels (new H, then new E after the lean runs) and every grid's lean runs in one launch; run
+// lists as the single-grid ones with the grid's table index in k1's high bits (k1 | g << 20).
+// parts: 1 the general runs' new H, 2 the lean runs, 4 the general runs' new E (which reads the
+// new H of both), launched in that order; 1 and 2 may run on two streams at once.
+cudaError_t launch_fused3t_batch_split(const F3tBatchGrid *grids, const int4 *gen, int ngen, const int4 *lean, int nlean,
+                                       int form, int parts, int *err, void *stream);
 // the batched pass over n grids (device table, largest grid first) with `blocks` blocks in all
 cudaError_t launch_fused3t_batch(const F3tBatchGrid *grids, int n, long long blocks, int form, int *err,
                                  void *stream);

@@ -256,6 +256,41 @@ static cudaError_t launch_f3t_batch(const F3tBatchGrid *grids, int n, long long 
     return cudaGetLastError();
 }
 
+cudaError_t launch_fused3t_batch_split(const F3tBatchGrid *grids, const int4 *gen, int ngen, const int4 *lean, int nlean,
+                                       int form, int parts, int *err, void *sv)
+{
+    const cudaStream_t s = (cudaStream_t)sv;
+    const int ty = f3t_rows(form), nd = f3t_ring(form);
+    const dim3 b(32, (unsigned)ty);
+    if (ngen > 0 && (parts & 1)) {
+        if (ty == 16) k_f3g_h_batch<16><<<(unsigned)ngen, b, 0, s>>>(grids, gen);
+        else k_f3g_h_batch<8><<<(unsigned)ngen, b, 0, s>>>(grids, gen);
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    if (nlean > 0 && (parts & 2)) {
+        static int have16[FZ_MAX_DEV] = {}, have8[FZ_MAX_DEV] = {};
+        if (ty == 16) {
+            const int bytes = F3tShape<16>::smem(nd);
+            const cudaError_t e = f3t_smem_attr(k_fused3_batch_lean<16>, have16, bytes);
+            if (e != cudaSuccess) return e;
+            k_fused3_batch_lean<16><<<(unsigned)nlean, F3tShape<16>::THREADS, bytes, s>>>(grids, lean, nd, err);
+        } else {
+            const int bytes = F3tShape<8>::smem(nd);
+            const cudaError_t e = f3t_smem_attr(k_fused3_batch_lean<8>, have8, bytes);
+            if (e != cudaSuccess) return e;
+            k_fused3_batch_lean<8><<<(unsigned)nlean, F3tShape<8>::THREADS, bytes, s>>>(grids, lean, nd, err);
+        }
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    if (ngen > 0 && (parts & 4)) {
+        if (ty == 16) k_f3g_e_batch<16><<<(unsigned)ngen, b, 0, s>>>(grids, gen);
+        else k_f3g_e_batch<8><<<(unsigned)ngen, b, 0, s>>>(grids, gen);
+    }
+    return cudaGetLastError();
+}
+
 cudaError_t launch_fused3t_batch(const F3tBatchGrid *grids, int n, long long blocks, int form, int *err, void *s)
 {
     const int nd = f3t_ring(form);

@@ -415,10 +415,15 @@ class Batch:
         A.check(lib().omx_batch_create(arr, len(self.grids), C.byref(self._b)))
 
     def autotune(self, reps=10):
-        """Tile depth of the batched passes, timed on the zero initial fields; returns it."""
+        """Launch shape of the batched passes, timed on the zero initial fields; returns it
+        (encoded as omx_batch_autotune describes)."""
         choice = C.c_int()
         A.check(lib().omx_batch_autotune(self._b, int(reps), C.byref(choice)))
         return choice.value
+
+    def set_launch_shape(self, shape):
+        """Launch shape of the batched passes, encoded as autotune returns it."""
+        A.check(lib().omx_batch_set_launch_shape(self._b, int(shape)))
 
     def drain_async(self):
         """Enqueue the copy of the recorded samples into a pinned slot; returns a ticket."""

@@ -118,6 +118,7 @@ SIGNATURES = {
     "omx_autotune": (_I, [_VP, _I, _PI]),
     "omx_batch_create": (_I, [C.POINTER(_VP), _I, C.POINTER(_VP)]),
     "omx_batch_autotune": (_I, [_VP, _I, _PI]),
+    "omx_batch_set_launch_shape": (_I, [_VP, _I]),
     "omx_batch_run": (_I, [_VP, _I, _I, _I, _I, _I]),
     "omx_batch_run_prepare": (_I, [_VP, _I, _I, _I, _I]),
     "omx_batch_launch_count": (C.c_longlong, [_VP]),

@@ -1,6 +1,6 @@
 """Batched multi-grid runs (omx_batch_*): several 3D instances of the inverse-design sweep advance
-together -- FP32 grids that step with one fused pass in one k_fused3_batch launch per step, the
-others through one persistent launch per half-step pass; every grid must equal its own solo run
+together -- FP32 grids that step with one fused pass in one k_fused3_batch launch per step (or the
+pass split by plane form), the others through one persistent launch per half-step pass; every grid must equal its own solo run
 bit for bit (same arithmetic, same per-grid order), with and without the graph and after the
 batch autotuner.  Calls go through the C-ABI."""
 import numpy as np
@@ -46,8 +46,9 @@ def test_batch_equals_solo_runs(precision, form, use_graph, autotune):
         fused = precision == "fp32" and form == omx.STEP_DEFAULT
         choice = b.autotune(reps=2)
         if fused:
-            # (ring depth x 100 + tile rows) x 1000 + planes per block
-            assert choice // 1000 % 100 in (8, 16) and choice // 100000 in (0, 6, 8)
+            # split x 1000000 + (ring depth x 100 + tile rows) x 1000 + planes per block
+            form = choice // 1000 % 1000
+            assert choice // 1000000 in (0, 1) and form % 100 in (8, 16) and form // 100 in (0, 6, 8)
             assert choice % 1000 in (16, 32, 64, 128)
         else:
             assert choice in (4, 8, 16, 32)
@@ -61,6 +62,39 @@ def test_batch_equals_solo_runs(precision, form, use_graph, autotune):
         assert np.array_equal(tr, tr_solo)
         for a, s in zip(fields(g), f_solo):
             assert np.array_equal(a, s)
+    b.kill()
+    for _, g in batch:
+        g.kill()
+
+
+@pytest.mark.parametrize("shape", [8064, 1016032, 1608016])
+def test_fused_batch_shapes_equal_solo_runs(shape):
+    """FP32 fused batch in a set launch shape: one k_fused3_batch launch (8064), or the pass split
+    by plane form (1016032: tile 32 x 16, 32 planes per lean run; 1608016: ring of 6, tile 32 x 8,
+    16 planes), where the 96^3 grid has lean runs clear of its CPML slabs and the small grids are
+    general runs only; every grid equals its solo run bit for bit."""
+    sizes, steps = (96, 36, 29), 50
+    solo, batch = [], []
+    for k, n in enumerate(sizes):
+        d, g = build(n, 500 + k, "fp32")
+        g.run(1, steps, d["n_skip"], d["t_det_print"], use_graph=True)
+        solo.append((fields(g), g.drain_detectors()[1]))
+        g.kill()
+        batch.append(build(n, 500 + k, "fp32"))
+    b = omx.Batch([g for _, g in batch])
+    for bad in (2008064, 8, 16000, 8200):    # split flag 2, a two-pass depth, 0 planes, 200 planes
+        with pytest.raises(omx.OMXError):
+            b.set_launch_shape(bad)
+    b.set_launch_shape(shape)
+    d0 = batch[0][0]
+    b.run(1, 20, d0["n_skip"], d0["t_det_print"], use_graph=False)
+    b.run(21, steps - 20, d0["n_skip"], d0["t_det_print"], use_graph=True)
+    for (d, g), (f_solo, tr_solo) in zip(batch, solo):
+        tr = g.drain_detectors()[1]
+        assert tr.shape == tr_solo.shape and np.array_equal(tr, tr_solo)
+        assert max(np.max(np.abs(f)) for f in f_solo) > 0     # the source has driven every grid
+        for a, s_ in zip(fields(g), f_solo):
+            assert np.array_equal(a, s_)
     b.kill()
     for _, g in batch:
         g.kill()
