@@ -436,7 +436,8 @@ def measure(args, dist, config, grid, K, W, err_steps, cpu_seconds):
     if per["H"]["launches"] == 0:      # one fused pass per step
         per["fused_HE"] = per.pop("E")
         per.pop("H")
-        dom, kernel_name = "fused_HE", ("k_fused3_tma (3D H+E step in one pass, planes staged by TMA)"
+        dom, kernel_name = "fused_HE", ("k_fused3_tma<TY, LEAN_ONLY> + k_f3g_h / k_f3g_e (3D H+E step in one "
+                                        "pass split by plane form, lean planes staged by TMA)"
                                         if dims == 3 else
                                         "k_fused_tmz_ws (H+E step in one pass; form from omx_autotune)")
     alg_bytes = gpu.algorithmic_bytes(kc_dom)
@@ -529,8 +530,8 @@ def measure(args, dist, config, grid, K, W, err_steps, cpu_seconds):
     if shape is None:
         shape_desc = "library default"
     elif dims == 3 and shape >= 1000:
-        shape_desc = "fused 3D tile 32 x %d, %d planes per block, ring of %d planes (omx_autotune)" % (
-            shape // 1000 % 100, shape % 1000, shape // 100000 or 4)
+        shape_desc = "fused 3D pass split by plane form, tile 32 x %d, %d planes per block, ring of %d planes " \
+                     "(omx_autotune)" % (shape // 1000 % 100, shape % 1000, shape // 100000 or 4)
     elif dims == 2:
         shape_desc = "fused-kernel form %d (omx_autotune)" % shape
     elif dims == 3:
