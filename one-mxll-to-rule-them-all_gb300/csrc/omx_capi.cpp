@@ -1220,9 +1220,21 @@ void f3t_runs(const omx_ctx *c, int ty, int kch, std::vector<int4> &gen, std::ve
     const auto rx = rest(ox, nx, 32), ry = rest(oy, ny, ty);
     const bool box = c->bb1[0] >= c->bb0[0] && c->bb1[1] >= c->bb0[1] && c->bb1[2] >= c->bb0[2];
     const int gk = std::min(kch, F3T_GEN_KCH);
+    // planes of the media box in a grid with dispersive cells: general runs of at most
+    // F3T_MEDIA_KCH planes there (a dispersive cell's ADE waits on its pole state plane by plane,
+    // so shorter marches put more threads on the few columns that hold them)
+    const bool disp = box && c->ade_n > 0;
+    auto media_k = [&](int k) { return disp && k >= c->bb0[2] && k <= c->bb1[2]; };
+    const int mkch = std::min(gk, F3T_MEDIA_KCH);
     auto general_column = [&](int i0, int w, int j0, int h) {
-        for (int k = 1; k <= nz; k += gk)
-            gen.push_back(make_int4(i0 | (w << 20), j0 | (h << 20), k, std::min(nz, k + gk - 1)));
+        const bool mxy = disp && c->bb0[0] <= i0 + w - 1 && c->bb1[0] >= i0 && c->bb0[1] <= j0 + h - 1 && c->bb1[1] >= j0;
+        for (int k = 1; k <= nz;) {
+            const bool m = mxy && media_k(k);
+            int e = k;
+            while (e < nz && e - k + 1 < (m ? mkch : gk) && (mxy && media_k(e + 1)) == m) ++e;
+            gen.push_back(make_int4(i0 | (w << 20), j0 | (h << 20), k, e));
+            k = e + 1;
+        }
     };
     std::vector<char> lk(nz + 1);
     for (int j0 : oy)
@@ -1238,9 +1250,10 @@ void f3t_runs(const omx_ctx *c, int ty, int kch, std::vector<int4> &gen, std::ve
             for (int k = 1; k <= nz;) {
                 // general runs in short pieces: their plain kernels march a thread per column,
                 // so more pieces are more threads in flight
-                const int cap = lk[k] ? kch : std::min(kch, F3T_GEN_KCH);
+                const bool m = !lk[k] && mb && media_k(k);
+                const int cap = lk[k] ? kch : (m ? mkch : gk);
                 int e = k;
-                while (e < nz && lk[e + 1] == lk[k] && e - k + 1 < cap) ++e;
+                while (e < nz && lk[e + 1] == lk[k] && e - k + 1 < cap && (!lk[k] && mb && media_k(e + 1)) == m) ++e;
                 if (lk[k]) lean.push_back(make_int4(i0, j0, k, e));
                 else gen.push_back(make_int4(i0 | (w << 20), j0 | (h << 20), k, e));
                 k = e + 1;

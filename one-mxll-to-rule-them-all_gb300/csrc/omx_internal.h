@@ -206,6 +206,7 @@ struct F3tBatchGrid {
 };
 constexpr int F3T_KMAX = 128;   // planes per block of the fused 3D pass at most
 constexpr int F3T_GEN_KCH = 8;  // planes per run of the fused 3D pass's general runs at most
+constexpr int F3T_MEDIA_KCH = 1;   // the same in the media box's planes when it holds dispersive cells
 // a fused 3D form is ring depth x 100 + tile rows (8 or 16); depth 0 and form <= 0 are defaults
 constexpr int F3T_RING_DEFAULT = 4;   // plane slots in a block's ring
 constexpr int F3T_RING_MAX = 16;

@@ -105,17 +105,35 @@ def test_noalloc_emitter_step_matches_qgroup_step(scene):
     dJ_d = torch.zeros_like(J_d)
     stream = torch.cuda.current_stream(dev).cuda_stream
 
-    for call, tt in enumerate((60, 61)):
+    def call_noalloc(s):
+        return L.omx_emitter_step_noalloc(model, n, E_d.data_ptr(), par_d.data_ptr(), rho_d.data_ptr(),
+                                          dip_d.data_ptr(), npnt, win_d.data_ptr(), wk_d.data_ptr(), J_d.data_ptr(),
+                                          Jo_d.data_ptr(), dJ_d.data_ptr(), c0, c1, dt, C.c_void_p(s))
+
+    # steps 60, 61: direct calls; step 62: the call captured in a CUDA graph (it allocates
+    # nothing, so it captures) with its input E written after the capture, then one replay
+    for call, tt in enumerate((60, 61, 62)):
         _advance(g, deck, group, state, tt)          # the context API's step (gather, RK4, scatter)
         ref = group.read()
-        E_d.copy_(torch.from_numpy(ref["E"]))
         J_before = J_d.cpu().numpy().copy()
-        rc = L.omx_emitter_step_noalloc(model, n, E_d.data_ptr(), par_d.data_ptr(), rho_d.data_ptr(),
-                                         dip_d.data_ptr(), npnt, win_d.data_ptr(), wk_d.data_ptr(), J_d.data_ptr(),
-                                         Jo_d.data_ptr(), dJ_d.data_ptr(), c0, c1, dt, C.c_void_p(stream))
-        assert rc == 0, L.omx_last_error(None)
+        if tt < 62:
+            E_d.copy_(torch.from_numpy(ref["E"]))
+            rc = call_noalloc(stream)
+            assert rc == 0, L.omx_last_error(None)
+        else:
+            side = torch.cuda.Stream(dev)
+            side.wait_stream(torch.cuda.current_stream(dev))
+            graph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(graph, stream=side):
+                rc = call_noalloc(side.cuda_stream)
+            assert rc == 0, L.omx_last_error(None)
+            torch.cuda.synchronize()
+            assert _rel(rho_d.cpu().numpy(), prev_rho) == 0.0      # capturing ran nothing
+            E_d.copy_(torch.from_numpy(ref["E"]))
+            graph.replay()
         torch.cuda.synchronize()
         rho, dip = rho_d.cpu().numpy(), dip_d.cpu().numpy()
+        prev_rho = rho.copy()
         J, Jo, dJ = J_d.cpu().numpy(), Jo_d.cpu().numpy(), dJ_d.cpu().numpy()
         assert _rel(rho, ref["rho"]) <= TOL and _rel(dip, ref["dipole"]) <= TOL, call
         for c in range(c0, c1 + 1):
