@@ -1125,6 +1125,7 @@ template <class R> void do_group(omx_ctx *c, GroupRec &g, StepParam move)
     A.dt = g.d.dt;
     A.h2 = 0.5 * g.d.dt;
     A.h6 = g.d.dt / 6.0;
+    A.inv_dt = c->fp32 ? 1.0 / g.d.dt : 0.0;
     A.only_if = nullptr;
     if (g.cl) {
         // network step, spot-check subset, check / fallback; the plain propagator below runs only
@@ -1147,6 +1148,7 @@ template <class R> void do_group(omx_ctx *c, GroupRec &g, StepParam move)
     S.wk = g.wk.p;
     S.dPdt = g.dPdt.p;
     S.dt = g.d.dt;
+    S.inv_dt = c->fp32 ? 1.0 / g.d.dt : 0.0;
     launch_scatter(jstate(c), S, move, c->stream);
     c->launches += 2;
 }
@@ -1848,6 +1850,8 @@ void apply_shape(omx_ctx *c, int v)
     }
 }
 
+constexpr int AUTOTUNE_STEPS = 4;   // steps timed back to back per candidate and round
+
 // Time each candidate launch shape on the device and keep the fastest.  Runs on fields that are
 // still all zero: every kernel maps zero fields, zero psi and zero ADE state to zero, so the
 // candidates leave no trace in the simulation state.
@@ -1889,9 +1893,10 @@ template <class R> int autotune_impl(omx_ctx *c, int reps)
             do_E<R>(c, imm(0.0), imm(0.0));
         }
     };
-    // first use of every form sets its kernel attributes; then `reps` rounds, each timing one
-    // step of every candidate in turn (interleaved, so that clock or thermal drift affects all
-    // candidates alike); a candidate's time is its fastest round
+    // first use of every form sets its kernel attributes; then `reps` rounds, each timing
+    // AUTOTUNE_STEPS steps of every candidate in turn (interleaved, so that clock or thermal drift
+    // affects all candidates alike; several steps back to back, so that the host's launch gaps
+    // hide behind the device's work as in a run); a candidate's time is its fastest round
     for (int v : cand) {
         select(v);
         once();
@@ -1901,7 +1906,7 @@ template <class R> int autotune_impl(omx_ctx *c, int reps)
         for (size_t k = 0; k < cand.size(); ++k) {
             select(cand[k]);
             ck(cudaEventRecord(c->t0, c->stream), "autotune");
-            once();
+            for (int s = 0; s < AUTOTUNE_STEPS; ++s) once();
             ck(cudaEventRecord(c->t1, c->stream), "autotune");
             ck(cudaEventSynchronize(c->t1), "autotune");
             float ms = 0.f;

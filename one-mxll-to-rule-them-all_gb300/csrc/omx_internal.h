@@ -132,6 +132,9 @@ struct EmitArgs {
     const double *rates;      // (1/T1, 1/T2) per emitter, formed at group creation
     double *rho, *E, *dipole, *dPdt;
     double dt, h2, h6;        // dt, dt/2, dt/6
+    // 0: dPt_dt = (new - old) / dt, the reference's division (FP64 fields); else (new - old) * inv_dt,
+    // 1/dt rounded once (FP32 fields: within an ulp of the quotient, without an FP64 division)
+    double inv_dt;
     const int *only_if;       // optional: run only while *only_if != 0 (the closure's fallback flag)
 };
 
@@ -141,6 +144,7 @@ struct ScatArgs {
     const double *wk;
     const double *dPdt;
     double dt;
+    double inv_dt;            // as EmitArgs::inv_dt, for dJ = (J - J_old) / dt
 };
 
 struct DetArgs {

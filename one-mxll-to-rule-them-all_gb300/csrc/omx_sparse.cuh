@@ -110,14 +110,15 @@ __global__ void k_emit(FieldPtrs<R> F, Lay L, EmitArgs A, StepParam move_p)
         const double old = A.dipole[3 * n + a];
         const double nw = d * u[a];
         A.dipole[3 * n + a] = nw;
-        A.dPdt[3 * n + a] = (nw - old) / A.dt;
+        A.dPdt[3 * n + a] = A.inv_dt != 0.0 ? (nw - old) * A.inv_dt : (nw - old) / A.dt;
         A.E[3 * n + a] = E[a];
     }
 }
 
 // send_J_to_E_ranks (interactions_mod.f90:1046-1220): J_old = J; J(point) = wk*dPt_dt of the
-// last emitter writing the point (assignment); dJ = (J - J_old)/dt.  Points this group does
-// not write keep J, so their dJ becomes zero, as with the reference's full-grid passes.
+// last emitter writing the point (assignment); dJ = (J - J_old)/dt (times 1/dt with FP32 fields,
+// as dPt_dt in k_emit).  Points this group does not write keep J, so their dJ becomes zero, as
+// with the reference's full-grid passes.
 __global__ void k_scatter(JState J, ScatArgs S, StepParam move_p)
 {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -129,7 +130,7 @@ __global__ void k_scatter(JState J, ScatArgs S, StepParam move_p)
         const double jn = (w >= 0) ? S.wk[p] * S.dPdt[3 * w + c] : jo;
         J.Jo[c][p] = jo;
         J.J[c][p] = jn;
-        J.dJ[c][p] = (jn - jo) / S.dt;
+        J.dJ[c][p] = S.inv_dt != 0.0 ? (jn - jo) * S.inv_dt : (jn - jo) / S.dt;
     }
 }
 
