@@ -621,23 +621,33 @@ def batch_shape_text(shape):
         return "the two half-step passes of every grid (k_batch3)", "tile depth %d" % shape
     form = shape // 1000 % 1000
     tile = "tile 32 x %d, %d planes per block, ring of %d planes" % (form % 100, shape % 1000, form // 100 or 4)
-    if shape >= 1000000:
-        return ("the fused pass of every grid split by plane form: the general runs' new H (k_f3g_h_batch) "
-                "on a second stream beside one launch of every grid's lean runs (k_fused3_batch_lean), "
-                "then the general runs' new E (k_f3g_e_batch)"), tile
+    s = shape // 1000000
+    if s > 0:
+        return ("the fused pass of the %d largest grids split by plane form (their general runs' new H, "
+                "k_f3g_h_batch, and one k_fused3_batch launch over the other grids' tiles on a second stream "
+                "beside one launch of their lean runs, k_fused3_batch_lean, then their general runs' new E, "
+                "k_f3g_e_batch)" % s), tile
     return "one k_fused3_batch launch per step over every grid's tiles (largest grid first)", tile
 
 
 def gpu_arm_cfg5(args, dist):
-    import numpy as np
-
     import omx
 
     if dist.world > 1:
         omx.select_device(dist.local_rank % max(1, omx.device_count()))
+    line = measure_cfg5(args, dist, args.steps, max(3, args.warmup), args.cpu_seconds)
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def measure_cfg5(args, dist, K, W, cpu_seconds):
+    """The batched sweep against the same grids one at a time; the bench line (rank 0) or None."""
+    import numpy as np
+
+    import omx
+
     dks, sides = cfg5_decks(args.instances, args.side_min, args.side_max)
     cells = sum(cells_of(d) for d in dks)
-    K, W = args.steps, max(3, args.warmup)
     tdp = 1
     # ---- batched: one persistent launch per pass over all grids, the step in a CUDA graph
     grids = [build_gpu(d, "fp32")[0] for d in dks]
@@ -663,10 +673,13 @@ def gpu_arm_cfg5(args, dist):
     for g in grids:
         g.kill()
     # ---- the same grids one at a time (each its own omx_run, CUDA graphs per grid, the graphs
-    # captured before the clock) with the batch's arithmetic (traces compared bit for bit)
+    # captured before the clock) with the batch's arithmetic (traces compared bit for bit), each
+    # grid in the fused shape its own autotuner picks (the fused pass only: its bits are the batch's)
     t_solo, same = 0.0, True
     for d, tb in zip(dks, traces_b):
         g = build_gpu(d, "fp32")[0]
+        g.set_step_form(omx.STEP_SINGLE_PASS)
+        g.autotune(reps=3)
         g.run(1, W, 1, tdp, use_graph=True)
         g.prepare_run(1 + W, K, 1, tdp)
         g.synchronize()
@@ -687,7 +700,7 @@ def gpu_arm_cfg5(args, dist):
         small = sorted(range(len(dks)), key=lambda k: sides[k])[:2]
         done, el_total, cores, cc = 0, 0.0, 1, 0
         for k in small:
-            n, el, cores = cpu_run(dks[k], seconds=args.cpu_seconds / 2)
+            n, el, cores = cpu_run(dks[k], seconds=cpu_seconds / 2)
             done += n * cells_of(dks[k])
             el_total += el
         cpu = {"value": done / el_total / 1e9, "unit": "Gcell-updates/s", "cores": cores, "kind": "port",
@@ -709,7 +722,8 @@ def gpu_arm_cfg5(args, dist):
                                "omx_batch_autotune: %s" % batch_shape_text(shape),
                        "timing": "wall clock around omx_batch_run + omx_batch_synchronize"},
             "one_at_a_time": {"value": solo_value, "unit": "Gcell-updates/s",
-                              "how": "the same grids, each its own omx_run (CUDA graph), run one after another",
+                              "how": "the same grids, each its own omx_run (CUDA graph) in the fused shape "
+                                     "its own omx_autotune picks, run one after another",
                               "batch_speedup": value / solo_value,
                               "detector_traces_bit_identical": same,
                               "arithmetic": "one fused pass per grid and step, as the batch"},
@@ -723,7 +737,8 @@ def gpu_arm_cfg5(args, dist):
             "gpu_launches": launches,
             "clocks": clk,
         }
-        print(json.dumps(line), flush=True)
+        return line
+    return None
 
 
 # ---------------------------------------------------------------------------------- cfg4: closure

@@ -334,8 +334,9 @@ int omx_set_launch_shape(omx_ctx *ctx, int shape);
  * A batch groups n configured 3D contexts of one precision on the current device (for example
  * the instances of a parameter sweep).  omx_batch_run advances all of them together.  When every
  * member steps with the fused FP32 3D pass, each step runs that pass for every grid at once (one
- * launch over all grids' tiles, or the pass split by plane form: the general runs' new H on a
- * second stream beside one launch of every grid's lean runs, then the general runs' new E), one
+ * launch over all grids' tiles, or for the largest grids the pass split by plane form: their
+ * general runs' new H on a second stream beside one launch of their lean runs, then their general
+ * runs' new E, the other grids' one launch on that second stream too), one
  * launch per round of the other sources, the per-grid emitter work and one launch for the
  * detectors of every grid.  Otherwise each step runs ONE persistent launch for the H pass of
  * every grid (its blocks walk a list of all grids' tiles), one launch per round of radial sources
@@ -349,8 +350,9 @@ int omx_batch_create(omx_ctx *const *ctxs, int n, omx_batch **out);
 /* The launch shape of the batched passes, each candidate timed `reps` times on the initial zero
  * fields; same preconditions as omx_autotune.  *choice (may be NULL) is the tile depth (z planes
  * per tile: 4, 8, 16 or 32) of the two half-step passes, or for the fused pass
- * split x 1000000 + (ring depth x 100 + tile rows) x 1000 + planes per block, split 1 for the pass
- * split by plane form and ring depth 0 for the default of 4 planes. */
+ * s x 1000000 + (ring depth x 100 + tile rows) x 1000 + planes per block: the s largest grids step
+ * with the pass split by plane form, the others in one launch over their tiles (s = 0: every grid
+ * in that launch); ring depth 0 for the default of 4 planes. */
 int omx_batch_autotune(omx_batch *batch, int reps, int *choice);
 /* No counterpart in the reference: sets the launch shape of the batched passes, encoded as
  * omx_batch_autotune's choice (a fused shape when every member steps with the fused FP32 pass,

@@ -3141,9 +3141,11 @@ template <class R> struct BatchTables {
     const BatchDet<R> *dets = nullptr;
     int ndet = 0;
     long long det_pts = 0;
-    // fused path: the grids of the batched pass (largest first) and its blocks; the runs of the
-    // split pass (general runs, then lean runs, each with its grid's table index)
+    // fused path: the grids of the batched pass (largest first); the first nsplit of them step with
+    // the split pass (its runs: general runs, then lean runs, each with its grid's table index),
+    // the others in one k_fused3_batch launch of f3_blocks blocks over their tiles
     const F3tBatchGrid *f3 = nullptr;
+    int nsplit = 0, nmixed = 0;
     long long f3_blocks = 0;
     const int4 *f3gen = nullptr, *f3lean = nullptr;
     int nf3gen = 0, nf3lean = 0;
@@ -3165,11 +3167,12 @@ struct omx_batch {
     // launch per step; 0: the two half-step passes (k_batch3); -1: not decided yet
     int fused = -1;
     int f3form = 8, f3kch = 64;   // tile rows and planes per block of the fused batched pass
-    // the fused batched pass split by plane form (general runs' H on `aux` beside the lean runs,
-    // then their E) instead of one k_fused3_batch launch
-    bool f3split = false;
+    // the f3nsplit largest grids step with the fused pass split by plane form (their general runs'
+    // H on `aux` beside their lean runs, then their E), the others in one k_fused3_batch launch
+    // (on `aux` after that H)
+    int f3nsplit = 0;
     cudaStream_t aux = nullptr;
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_mixed = nullptr;
     // tables and captured step graphs, kept while the key (each member's configuration epoch,
     // buffer set, step table and the launch shapes) is unchanged
     std::vector<long long> key;
@@ -3332,6 +3335,7 @@ BatchTables<R> batch_tables(omx_batch *b, const std::vector<RunPlan> *plans, int
                 return (long long)x->n[0] * x->n[1] * x->n[2] > (long long)y->n[0] * y->n[1] * y->n[2];
             });
             const int TY = f3t_rows(b->f3form);
+            const int ns = std::min(std::max(b->f3nsplit, 0), n);
             long long item = 0;
             for (int i : order) {
                 omx_ctx *c = b->ctx[i];
@@ -3361,18 +3365,22 @@ BatchTables<R> batch_tables(omx_batch *b, const std::vector<RunPlan> *plans, int
                 e.tx = (c->L.nx + 31) / 32;
                 e.ty = (c->L.ny + TY - 1) / TY;
                 e.tz = (c->L.nz + e.kch - 1) / e.kch;
-                e.item0 = item;
-                item += (long long)e.tx * e.ty * e.tz;
-                // the grid's runs for the split pass, tagged with its place in the table
-                std::vector<int4> g0, l0;
-                f3t_runs(c, TY, e.kch, g0, l0);
                 const int gi = (int)f3g.size();
-                for (int4 &r : g0) r.w |= gi << 20;
-                for (int4 &r : l0) r.w |= gi << 20;
-                e.n_gen = (int)g0.size();
-                e.n_lean = (int)l0.size();
-                runs_gen.insert(runs_gen.end(), g0.begin(), g0.end());
-                runs_lean.insert(runs_lean.end(), l0.begin(), l0.end());
+                if (gi >= ns) {
+                    // one launch over the tiles of the grids from ns on
+                    e.item0 = item;
+                    item += (long long)e.tx * e.ty * e.tz;
+                } else {
+                    // the grid's runs for the split pass, tagged with its place in the table
+                    std::vector<int4> g0, l0;
+                    f3t_runs(c, TY, e.kch, g0, l0);
+                    for (int4 &r : g0) r.w |= gi << 20;
+                    for (int4 &r : l0) r.w |= gi << 20;
+                    e.n_gen = (int)g0.size();
+                    e.n_lean = (int)l0.size();
+                    runs_gen.insert(runs_gen.end(), g0.begin(), g0.end());
+                    runs_lean.insert(runs_lean.end(), l0.begin(), l0.end());
+                }
                 f3g.push_back(e);
             }
             b->df3[q].alloc(sizeof(F3tBatchGrid) * f3g.size(), false);
@@ -3380,6 +3388,8 @@ BatchTables<R> batch_tables(omx_batch *b, const std::vector<RunPlan> *plans, int
                                b->stream),
                "batch");
             T.f3 = reinterpret_cast<const F3tBatchGrid *>(b->df3[q].p);
+            T.nsplit = ns;
+            T.nmixed = n - ns;
             T.f3_blocks = item;
             std::vector<int4> runs(runs_gen);
             runs.insert(runs.end(), runs_lean.begin(), runs_lean.end());
@@ -3422,33 +3432,51 @@ struct BatchStreams {
     }
 };
 
-// The fused pass of every member: one k_fused3_batch launch, or the split pass (the general runs'
-// new H on the auxiliary stream while the lean runs go, then the general runs' new E).  Returns
-// the kernels launched.
-template <class R> long long batch_fused_pass(omx_batch *b, const BatchTables<R> &T, int form, bool split)
+// The fused pass of every member: the split pass for the T.nsplit largest grids (their general
+// runs' new H on the auxiliary stream while their lean runs go on the batch's stream, then their
+// general runs' new E) and one k_fused3_batch launch for the others (on the auxiliary stream after
+// that H, so beside the lean runs too); every grid's pass writes only that grid.  Returns the
+// kernels launched.
+template <class R> long long batch_fused_pass(omx_batch *b, const BatchTables<R> &T, int form)
 {
-    const int n = (int)b->ctx.size();
     int *err = b->ctx[0]->d_err.p;
-    if (!split) {
-        ck(launch_fused3t_batch(T.f3, n, T.f3_blocks, form, err, b->stream), "batched fused pass");
+    if (T.nsplit == 0) {
+        ck(launch_fused3t_batch(T.f3, T.nmixed, T.f3_blocks, form, err, b->stream), "batched fused pass");
         return 1;
     }
-    if (T.nf3gen == 0) {
-        ck(launch_fused3t_batch_split(T.f3, T.f3gen, 0, T.f3lean, T.nf3lean, form, 2, err, b->stream),
-           "batched fused pass");
-        return T.nf3lean > 0 ? 1 : 0;
+    long long k = 0;
+    const bool side = T.nf3gen > 0 || T.nmixed > 0;
+    if (side) {
+        ck(cudaEventRecord(b->ev_fork, b->stream), "event");
+        ck(cudaStreamWaitEvent(b->aux, b->ev_fork, 0), "event");
+        if (T.nf3gen > 0) {
+            ck(launch_fused3t_batch_split(T.f3, T.f3gen, T.nf3gen, T.f3lean, T.nf3lean, form, 1, err, b->aux),
+               "batched fused pass (general runs, H)");
+            ++k;
+        }
+        ck(cudaEventRecord(b->ev_join, b->aux), "event");
+        if (T.nmixed > 0) {
+            ck(launch_fused3t_batch(T.f3 + T.nsplit, T.nmixed, T.f3_blocks, form, err, b->aux),
+               "batched fused pass (one launch)");
+            ++k;
+        }
+        ck(cudaEventRecord(b->ev_mixed, b->aux), "event");
     }
-    ck(cudaEventRecord(b->ev_fork, b->stream), "event");
-    ck(cudaStreamWaitEvent(b->aux, b->ev_fork, 0), "event");
-    ck(launch_fused3t_batch_split(T.f3, T.f3gen, T.nf3gen, T.f3lean, T.nf3lean, form, 1, err, b->aux),
-       "batched fused pass (general runs, H)");
-    ck(cudaEventRecord(b->ev_join, b->aux), "event");
-    ck(launch_fused3t_batch_split(T.f3, T.f3gen, T.nf3gen, T.f3lean, T.nf3lean, form, 2, err, b->stream),
-       "batched fused pass (lean runs)");
-    ck(cudaStreamWaitEvent(b->stream, b->ev_join, 0), "event");
-    ck(launch_fused3t_batch_split(T.f3, T.f3gen, T.nf3gen, T.f3lean, T.nf3lean, form, 4, err, b->stream),
-       "batched fused pass (general runs, E)");
-    return 2 + (T.nf3lean > 0 ? 1 : 0);
+    if (T.nf3lean > 0) {
+        ck(launch_fused3t_batch_split(T.f3, T.f3gen, T.nf3gen, T.f3lean, T.nf3lean, form, 2, err, b->stream),
+           "batched fused pass (lean runs)");
+        ++k;
+    }
+    if (side) {
+        ck(cudaStreamWaitEvent(b->stream, b->ev_join, 0), "event");
+        if (T.nf3gen > 0) {
+            ck(launch_fused3t_batch_split(T.f3, T.f3gen, T.nf3gen, T.f3lean, T.nf3lean, form, 4, err, b->stream),
+               "batched fused pass (general runs, E)");
+            ++k;
+        }
+        ck(cudaStreamWaitEvent(b->stream, b->ev_mixed, 0), "event");
+    }
+    return k;
 }
 
 // One batched step: H of every grid in one launch, the sources, the dispersive cells and the
@@ -3462,7 +3490,7 @@ template <class R> long long batch_step(omx_batch *b, const BatchTables<R> &T, c
         // the fused pass of every member (dispersive cells and folded plane sources inside), then
         // the work on the sets it wrote: the other sources, the emitter current and q-groups,
         // the detectors
-        k += batch_fused_pass(b, T, b->f3form, b->f3split);
+        k += batch_fused_pass(b, T, b->f3form);
         for (auto *c : b->ctx) c->cur ^= 1;
         for (size_t r = 0; r < T.src.size(); ++r) {
             if (T.nsrc[r] > 0) {
@@ -3558,7 +3586,7 @@ template <class R> void batch_run_impl(omx_batch *b, int tt0, int nsteps, int n_
     if (b->blocks == 0) b->blocks = batch3_blocks<R>();
     // the fused path alternates the members' buffer sets: step s of this call uses T[s & 1]
     const bool f3 = b->fused == 1;
-    std::vector<long long> key = {b->fused, kch, b->f3form, b->f3kch, b->f3split, b->blocks};
+    std::vector<long long> key = {b->fused, kch, b->f3form, b->f3kch, b->f3nsplit, b->blocks};
     for (size_t i = 0; i < b->ctx.size(); ++i) {
         const omx_ctx *c = b->ctx[i];
         key.insert(key.end(), {(long long)c->epoch, c->cur, (long long)(uintptr_t)c->tab.p, plans[i].W,
@@ -3624,9 +3652,10 @@ template <class R> int batch_autotune_impl(omx_batch *b, int reps)
     if (b->blocks == 0) b->blocks = batch3_blocks<R>();
     const int n = (int)b->ctx.size();
     if (b->fused == 1) {
-        // fused batched pass: split x 1000000 + (ring depth x 100 + tile rows) x 1000 + planes
-        // per block (split 1: the pass split by plane form, 0: one k_fused3_batch launch), each
-        // candidate timed over `reps` passes on the zero initial fields (the pass maps them to zero)
+        // fused batched pass: s x 1000000 + (ring depth x 100 + tile rows) x 1000 + planes per
+        // block (the s largest grids in the pass split by plane form, the others in one
+        // k_fused3_batch launch; s among 0, n/4, n/2, n), each candidate timed over `reps` passes
+        // on the zero initial fields (the pass maps them to zero)
         cudaEvent_t e0, e1;
         ck(cudaEventCreate(&e0), "event");
         ck(cudaEventCreate(&e1), "event");
@@ -3636,7 +3665,9 @@ template <class R> int batch_autotune_impl(omx_batch *b, int reps)
         int dev = 0, optin = 0;
         ck(cudaGetDevice(&dev), "device");
         ck(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev), "device");
-        for (int split : {0, 1})
+        std::vector<int> splits = {0, std::max(1, n / 4), std::max(1, n / 2), n};
+        splits.erase(std::unique(splits.begin(), splits.end()), splits.end());
+        for (int split : splits)
             for (int ring : {0, 6, 8})
                 for (int ty : {8, 16})
                     for (int kch : {16, 32, 64, 128}) {
@@ -3644,8 +3675,9 @@ template <class R> int batch_autotune_impl(omx_batch *b, int reps)
                         if (f3t_smem_bytes(form) > optin) continue;
                         b->f3form = form;
                         b->f3kch = kch;
+                        b->f3nsplit = split;
                         const BatchTables<R> T = batch_tables<R>(b, nullptr, kch, 0);
-                        auto once = [&]() { batch_fused_pass(b, T, form, split != 0); };
+                        auto once = [&]() { batch_fused_pass(b, T, form); };
                         once();
                         ck(cudaEventRecord(e0, b->stream), "event");
                         for (int r = 0; r < reps; ++r) once();
@@ -3661,7 +3693,7 @@ template <class R> int batch_autotune_impl(omx_batch *b, int reps)
                     }
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
-        b->f3split = pick >= 1000000;
+        b->f3nsplit = pick / 1000000;
         b->f3form = pick / 1000 % 1000;
         b->f3kch = pick % 1000;
         return pick;
@@ -3747,6 +3779,7 @@ int omx_batch_create(omx_ctx *const *ctxs, int n, omx_batch **out)
     ck(cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming), "event");
     ck(cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming), "event");
     ck(cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming), "event");
+    ck(cudaEventCreateWithFlags(&b->ev_mixed, cudaEventDisableTiming), "event");
     *out = b.release();
     OMX_API_END(nullptr)
 }
@@ -3778,15 +3811,15 @@ int omx_batch_set_launch_shape(omx_batch *b, int shape)
     batch_decide(b);
     if (b->fused == 1) {
         const int form = shape / 1000 % 1000, rows = form % 100, ring = form / 100, kch = shape % 1000;
-        req(shape / 1000000 <= 1 && (rows == 8 || rows == 16) && (ring == 0 || (ring >= 2 && ring <= F3T_RING_MAX)) &&
-                kch >= 1 && kch <= F3T_KMAX,
-            "fused batched shape: split (0 | 1) * 1000000 + ring depth (0 or 2..16) * 100000 + (8 | 16) * 1000 + "
+        req(shape / 1000000 <= (int)b->ctx.size() && (rows == 8 || rows == 16) &&
+                (ring == 0 || (ring >= 2 && ring <= F3T_RING_MAX)) && kch >= 1 && kch <= F3T_KMAX,
+            "fused batched shape: split grids (0..n) * 1000000 + ring depth (0 or 2..16) * 100000 + (8 | 16) * 1000 + "
             "planes (1..128)");
         int dev = 0, optin = 0;
         ck(cudaGetDevice(&dev), "device");
         ck(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev), "device");
         req(f3t_smem_bytes(form) <= optin, "fused batched shape: the ring does not fit in a block's shared memory");
-        b->f3split = shape >= 1000000;
+        b->f3nsplit = shape / 1000000;
         b->f3form = form;
         b->f3kch = kch;
     } else {
@@ -3841,6 +3874,7 @@ int omx_batch_destroy(omx_batch *b)
     if (b->done) cudaEventDestroy(b->done);
     if (b->ev_fork) cudaEventDestroy(b->ev_fork);
     if (b->ev_join) cudaEventDestroy(b->ev_join);
+    if (b->ev_mixed) cudaEventDestroy(b->ev_mixed);
     cudaStream_t s = b->stream, a = b->aux;
     delete b;
     if (s) cudaStreamDestroy(s);

@@ -46,9 +46,9 @@ def test_batch_equals_solo_runs(precision, form, use_graph, autotune):
         fused = precision == "fp32" and form == omx.STEP_DEFAULT
         choice = b.autotune(reps=2)
         if fused:
-            # split x 1000000 + (ring depth x 100 + tile rows) x 1000 + planes per block
+            # split grids x 1000000 + (ring depth x 100 + tile rows) x 1000 + planes per block
             form = choice // 1000 % 1000
-            assert choice // 1000000 in (0, 1) and form % 100 in (8, 16) and form // 100 in (0, 6, 8)
+            assert 0 <= choice // 1000000 <= len(SIZES) and form % 100 in (8, 16) and form // 100 in (0, 6, 8)
             assert choice % 1000 in (16, 32, 64, 128)
         else:
             assert choice in (4, 8, 16, 32)
@@ -67,11 +67,12 @@ def test_batch_equals_solo_runs(precision, form, use_graph, autotune):
         g.kill()
 
 
-@pytest.mark.parametrize("shape", [8064, 1016032, 1608016])
+@pytest.mark.parametrize("shape", [8064, 1016032, 3608016])
 def test_fused_batch_shapes_equal_solo_runs(shape):
-    """FP32 fused batch in a set launch shape: one k_fused3_batch launch (8064), or the pass split
-    by plane form (1016032: tile 32 x 16, 32 planes per lean run; 1608016: ring of 6, tile 32 x 8,
-    16 planes), where the 96^3 grid has lean runs clear of its CPML slabs and the small grids are
+    """FP32 fused batch in a set launch shape: every grid in one k_fused3_batch launch (8064), the
+    largest grid in the pass split by plane form and the others in one launch (1016032: tile
+    32 x 16, 32 planes per lean run), or all three split (3608016: ring of 6, tile 32 x 8, 16
+    planes), where the 96^3 grid has lean runs clear of its CPML slabs and the small grids are
     general runs only; every grid equals its solo run bit for bit."""
     sizes, steps = (96, 36, 29), 50
     solo, batch = [], []
@@ -82,7 +83,7 @@ def test_fused_batch_shapes_equal_solo_runs(shape):
         g.kill()
         batch.append(build(n, 500 + k, "fp32"))
     b = omx.Batch([g for _, g in batch])
-    for bad in (2008064, 8, 16000, 8200):    # split flag 2, a two-pass depth, 0 planes, 200 planes
+    for bad in (4008064, 8, 16000, 8200):    # 4 of 3 grids split, a two-pass depth, 0 planes, 200 planes
         with pytest.raises(omx.OMXError):
             b.set_launch_shape(bad)
     b.set_launch_shape(shape)
