@@ -1874,11 +1874,11 @@ template <class R> int autotune_impl(omx_ctx *c, int reps)
                     if (kch <= c->n[2] * 2 && f3t_smem_bytes(ring * 100 + ty) <= optin)
                         cand.push_back((ring * 100 + ty) * 1000 + kch);
         if (both)
-            for (int m : {4, 8, 16, 32}) cand.push_back(m);
+            for (int m : {1, 2, 4, 8, 16, 32}) cand.push_back(m);
     } else if (fused) {
         cand = {0, 4, 5, 6, 8, 14, 15, 16, 24, 25, 34, 36, 44, 45};
     } else if (c->dims == 3) {
-        cand = {4, 8, 16, 32};
+        cand = {1, 2, 4, 8, 16, 32};
     } else if (c->dims == 2) {
         cand = {8, 16, 32, 64};
     } else {
