@@ -115,6 +115,10 @@ struct SourceRec {
 struct GroupRec {
     omx_qgroup_desc d;
     int npar, nst;
+    // the device arrays hold the emitters sorted by cell (neighbouring threads gather neighbouring
+    // field words, and the current's points, sorted by cell too, read neighbouring dPt_dt rows):
+    // emitter order[d] of the caller's list is device row d, and device row inv[e] is emitter e
+    std::vector<int> order, inv;
     DevBuf<int> ci, cj, ck;
     DevBuf<double> par, rates, rho, E, dipole, dPdt;
     DevBuf<int> win;
@@ -2520,17 +2524,34 @@ int omx_qgroup_create(omx_ctx *c, const omx_qgroup_desc *d, const int32_t *cell,
         cj[e] = ijk[1];
         ckk[e] = ijk[2];
     }
-    G->ci.upload(ci);
-    G->cj.upload(cj);
-    G->ck.upload(ckk);
-    std::vector<double> par(params, params + (size_t)n * G->npar);
+    // device rows sorted by cell (stable: emitters of one cell keep their order); every emitter's
+    // arithmetic is its own, so the order changes no result
+    G->order.resize(n);
+    G->inv.resize(n);
+    for (int e = 0; e < n; ++e) G->order[e] = e;
+    std::stable_sort(G->order.begin(), G->order.end(), [&](int a, int b) {
+        return cell_key(c, ci[a], cj[a], ckk[a]) < cell_key(c, ci[b], cj[b], ckk[b]);
+    });
+    for (int r = 0; r < n; ++r) G->inv[G->order[r]] = r;
+    std::vector<int> di(n), dj(n), dk(n);
+    std::vector<double> par((size_t)n * G->npar);
+    for (int r = 0; r < n; ++r) {
+        const int e = G->order[r];
+        di[r] = ci[e];
+        dj[r] = cj[e];
+        dk[r] = ckk[e];
+        std::copy(params + (size_t)e * G->npar, params + (size_t)(e + 1) * G->npar, par.begin() + (size_t)r * G->npar);
+    }
+    G->ci.upload(di);
+    G->cj.upload(dj);
+    G->ck.upload(dk);
     G->par.upload(par);
     // decay rates 1/T1, 1/T2 (IEEE quotients, the same values the oracle forms every step)
     std::vector<double> rates((size_t)2 * n);
     const int it1 = d->model == OMX_EMITTER_TWO_LEVEL ? 2 : 4;
-    for (int e = 0; e < n; ++e) {
-        rates[2 * e] = 1.0 / par[(size_t)e * G->npar + it1];
-        rates[2 * e + 1] = 1.0 / par[(size_t)e * G->npar + it1 + 1];
+    for (int r = 0; r < n; ++r) {
+        rates[2 * r] = 1.0 / par[(size_t)r * G->npar + it1];
+        rates[2 * r + 1] = 1.0 / par[(size_t)r * G->npar + it1 + 1];
     }
     G->rates.upload(rates);
     G->rho.alloc((size_t)n * G->nst);
@@ -2541,7 +2562,7 @@ int omx_qgroup_create(omx_ctx *c, const omx_qgroup_desc *d, const int32_t *cell,
     if (d->group_type == OMX_Q_MATERIAL) {
         for (int e = 0; e < n; ++e) {
             G->pts.push_back({cell_key(c, ci[e], cj[e], ckk[e]), d->density});
-            G->pts_owner.push_back(e);
+            G->pts_owner.push_back(G->inv[e]);
         }
     } else {
         const int nk = 3;   // q_group_mod.f90:19
@@ -2558,7 +2579,7 @@ int omx_qgroup_create(omx_ctx *c, const omx_qgroup_desc *d, const int32_t *cell,
                             (dims == 3 && (pk < 1 || pk > c->n[2] + 1)))
                             continue;   // outside the reference's J arrays
                         G->pts.push_back({cell_key(c, pi, pj, pk), d->density * mk[(size_t)p]});
-                        G->pts_owner.push_back(e);
+                        G->pts_owner.push_back(G->inv[e]);
                     }
     }
     c->groups.push_back(std::move(G));
@@ -2609,7 +2630,7 @@ int omx_qgroup_attach_closure(omx_ctx *c, int gid, omx_closure *cl, double check
     const int ns = std::max(1, (int)std::floor(check_fraction * n));
     std::vector<int> sub(ns), sub_of(n, -1);
     for (int s = 0; s < ns; ++s) {
-        sub[s] = (int)(((long long)s * n) / ns);    // spread evenly over the group
+        sub[s] = g.inv[(size_t)(((long long)s * n) / ns)];   // spread evenly over the caller's list
         sub_of[sub[s]] = s;
     }
     g.sub.upload(sub);
@@ -2674,10 +2695,19 @@ int omx_qgroup_read(omx_ctx *c, int gid, double *dipole, double *dPdt, double *e
     GroupRec &g = *c->groups[gid];
     ck(cudaStreamSynchronize(c->stream), "sync");
     const size_t n = (size_t)g.d.n_systems;
-    if (dipole) ck(cudaMemcpy(dipole, g.dipole.p, n * 3 * sizeof(double), cudaMemcpyDeviceToHost), "read");
-    if (dPdt) ck(cudaMemcpy(dPdt, g.dPdt.p, n * 3 * sizeof(double), cudaMemcpyDeviceToHost), "read");
-    if (efield) ck(cudaMemcpy(efield, g.E.p, n * 3 * sizeof(double), cudaMemcpyDeviceToHost), "read");
-    if (rho) ck(cudaMemcpy(rho, g.rho.p, n * g.nst * sizeof(double), cudaMemcpyDeviceToHost), "read");
+    // device rows back into the caller's emitter order
+    std::vector<double> tmp;
+    auto get = [&](double *out, const double *dev, int w) {
+        if (!out) return;
+        tmp.resize(n * w);
+        ck(cudaMemcpy(tmp.data(), dev, n * w * sizeof(double), cudaMemcpyDeviceToHost), "read");
+        for (size_t r = 0; r < n; ++r)
+            std::copy(tmp.begin() + r * w, tmp.begin() + (r + 1) * w, out + (size_t)g.order[r] * w);
+    };
+    get(dipole, g.dipole.p, 3);
+    get(dPdt, g.dPdt.p, 3);
+    get(efield, g.E.p, 3);
+    get(rho, g.rho.p, g.nst);
     OMX_API_END(c)
 }
 
@@ -3037,10 +3067,11 @@ int omx_qgroup_write_text(omx_ctx *c, int gid, const char *dir, double time, int
                     "Dipole_y (a.u.)             Dipole_z (a.u.)\n");
     const double au_to_ev = (double)27.2114f;
     for (int e = 0; e < n; ++e) {
-        const double *p = &par[(size_t)e * g.npar], *r = &rho[(size_t)e * g.nst];
+        const size_t q = (size_t)g.inv[e];   // the emitter's device row
+        const double *p = &par[q * g.npar], *r = &rho[q * g.nst];
         const double en = g.d.model == OMX_EMITTER_TWO_LEVEL ? p[0] * r[0] : p[0] * r[0] + p[1] * r[1];
-        std::fprintf(f, "%8d %24.16E %24.16E %24.16E %24.16E\n", e + 1, en * au_to_ev, dip[3 * e], dip[3 * e + 1],
-                     dip[3 * e + 2]);
+        std::fprintf(f, "%8d %24.16E %24.16E %24.16E %24.16E\n", e + 1, en * au_to_ev, dip[3 * q], dip[3 * q + 1],
+                     dip[3 * q + 2]);
     }
     std::fclose(f);
     OMX_API_END(c)
