@@ -3207,8 +3207,8 @@ struct omx_batch {
     DevBuf<unsigned char> dgrid[2], dsrc[2], ddet[2], df3[2];
     DevBuf<int4> df3runs[2];
     cudaEvent_t done = nullptr;   // recorded after a batched call; member streams wait on it
-    // 1: every member steps with one fused pass and the batch runs them in one k_fused3_batch
-    // launch per step; 0: the two half-step passes (k_batch3); -1: not decided yet
+    // 1: every member steps with one fused pass and the batch runs the batched fused pass; 0: the
+    // two half-step passes (k_batch3); -1: not decided yet
     int fused = -1;
     int f3form = 8, f3kch = 64;   // tile rows and planes per block of the fused batched pass
     // the f3nsplit largest grids step with the fused pass split by plane form (their general runs'
@@ -3780,8 +3780,9 @@ template <class R> int batch_autotune_impl(omx_batch *b, int reps)
 }
 
 // The batch's arithmetic, fixed at its first autotune or run: when every member steps with one
-// fused FP32 pass, one k_fused3_batch launch per step; otherwise the two half-step passes
-// (k_batch3), which every member then keeps when used on its own.
+// fused FP32 pass, the batched fused pass (one launch, or split by plane form for the largest
+// grids); otherwise the two half-step passes (k_batch3), which every member then keeps when used
+// on its own.
 void batch_decide(omx_batch *b)
 {
     if (b->fused >= 0) return;
